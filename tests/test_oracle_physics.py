@@ -1,0 +1,77 @@
+"""The reference's simulation tests (test/simulate.jl) run on the CPU oracle.
+
+These are physics-tolerance tests, the same acceptance suite the GPU path
+runs in tests/test_gpu_physics.py.  Julia's RNG stream cannot be reproduced
+here, so the random interface uses a seeded numpy Gaussian of the same
+amplitude.
+"""
+import math
+
+import numpy as np
+import pytest
+
+
+def droplet_expectations(R, th0, th):
+    c0, c1 = math.cos(math.pi * th0), math.cos(math.pi * th)
+    vol = math.pi / 3 * R ** 3 * (2 + c0) * (1 - c0) ** 2
+    R1 = ((R ** 3 * (2 + c0) * (1 - c0) ** 2) / ((2 + c1) * (1 - c1) ** 2)) ** (1 / 3)
+    return vol, math.sin(math.pi * th) * R1
+
+
+def droplet_shape(h, row):
+    drop1d = np.nonzero(h[row, :] > 0.055)[0]
+    droprad = len(drop1d) / 2
+    droph = h.max()
+    vnum = 1 / 6 * math.pi * droph * (3 * droprad ** 2 + droph ** 2)
+    return droprad, vnum
+
+
+def test_random_interface_flattens(orc, golden):
+    # test/simulate.jl:281-286: max - min < 0.1 after 10k steps, θ = 1/9
+    g = golden["simulate"]["random"]
+    L = g["L"]
+    P = orc.params(L, L, Tmax=g["Tmax"], tdump=5000)
+    rng = np.random.default_rng(11)
+    h0 = 1.0 * (1.0 + g["eps"] * rng.standard_normal((L, L)))
+    r = orc.FusedState(P, h0).run(g["Tmax"], theta=1 / 9)
+    assert r.height.max() - r.height.min() < g["bound"]
+
+
+def test_rayleigh_taylor_grows(orc, golden):
+    # test/simulate.jl:297-300: diff[1] < diff[end]
+    g = golden["simulate"]["rayleigh_taylor"]
+    L = g["L"]
+    P = orc.params(L, L, Tmax=g["Tmax"], tdump=500, g=g["g"])
+    i = np.arange(1, L + 1)[:, None]
+    j = np.arange(1, L + 1)[None, :]
+    h0 = 1.0 * (1 + g["eps"] * np.sin(2 * np.pi * g["kx"] * i / (L - 1)) *
+                np.sin(2 * np.pi * g["ky"] * j / (L - 1)))
+    r = orc.FusedState(P, h0).run(g["Tmax"], record_dh=True)
+    assert r.dh[0] < r.dh[-1]
+
+
+def test_droplet_relaxes(orc, golden):
+    # test/simulate.jl:307-325: volume and radius within 10 %, wetted area grows
+    g = golden["simulate"]["droplet"]
+    L, R = g["L"], g["R"]
+    P = orc.params(L, L, Tmax=g["Tmax"], delta=g["delta"])
+    h0 = orc.singledroplet(L, L, R, g["theta0"], (L // 2, L // 2))
+    r = orc.FusedState(P, h0).run(g["Tmax"], callback="wetted")
+    vol, r1 = droplet_expectations(R, g["theta0"], g["theta"])
+    droprad, vnum = droplet_shape(r.height, 74)
+    assert vnum == pytest.approx(vol, abs=vol * g["rtol"])
+    assert droprad == pytest.approx(r1, abs=r1 * g["rtol"])
+    assert r.wet[0] < r.wet[-1]
+
+
+def test_sliding_droplet(orc, golden):
+    # test/simulate.jl:411-420: maximum moves in x only, |u| < 0.1
+    g = golden["simulate"]["sliding"]
+    L, R = g["L"], g["R"]
+    P = orc.params(L, L, Tmax=g["Tmax"], delta=g["delta"])
+    h0 = orc.singledroplet(L, L, R, 1 / 6, (L // 2, L // 2))
+    r = orc.FusedState(P, h0).run(g["Tmax"], callback="inclination",
+                                  incl={"alpha": (g["fx"], 0.0)})
+    ix, iy = np.unravel_index(np.argmax(r.height), r.height.shape)
+    assert ix + 1 != 75 and iy + 1 == 75
+    assert np.all(r.velx < 0.1) and np.all(r.vely < 0.1)
