@@ -1,0 +1,409 @@
+#!/usr/bin/env python3
+"""Throughput of the fused thin-film LBM step on GB300, as one JSON line.
+
+Workload (Rayleigh-Taylor film, 512x512): g = -0.001, γ = 0.0005, θ = 1/9,
+h0 = 1 + U[-0.01, 0.01] (seed 2), the Δh and mass series recorded every
+time step (time_loop(sys, state, Δh), src/simulate.jl:47-67).  The hanging
+film is linearly unstable: from this input the Float64 reference algorithm
+diverges near t = 2300, so one benchmark step is a fresh simulation of 2000
+time steps from h0 (state reset on the device), and the default 25 steps
+add up to the configuration's 50,000 time steps.
+
+  value      device time (CUDA events on the launching stream), inputs
+             resident in HBM, L2 flushed (256 MiB write) between steps
+  e2e        the same work through the reference-facing API with host
+             buffers: state.height = h0 (host), time_loop, height back
+  roofline   the fused step kernel: algorithmic bytes per launch (72 B per
+             lattice update in FP32: 9 reads + 9 writes) over its average
+             launch time, against the measured HBM copy bandwidth
+  cpu_baseline  the oracle (Float64, fused, OpenMP on all host cores) on a
+             bounded sample of the same workload
+
+`--impl reference` times the CPU restatement of the reference algorithm
+(Float64, all host threads) on the same configuration instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "swalbe.jl_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+CHUNK = 2000  # time steps per benchmark step
+B_ALG = {"f64": 144, "f32": 72, "f16": 40}  # bytes per lattice update: 9 reads + 9 writes
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=25)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="f32", choices=["f32", "f16", "f64"])
+    ap.add_argument("--chunk", type=int, default=CHUNK)
+    ap.add_argument("--no-extras", action="store_true", help="skip the 2048² and FP64 side runs")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.lines = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.device)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def load_traffic(kernel_key: str):
+    """Per-launch DRAM bytes of the kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    try:
+        with open(path) as fh:
+            d = json.load(fh)
+        return d.get(kernel_key)
+    except Exception:
+        return None
+
+
+def cpu_baseline(h0, sysc, chunk_steps=1000, chunks=4):
+    """The oracle (Float64, fused, OpenMP) on a bounded sample of the workload."""
+    import oracle
+    oracle.build()
+    p = sysc.param
+    P = oracle.params(sysc.Lx, sysc.Ly, Tmax=chunk_steps, tdump=chunk_steps, tau=p.tau,
+                      gamma=p.gamma, theta=p.theta, g=p.g, delta=p.delta, n=p.n, m=p.m,
+                      hmin=p.hmin, hcrit=p.hcrit)
+    threads = oracle.max_threads()
+    t0 = time.perf_counter()
+    for _ in range(chunks):
+        oracle.FusedState(P, h0).run(chunk_steps, record_dh=True, nthreads=threads)
+    dt = time.perf_counter() - t0
+    lu = sysc.Lx * sysc.Ly * chunk_steps * chunks
+    return {"value": lu / dt / 1e6, "unit": "MLUPS", "cores": threads, "kind": "port",
+            "sample": f"{chunks} x {chunk_steps} time steps of the {sysc.Lx}x{sysc.Ly} workload "
+                      f"from h0, Float64, {dt:.1f} s"}
+
+
+def run_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    import oracle
+    from swalbe_gb300 import configs
+    oracle.build()
+    sysc, h0, _ = configs.rayleigh_taylor_512()
+    p = sysc.param
+    sample_steps = 100
+    P = oracle.params(sysc.Lx, sysc.Ly, Tmax=sample_steps, tdump=sample_steps, tau=p.tau,
+                      gamma=p.gamma, theta=p.theta, g=p.g)
+    threads = oracle.max_threads()
+    for _ in range(args.warmup):
+        oracle.FusedState(P, h0).run(sample_steps, record_dh=True, nthreads=threads)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        oracle.FusedState(P, h0).run(sample_steps, record_dh=True, nthreads=threads)
+        times.append(time.perf_counter() - t0)
+    lu = sysc.Lx * sysc.Ly * sample_steps
+    value = lu * len(times) / sum(times) / 1e6
+    line = {
+        "impl": "reference", "metric": "MLUPS", "value": value, "unit": "MLUPS", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": "rayleigh_taylor_512: 512x512, g=-0.001, gamma=0.0005, theta=1/9, "
+                               "h0=1+U[-0.01,0.01] seed 2",
+                   "sample": f"{sample_steps} time steps from h0 per step"},
+        "cpu_baseline": {"value": value, "unit": "MLUPS", "cores": threads, "kind": "port",
+                         "sample": f"{sample_steps} time steps of 512x512 per step, Float64, "
+                                   "oracle restatement of the Julia reference (Julia is absent)"},
+        "e2e": {"value": value, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def timed_chunks(st, sw, torch, stream, d_h0, d_zero, flush, K, chunk, N):
+    """K benchmark steps; returns (per-step ms list, per-launch kernel ms list)."""
+    step_ms, launch_ms = [], []
+    for _ in range(K):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        k0 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        st.set_device("height", d_h0.data_ptr())
+        st.set_device("velx", d_zero.data_ptr())
+        st.set_device("vely", d_zero.data_ptr())
+        k0.record(stream)
+        st.step(chunk)
+        e1.record(stream)
+        e1.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+        launch_ms.append(k0.elapsed_time(e1) / chunk)
+        st.measures()  # drain the Δh/mass records (outside the events)
+    return step_ms, launch_ms
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    import swalbe_gb300 as sw
+    from swalbe_gb300 import _lib as L
+    from swalbe_gb300 import configs
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    dev = torch.cuda.current_device()
+    sw.build()
+    T = {"f32": np.float32, "f16": np.float16, "f64": np.float64}[args.precision]
+    sysc, h0, total = configs.rayleigh_taylor_512()
+    N = sysc.Lx * sysc.Ly
+    chunk = args.chunk
+    stream = torch.cuda.Stream()
+    st = sw.Sys(sysc, "GB300", T=T)
+    st.set_stream(stream.cuda_stream)
+    st.set_theta(sysc.param.theta)
+    st.set_measures(L.MEAS_MASS | L.MEAS_MAXMIN)
+    d_h0 = torch.from_numpy(np.ascontiguousarray(h0.ravel(order="F"))).to(f"cuda:{dev}")
+    d_zero = torch.zeros(N, dtype=torch.float64, device=f"cuda:{dev}")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{dev}")
+    torch.cuda.synchronize()
+
+    # warm-up (graph capture, clocks)
+    timed_chunks(st, sw, torch, stream, d_h0, d_zero, flush, args.warmup, chunk, N)
+
+    clocks = ClockSampler(dev)
+    clocks.start()
+    n0 = sw.launch_count()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter()
+    step_ms, launch_ms = timed_chunks(st, sw, torch, stream, d_h0, d_zero, flush, args.steps,
+                                      chunk, N)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t_wall
+    if world > 1:
+        torch.distributed.barrier()
+    launches = sw.launch_count() - n0
+    clk = clocks.stop()
+
+    dev_s = sum(step_ms) / 1e3
+    if world > 1:
+        t = torch.tensor([dev_s], device=f"cuda:{dev}", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        dev_s = float(t.item())
+    lu_rank = N * chunk * args.steps
+    value = world * lu_rank / dev_s / 1e6
+
+    # result check: the first chunk against the GPU Float64 path
+    st.set_device("height", d_h0.data_ptr())
+    st.set_device("velx", d_zero.data_ptr())
+    st.set_device("vely", d_zero.data_ptr())
+    st.step(chunk)
+    h_ours = st.height
+    st.measures()
+    ref64 = sw.Sys(sysc, "GB300", T=np.float64)
+    ref64.height = h0
+    ref64.step(chunk)
+    h_ref = ref64.height
+    rel = float(np.linalg.norm(h_ours - h_ref) / np.linalg.norm(h_ref))
+    rel_dev = float(np.linalg.norm(h_ours - h_ref) / np.linalg.norm(h_ref - 1.0))
+    del ref64
+
+    # e2e: reference-facing API with host buffers
+    st.set_stream(None)
+    e2e_sys = sw.SysConst(sysc.Lx, sysc.Ly, sysc.param.replace(Tmax=chunk, tdump=chunk))
+    zeros = np.zeros((sysc.Lx, sysc.Ly))
+    e2e_times = []
+    for k in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        st.height = h0
+        st.velx = zeros
+        st.vely = zeros
+        diff = []
+        sw.time_loop(e2e_sys, st, diff)
+        h_out = st.height
+        dt = time.perf_counter() - t0
+        if k >= args.warmup:
+            e2e_times.append(dt)
+    rb = 8 if args.precision == "f64" else 4
+    e2e_value = world * N * chunk * len(e2e_times) / sum(e2e_times) / 1e6
+
+    hbm, peak_kind = peaks()
+    t_launch = statistics.median(launch_ms) / 1e3
+    alg_bytes = B_ALG[args.precision] * N
+    achieved = alg_bytes / t_launch / 1e9
+    key = f"fused_step_{args.precision}_512"
+    traffic = load_traffic(key)
+
+    extras = {}
+    if not args.no_extras:
+        extras = side_runs(sw, L, np, torch, hbm)
+
+    line = {
+        "metric": "MLUPS", "value": value, "unit": "MLUPS", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": sum(step_ms) / len(step_ms),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": args.precision, "data": "synthetic",
+        "config": {
+            "workload": "rayleigh_taylor_512: 512x512 thin film, g=-0.001, gamma=0.0005, "
+                        "theta=1/9, tau=1, h0=1+U[-0.01,0.01] seed 2; Δh and mass every time step",
+            "time_steps_per_step": chunk, "total_time_steps": chunk * args.steps,
+            "precision": {"f32": "FP32 arithmetic, FP32 populations",
+                          "f16": "FP32 arithmetic, FP32 f0 + FP16 f1..f8",
+                          "f64": "Float64 arithmetic (reference operation order)"}[args.precision],
+            "l2": "flushed between timed steps (256 MiB write); the 512x512 state (19 MB) is "
+                  "L2-resident within a step",
+            "parallelism": "replicas" if world > 1 else "single GPU",
+        },
+        "e2e": {"value": e2e_value, "unit": "MLUPS",
+                "h2d_bytes_per_step": 3 * N * rb,
+                "d2h_bytes_per_step": N * rb + chunk * 56},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": traffic,
+                     "kernel": f"fused_step_kernel<{args.precision}>, 512x512, "
+                               f"{B_ALG[args.precision]} B/LU algorithmic",
+                     "launch_us": t_launch * 1e6, "peak_kind": f"{peak_kind} (hbm_gbs burst)"},
+        "clocks": clk,
+        "wall_s": wall,
+        "check": {"vs": "GPU Float64 path (bit-identical to the oracle)", "after_time_steps": chunk,
+                  "rel_l2_h": rel, "rel_l2_h_minus_1": rel_dev},
+    }
+    line.update(extras)
+    if rank == 0 and world == 1:
+        line["cpu_baseline"] = cpu_baseline(h0, sysc)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def side_runs(sw, L, np, torch, hbm):
+    """HBM-bound 2048² runs (state larger than L2) and the Float64 paths."""
+    out = {}
+    rng = np.random.default_rng(3)
+    n = 2048
+    h0 = np.asfortranarray(1.0 + rng.uniform(-0.1, 0.1, (n, n)))
+    s2 = sw.SysConst(n, n, sw.Taumucs())
+    for prec, T, steps in (("f32", np.float32, 300), ("f16", np.float16, 300), ("f64", np.float64, 30)):
+        st = sw.Sys(s2, "GB300", T=T)
+        stream = torch.cuda.Stream()
+        st.set_stream(stream.cuda_stream)
+        st.height = h0
+        st.step(64)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        st.step(steps)
+        e1.record(stream)
+        e1.synchronize()
+        t = e0.elapsed_time(e1) / 1e3 / steps
+        ach = B_ALG[prec] * n * n / t / 1e9
+        out.setdefault("lattice_2048", {})[prec] = {
+            "MLUPS": n * n / t / 1e6, "launch_us": t * 1e6, "achieved_GBs": ach, "frac": ach / hbm}
+        del st
+    s5 = sw.SysConst(512, 512, sw.Taumucs(g=-0.001, gamma=0.0005))
+    h5 = np.asfortranarray(1.0 + np.random.default_rng(2).uniform(-0.01, 0.01, (512, 512)))
+    for dev_name, steps in (("GB300", 200), ("GB300-plain", 50)):
+        st = sw.Sys(s5, dev_name, T=np.float64)
+        st.height = h5
+        st.step(10)
+        st.sync()
+        t0 = time.perf_counter()
+        st.step(steps)
+        st.sync()
+        dt = time.perf_counter() - t0
+        out.setdefault("fp64_512", {})["fused" if dev_name == "GB300" else "plain"] = {
+            "MLUPS": 512 * 512 * steps / dt / 1e6}
+        del st
+    return out
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

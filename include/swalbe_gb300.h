@@ -1,0 +1,243 @@
+/*
+ * swalbe_gb300.h -- C ABI of the GB300-native thin-film lattice Boltzmann step.
+ *
+ * A drop-in for the time loop of Swalbe.jl.  The reference has no FFI: its
+ * extension point is Julia multiple dispatch on `LBM_state_2D` plus the
+ * `device` string of `Sys` (src/initialize.jl:4, 491-572).  Each entry point
+ * below names the reference function it replaces (paths relative to the
+ * Swalbe.jl project root).  The Julia binding is in
+ * swalbe.jl_gb300/julia/SwalbeGB300.jl, the Python binding in
+ * swalbe.jl_gb300/swalbe_gb300/.
+ *
+ * Conventions
+ *  - Host arrays are Float64, column-major with x (i) fastest, exactly the
+ *    memory of a Julia `Matrix{Float64}(undef, Lx, Ly)`; they are read or
+ *    written only during the call.
+ *  - Every function returns an int status: SWB_OK (0) or a negative error
+ *    class.  No exception crosses the ABI.  swb_last_error() gives the text.
+ *  - A handle owns its device memory and one CUDA stream; it is not
+ *    thread-safe.  Use different handles from different threads.
+ *  - Calls are asynchronous on the handle's stream unless they return host
+ *    data (get_*), which synchronise.
+ */
+#ifndef SWALBE_GB300_H
+#define SWALBE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SWB_ABI_VERSION 1
+
+/* ---- status codes ---- */
+#define SWB_OK 0
+#define SWB_ERR_ARG (-1)         /* invalid argument / size                       */
+#define SWB_ERR_OOM (-2)         /* device allocation failed / over HBM budget     */
+#define SWB_ERR_CUDA (-3)        /* CUDA runtime error (text in swb_last_error)   */
+#define SWB_ERR_NAN (-4)         /* non-finite height detected during a step      */
+#define SWB_ERR_UNSUPPORTED (-5) /* operation not available in this precision mode */
+#define SWB_ERR_CANCELLED (-6)   /* request cancelled                              */
+#define SWB_ERR_NOT_FOUND (-7)   /* unknown request id                             */
+
+/* ---- precision modes ---- */
+#define SWB_F64 0     /* fused step, Float64 arithmetic in the reference's operation order */
+#define SWB_F32 1     /* fused step, FP32 arithmetic and FP32 populations               */
+#define SWB_F16 2     /* fused step, FP32 arithmetic; f0 FP32, f1..f8 FP16 (scaled 2^10) */
+#define SWB_PLAIN64 3 /* one kernel per reference op, Float64, full State arrays        */
+
+/* Taumucs{T} + SysConst{T} (src/initialize.jl:43-60, 76-81).  θ is in
+ * multiples of π as in the reference (cospi(θ), src/pressure.jl:143). */
+typedef struct swb_params {
+    int32_t Lx, Ly;       /* lattice size                                  */
+    int32_t Tmax, tdump;  /* time steps, dump interval                     */
+    double tau, cs, mu;   /* relaxation time, sound speed, kinematic visc.  */
+    double delta, kbt;    /* slip length, thermal energy (must be 0)        */
+    double gamma;         /* surface tension                                */
+    int32_t n, m;         /* disjoining-pressure exponents                  */
+    double hmin, hcrit;   /* Π(hmin) = 0, stabiliser                        */
+    double theta, g;      /* contact angle (units of π), gravity            */
+} swb_params;
+
+/* Fields of a state (the arrays of `State`, src/initialize.jl:149-168). */
+#define SWB_FIELD_HEIGHT 0
+#define SWB_FIELD_VELX 1
+#define SWB_FIELD_VELY 2
+#define SWB_FIELD_PRESSURE 3 /* fused modes: film pressure of the current height */
+#define SWB_FIELD_FOUT 4     /* Lx*Ly*9, the streamed populations (fout == ftemp) */
+#define SWB_FIELD_FEQ 5      /* PLAIN64 only */
+#define SWB_FIELD_FX 6       /* PLAIN64 only */
+#define SWB_FIELD_FY 7       /* PLAIN64 only */
+#define SWB_FIELD_SLIPX 8    /* PLAIN64 only */
+#define SWB_FIELD_SLIPY 9    /* PLAIN64 only */
+#define SWB_FIELD_HGRADPX 10 /* PLAIN64 only: h∇px */
+#define SWB_FIELD_HGRADPY 11 /* PLAIN64 only: h∇py */
+#define SWB_FIELD_VSQ 12     /* PLAIN64 only */
+
+/* Per-step measures, recorded for time_loop iteration t on the height at
+ * the start of that iteration -- where the reference takes them:
+ * mass = sum(height) (src/simulate.jl:10), wetted = count(h > hthresh)
+ * (src/measures.jl:13-17), hmax - hmin (src/simulate.jl:56), and the
+ * liquid-vapour area of surfacearea! (src/measures.jl:126-168). */
+#define SWB_MEAS_MASS 1
+#define SWB_MEAS_WETTED 2
+#define SWB_MEAS_MAXMIN 4
+#define SWB_MEAS_AREA 8
+#define SWB_MEAS_ALL 15
+
+typedef struct swb_measure {
+    int64_t t;       /* time_loop iteration (1-based)                     */
+    double mass;     /* Σ h (FP64 accumulation in every precision mode)   */
+    int64_t wetted;  /* #{h > hthresh}                                    */
+    double hmax;     /* maximum(h)                                        */
+    double hmin;     /* minimum(h)                                        */
+    double area;     /* Σ_{h>hthresh} sqrt(1 + |∇h|²)                     */
+    double energy;   /* area - Σ_{h>hthresh} cospi(θ)                      */
+} swb_measure;
+
+typedef struct swb_state swb_state;
+
+/* ---------------------------------------------------------------------- */
+/* Library                                                                 */
+/* ---------------------------------------------------------------------- */
+int swb_abi_version(void);
+/* Text of the most recent error on this thread (state may be NULL). */
+const char *swb_last_error(const swb_state *s);
+const char *swb_status_string(int status);
+/* Device memory a state of this size and mode needs, in bytes. */
+int swb_state_bytes(const swb_params *p, int precision, size_t *bytes);
+
+/* ---------------------------------------------------------------------- */
+/* One simulation                                                          */
+/* ---------------------------------------------------------------------- */
+/* Sys(sysc, device; T) (src/initialize.jl:491-536): zero populations,
+ * height = 1, velocities 0. */
+int swb_create(const swb_params *p, int precision, swb_state **out);
+int swb_destroy(swb_state *s);
+int swb_get_params(const swb_state *s, swb_params *p, int *precision);
+
+/* state.<field> .= values (host, column-major Float64).  Setting height or
+ * a velocity makes the next step start from the fields, as the reference's
+ * time_loop does after `state.height .= ...` (src/simulate.jl:240-242,
+ * 384-397); the populations are kept (they are the reference's ftemp). */
+int swb_set_field(swb_state *s, int field, const double *host);
+/* Copies a field to the host (synchronises).  SWB_FIELD_FOUT is Lx*Ly*9. */
+int swb_get_field(swb_state *s, int field, double *host);
+/* As swb_set_field, from a Float64 column-major DEVICE array (e.g. the
+ * memory of a CUDA.jl CuArray); asynchronous on the state's stream. */
+int swb_set_field_device(swb_state *s, int field, const double *device_ptr);
+
+/* Runs the state's work on `stream` (a cudaStream_t owned by the caller,
+ * e.g. CUDA.jl's task stream); NULL returns to the state's own stream. */
+int swb_set_stream(swb_state *s, void *stream);
+int swb_get_stream(swb_state *s, void **stream);
+/* Kernel launches issued by this library since load (all handles). */
+int swb_launch_count(uint64_t *count);
+
+/* θ for filmpressure!(state, sys; θ) (src/pressure.jl:119-147):
+ *   set_theta       -- scalar θ (time_loop(sys, state, θ::Number));
+ *   set_theta_field -- θ::Matrix (time_loop(sys, state, θ), src/simulate.jl:26-45);
+ *   set_theta_wave  -- θ(x,t) = θ0 + Δθ·sin(2π(x - v t)/Lx), x = i-1, t the
+ *                      time_loop iteration (moving wettability,
+ *                      scripts/Moving_wettability_structs.jl:139-152 does a
+ *                      discrete shift of such a pattern). */
+int swb_set_theta(swb_state *s, double theta);
+int swb_set_theta_field(swb_state *s, const double *theta);
+int swb_set_theta_wave(swb_state *s, double theta0, double dtheta, double v);
+
+/* inclination!(α, state; t, tstart, tsmooth) as the time_loop callback
+ * (src/forcing.jl:363-368, src/simulate.jl:89).  loop_time = 0 uses the
+ * fixed `t` (the callback's default 1000); loop_time = 1 uses the
+ * iteration.  ax = ay = 0 switches it off. */
+int swb_set_inclination(swb_state *s, double ax, double ay, int loop_time, int64_t t,
+                        int64_t tstart, int64_t tsmooth);
+
+/* Which measures swb_step records each iteration (SWB_MEAS_* mask). */
+int swb_set_measures(swb_state *s, int mask, double hthresh);
+
+/* `nsteps` iterations of the time_loop body (src/simulate.jl:15-22):
+ * filmpressure!, h∇p!, slippage!, forces, equilibrium!, BGKandStream!,
+ * moments!.  Asynchronous.  SWB_ERR_NAN is reported by the next
+ * synchronising call after a non-finite height was seen. */
+int swb_step(swb_state *s, int64_t nsteps);
+int swb_sync(swb_state *s);
+/* Number of iterations completed since swb_create. */
+int swb_steps_done(swb_state *s, int64_t *t);
+/* Drains the per-step measures recorded since the last call (oldest
+ * first); at most `cap` records (capacity of the device ring: 65536). */
+int swb_get_measures(swb_state *s, swb_measure *out, int64_t cap, int64_t *count);
+/* Measures of the current height now (mass, wetted, max/min, area). */
+int swb_measure_now(swb_state *s, double hthresh, swb_measure *out);
+
+/* ---------------------------------------------------------------------- */
+/* Per-op API, SWB_PLAIN64 only: one kernel per reference op on the full   */
+/* State arrays, same Float64 operation order.                             */
+/* ---------------------------------------------------------------------- */
+int swb_op_filmpressure(swb_state *s);          /* src/pressure.jl:119-155 (uses the θ set) */
+int swb_op_hgradp(swb_state *s);                /* src/forcing.jl:168-187 */
+int swb_op_slippage(swb_state *s);              /* src/forcing.jl:42-56 */
+int swb_op_force_sum(swb_state *s);             /* src/simulate.jl:18-19 */
+int swb_op_inclination(swb_state *s, double ax, double ay, int64_t t, int64_t tstart,
+                       int64_t tsmooth);        /* src/forcing.jl:363-368 */
+int swb_op_equilibrium(swb_state *s);           /* src/equilibrium.jl:63-119 */
+int swb_op_bgk_stream(swb_state *s);            /* src/collide.jl:261-296, 342-343 */
+int swb_op_moments(swb_state *s);               /* src/moments.jl:43-64 */
+
+/* ---------------------------------------------------------------------- */
+/* Batched ensemble: many lattices of uneven size and parameters advanced  */
+/* together by one launch per step over a packed tile table.  Replaces a   */
+/* loop of independent `run_*` simulations (src/simulate.jl:236-503).      */
+/* ---------------------------------------------------------------------- */
+typedef struct swb_batch swb_batch;
+int swb_batch_create(const swb_params *params, int count, int precision, swb_batch **out);
+int swb_batch_destroy(swb_batch *b);
+int swb_batch_set_height(swb_batch *b, int idx, const double *host);
+int swb_batch_get_height(swb_batch *b, int idx, double *host);
+int swb_batch_set_theta_wave(swb_batch *b, int idx, double theta0, double dtheta, double v);
+int swb_batch_step(swb_batch *b, int64_t nsteps);
+int swb_batch_sync(swb_batch *b);
+/* Tile shape chosen by the autotuner (0 until the first step). */
+int swb_batch_tile(swb_batch *b, int *tile_x, int *tile_y, int *steps_per_graph);
+
+/* ---------------------------------------------------------------------- */
+/* Serving: a request loop with HBM-footprint admission and continuous     */
+/* batching of resident simulations.                                       */
+/* ---------------------------------------------------------------------- */
+typedef struct swb_server swb_server;
+typedef struct swb_request_info {
+    int64_t id;
+    int32_t status;        /* 0 queued, 1 running, 2 done, <0 error        */
+    int64_t steps_done;
+    double t_submit;       /* seconds on the server's clock                */
+    double t_admit;
+    double t_done;
+} swb_request_info;
+typedef struct swb_server_stats {
+    int64_t submitted, admitted, completed, rejected;
+    int64_t queued, running;
+    double lattice_updates; /* total lattice updates served              */
+    double busy_seconds;    /* time with at least one resident request   */
+    size_t hbm_in_use, hbm_budget;
+    int64_t ticks;
+} swb_server_stats;
+
+/* hbm_budget: bytes of device memory the resident states may use.
+ * steps_per_tick: time steps run per scheduling tick. */
+int swb_server_create(size_t hbm_budget, int precision, int steps_per_tick, swb_server **out);
+int swb_server_destroy(swb_server *sv);
+/* Queues a solve: params (Lx, Ly, γ, θ, g, ...), initial height (copied),
+ * moving wettability (dtheta = 0 for none) and the step count. */
+int swb_server_submit(swb_server *sv, const swb_params *p, const double *h0, double theta0,
+                      double dtheta, double v, int64_t nsteps, int64_t *id);
+/* 1 if done (height copied to h_out when not NULL), 0 if not yet. */
+int swb_server_poll(swb_server *sv, int64_t id, double *h_out, swb_request_info *info);
+int swb_server_cancel(swb_server *sv, int64_t id);
+int swb_server_stats_get(swb_server *sv, swb_server_stats *st);
+double swb_server_clock(swb_server *sv);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SWALBE_GB300_H */

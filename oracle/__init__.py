@@ -359,3 +359,41 @@ class FusedState:
 
 def max_threads() -> int:
     return int(lib().orc_max_threads())
+
+
+class LiteralState:
+    """A literal-oracle `State` that can be stepped in chunks and edited between
+    chunks, like a Julia user script does (src/initialize.jl:491-508)."""
+
+    _IDS = {"fout": 0, "ftemp": 1, "feq": 2, "height": 3, "velx": 4, "vely": 5, "vsq": 6,
+            "pressure": 7, "Fx": 8, "Fy": 9, "slipx": 10, "slipy": 11, "h∇px": 12, "h∇py": 13}
+
+    def __init__(self, P: Params):
+        self.P = P
+        self._s = lib().orc_state_new(P.Lx, P.Ly)
+
+    def __del__(self):
+        if getattr(self, "_s", None):
+            lib().orc_state_free(self._s)
+            self._s = None
+
+    def field(self, name) -> np.ndarray:
+        n9 = name in ("fout", "ftemp", "feq")
+        shape = (self.P.Lx, self.P.Ly) + ((9,) if n9 else ())
+        ptr = lib().orc_state_field(self._s, self._IDS[name])
+        n = int(np.prod(shape))
+        return np.ctypeslib.as_array((C.c_double * n).from_address(ptr)).reshape(shape, order="F")
+
+    def run(self, steps, *, theta_field=None, theta=None, record_dh=False, callback=None,
+            hthresh=0.055, incl=None) -> LoopResult:
+        P = self.P
+        o, tf = _opts(theta_field, P.theta if theta is None else theta, record_dh, callback,
+                      hthresh, incl)
+        mass = np.full(steps, np.nan)
+        dh = np.zeros(steps) if record_dh else None
+        wet = np.zeros(steps, dtype=np.int64) if callback == "wetted" else None
+        out = LoopOut(mass.ctypes.data, None if dh is None else dh.ctypes.data,
+                      None if wet is None else wet.ctypes.data)
+        lib().orc_time_loop(self._s, C.byref(P), steps, C.byref(o), C.byref(out))
+        return LoopResult(self.field("height").copy(order="F"), self.field("velx").copy(order="F"),
+                          self.field("vely").copy(order="F"), mass, dh, wet)

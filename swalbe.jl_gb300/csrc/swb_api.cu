@@ -1,0 +1,927 @@
+// swb_api.cu -- host side of the C ABI (include/swalbe_gb300.h).
+//
+// A swb_state mirrors one `State` of the reference (src/initialize.jl:149-168):
+// it owns the device buffers of one lattice and a CUDA stream.  Time steps
+// are launched asynchronously; repeated launches are captured once into a
+// CUDA graph and replayed (the step counter lives on the device, so the
+// same graph serves every chunk of steps).
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include <cuda_fp16.h>
+
+#include "swb_internal.h"
+
+using swb::Control;
+using swb::PlainState;
+using swb::Record;
+using swb::StepArgs;
+using swb::TileRef;
+
+// ------------------------------------------------------------------ errors
+namespace {
+thread_local std::string g_err;
+
+int fail(std::string *slot, int code, const std::string &msg) {
+    g_err = msg;
+    if (slot) *slot = msg;
+    return code;
+}
+
+#define CUDA_TRY(slot, expr)                                                              \
+    do {                                                                                  \
+        cudaError_t e_ = (expr);                                                          \
+        if (e_ != cudaSuccess)                                                            \
+            return fail(slot, e_ == cudaErrorMemoryAllocation ? SWB_ERR_OOM : SWB_ERR_CUDA, \
+                        std::string(#expr) + ": " + cudaGetErrorString(e_));              \
+    } while (0)
+
+// cos(πx): exact at multiples of 1/2 (like Julia's Base.cospi), otherwise
+// the argument is reduced exactly modulo 2 and cos evaluated in long double,
+// then rounded once.
+double host_cospi(double x) {
+    if (!std::isfinite(x)) return NAN;
+    double r = std::fmod(std::fabs(x), 2.0);
+    if (r == 0.0) return 1.0;
+    if (r == 1.0) return -1.0;
+    if (r == 0.5 || r == 1.5) return 0.0;
+    const long double PI_L = 3.141592653589793238462643383279502884L;
+    return (double)cosl(PI_L * (long double)r);
+}
+
+// ((1 - cospi θ)(n-1)(m-1)) / ((n-m) hmin), left to right (src/pressure.jl:141-147)
+double host_kappa(double theta, int n, int m, double hmin) {
+    double a = 1.0 - host_cospi(theta);
+    a = a * (double)(n - 1);
+    a = a * (double)(m - 1);
+    return a / ((double)(n - m) * hmin);
+}
+
+double incl_factor(long long t, long long tstart, long long tsmooth) {
+    return 0.5 + 0.5 * std::tanh((double)(t - tstart) / (double)tsmooth);
+}
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+int real_bytes(int precision) { return precision == SWB_F64 || precision == SWB_PLAIN64 ? 8 : 4; }
+
+// Population buffer bytes for `pitch` cells.
+size_t fbuf_bytes(int precision, long long pitch) {
+    switch (precision) {
+        case SWB_F64: return (size_t)9 * pitch * 8;
+        case SWB_F32: return (size_t)9 * pitch * 4;
+        case SWB_F16: return (size_t)pitch * 4 + (size_t)8 * pitch * 2;
+        default: return 0;
+    }
+}
+
+long long pitch_of(long long N) { return (N + 63) / 64 * 64; }
+
+int check_params(const swb_params *p, std::string *slot) {
+    if (!p) return fail(slot, SWB_ERR_ARG, "params is NULL");
+    if (p->Lx < 1 || p->Ly < 1) return fail(slot, SWB_ERR_ARG, "Lx and Ly must be >= 1");
+    if ((long long)p->Lx * p->Ly * 9 >= (1LL << 31))
+        return fail(slot, SWB_ERR_ARG, "lattice too large: Lx*Ly*9 must be < 2^31");
+    if (!(p->tau > 0.0)) return fail(slot, SWB_ERR_ARG, "tau must be > 0");
+    if (p->n <= p->m || p->m < 1) return fail(slot, SWB_ERR_ARG, "need n > m >= 1");
+    if (!(p->hmin > 0.0)) return fail(slot, SWB_ERR_ARG, "hmin must be > 0");
+    if (p->kbt != 0.0)
+        return fail(slot, SWB_ERR_UNSUPPORTED, "thermal fluctuations (kbt != 0) are not supported");
+    return SWB_OK;
+}
+
+// Static parts of the step arguments from the parameters.
+void fill_args_from_params(StepArgs &a, const swb_params &p) {
+    a.Lx = p.Lx;
+    a.Ly = p.Ly;
+    a.gamma = p.gamma;
+    a.hmin = p.hmin;
+    a.hcrit = p.hcrit;
+    a.delta = p.delta;
+    a.mu = p.mu;
+    a.g = p.g;
+    a.invtau = 1.0 / p.tau;
+    a.omeg = 1.0 - 1.0 / p.tau;
+    a.tau_is_one = (p.tau == 1.0);
+    a.n = p.n;
+    a.m = p.m;
+    a.theta_mode = swb::THETA_SCALAR;
+    a.kap = host_kappa(p.theta, p.n, p.m, p.hmin);
+    a.cos_theta = host_cospi(p.theta);
+    a.tiles_x = (p.Lx + swb::kTX - 1) / swb::kTX;
+    a.tiles_y = (p.Ly + swb::kTY - 1) / swb::kTY;
+    a.hthresh = 0.055;
+}
+
+__global__ void fill_kernel(double *d, long long n, double v) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        d[i] = v;
+}
+__global__ void fill_kernel_f(float *d, long long n, float v) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        d[i] = v;
+}
+// Inverse of the pull fout_q(x) = fpost_q(x - c_q): fpost_q(x - c_q) = fout_q(x).
+template <class T>
+__global__ void push_kernel(const double *fout, void *fpost, int Lx, int Ly, long long pitch,
+                            int precision) {
+    const int CX[9] = {0, 1, 0, -1, 0, 1, -1, -1, 1};
+    const int CY[9] = {0, 0, 1, 0, -1, 1, 1, -1, -1};
+    const long long N = (long long)Lx * Ly;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < N;
+         c += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(c % Lx), j = (int)(c / Lx);
+        for (int q = 0; q < 9; ++q) {
+            int di = i - CX[q], dj = j - CY[q];
+            di = (di % Lx + Lx) % Lx;
+            dj = (dj % Ly + Ly) % Ly;
+            const double v = fout[q * N + c];
+            const long long d = (long long)dj * Lx + di;
+            if (precision == SWB_F64) {
+                ((double *)fpost)[q * pitch + d] = v;
+            } else if (precision == SWB_F32) {
+                ((float *)fpost)[q * pitch + d] = (float)v;
+            } else {
+                if (q == 0)
+                    ((float *)fpost)[d] = (float)v;
+                else
+                    ((__half *)((float *)fpost + pitch))[(q - 1) * pitch + d] =
+                        __float2half_rn((float)v * 1024.0f);
+            }
+        }
+    }
+}
+
+int blocks_for(long long n) {
+    long long b = (n + 255) / 256;
+    if (b > 4096) b = 4096;
+    return (int)(b < 1 ? 1 : b);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ dispatch
+namespace swb {
+void set_global_error(const char *msg) { g_err = msg; }
+static std::atomic<unsigned long long> g_launches{0};
+void count_launches(unsigned long long n) { g_launches += n; }
+
+cudaError_t launch_fused_step(int precision, const StepArgs &a, cudaStream_t st) {
+    count_launches(1);
+    return precision == SWB_F64 ? launch_fused_step_f64(a, st) : launch_fused_step_f32(precision, a, st);
+}
+cudaError_t launch_moments(int precision, const StepArgs &a, cudaStream_t st) {
+    count_launches(1);
+    return precision == SWB_F64 ? launch_moments_f64(a, st) : launch_moments_f32(precision, a, st);
+}
+cudaError_t launch_fout(int precision, const StepArgs &a, double *out, cudaStream_t st) {
+    count_launches(1);
+    return precision == SWB_F64 ? launch_fout_f64(a, out, st) : launch_fout_f32(precision, a, out, st);
+}
+cudaError_t launch_pressure_now(int precision, const StepArgs &a, double *out, cudaStream_t st) {
+    count_launches(1);
+    return precision == SWB_F64 ? launch_pressure_now_f64(a, out, st)
+                                : launch_pressure_now_f32(precision, a, out, st);
+}
+cudaError_t launch_batch_step(int precision, const StepArgs *d_args, const TileRef *d_tiles,
+                              int ntiles, int grid, cudaStream_t st) {
+    count_launches(1);
+    return precision == SWB_F64 ? launch_batch_step_f64(d_args, d_tiles, ntiles, grid, st)
+                                : launch_batch_step_f32(precision, d_args, d_tiles, ntiles, grid, st);
+}
+int batch_blocks_per_sm(int precision) {
+    return precision == SWB_F64 ? batch_blocks_per_sm_f64() : batch_blocks_per_sm_f32(precision);
+}
+}  // namespace swb
+
+// ------------------------------------------------------------------ state
+struct swb_state {
+    swb_params p{};
+    int precision = 0;
+    long long N = 0, pitch = 0;
+    cudaStream_t stream = nullptr;
+    cudaStream_t own_stream = nullptr;  // the state's own stream
+    std::vector<void *> allocs;
+    StepArgs a{};
+    PlainState ps{};
+    double *plain_kapF = nullptr;
+    // measures
+    Record *rec = nullptr;     // ring of kRecCap
+    Record *mrec = nullptr;    // slot for swb_measure_now
+    double *mscratch = nullptr;
+    unsigned int *mticket = nullptr;
+    long long rec_read = 0;    // records consumed by the host
+    long long plain_rec_head = 0;
+    int plain_meas_mask = 0;
+    // host mirrors
+    long long steps = 0;
+    bool host_fresh = true;      // next step starts from the fields
+    bool fields_current = true;  // fields equal the moments of the populations
+    // inclination for the plain path
+    int incl = 0, incl_loop_time = 0;
+    double ax = 0, ay = 0;
+    long long incl_t = 1000, incl_tstart = 0, incl_tsmooth = 1;
+    // graph cache
+    cudaGraphExec_t gexec = nullptr;
+    int gsteps = 0;
+    bool gvalid = false;
+    double *dtmp = nullptr;
+    size_t dtmp_bytes = 0;
+    std::string err;
+
+    int rb() const { return real_bytes(precision); }
+    bool plain() const { return precision == SWB_PLAIN64; }
+
+    cudaError_t alloc(void **ptr, size_t bytes) {
+        cudaError_t e = cudaMalloc(ptr, bytes);
+        if (e == cudaSuccess) allocs.push_back(*ptr);
+        return e;
+    }
+    void invalidate_graph() {
+        if (gexec) cudaGraphExecDestroy(gexec);
+        gexec = nullptr;
+        gvalid = false;
+    }
+    ~swb_state() {
+        invalidate_graph();
+        if (stream) cudaStreamSynchronize(stream);
+        if (own_stream) cudaStreamSynchronize(own_stream);
+        for (void *q : allocs) cudaFree(q);
+        if (own_stream) cudaStreamDestroy(own_stream);
+    }
+};
+
+namespace {
+
+int ensure_tmp(swb_state *s, size_t bytes) {
+    if (s->dtmp_bytes >= bytes) return SWB_OK;
+    if (s->dtmp) {
+        cudaFree(s->dtmp);
+        for (auto &q : s->allocs)
+            if (q == s->dtmp) q = nullptr;
+    }
+    s->dtmp = nullptr;
+    s->dtmp_bytes = 0;
+    CUDA_TRY(&s->err, s->alloc((void **)&s->dtmp, bytes));
+    s->dtmp_bytes = bytes;
+    return SWB_OK;
+}
+
+// Host Float64 column-major -> device field of the compute type.
+int upload_field(swb_state *s, void *dst, const double *host, long long n) {
+    if (s->rb() == 8) {
+        CUDA_TRY(&s->err, cudaMemcpyAsync(dst, host, n * 8, cudaMemcpyHostToDevice, s->stream));
+        CUDA_TRY(&s->err, cudaStreamSynchronize(s->stream));
+    } else {
+        std::vector<float> tmp(n);
+        for (long long i = 0; i < n; ++i) tmp[i] = (float)host[i];
+        CUDA_TRY(&s->err, cudaMemcpyAsync(dst, tmp.data(), n * 4, cudaMemcpyHostToDevice, s->stream));
+        CUDA_TRY(&s->err, cudaStreamSynchronize(s->stream));
+    }
+    return SWB_OK;
+}
+
+int download_field(swb_state *s, const void *src, double *host, long long n, int bytes) {
+    if (bytes == 8) {
+        CUDA_TRY(&s->err, cudaMemcpyAsync(host, src, n * 8, cudaMemcpyDeviceToHost, s->stream));
+        CUDA_TRY(&s->err, cudaStreamSynchronize(s->stream));
+    } else {
+        std::vector<float> tmp(n);
+        CUDA_TRY(&s->err, cudaMemcpyAsync(tmp.data(), src, n * 4, cudaMemcpyDeviceToHost, s->stream));
+        CUDA_TRY(&s->err, cudaStreamSynchronize(s->stream));
+        for (long long i = 0; i < n; ++i) host[i] = (double)tmp[i];
+    }
+    return SWB_OK;
+}
+
+// Fields <- moments of the populations (only needed after steps).
+int materialize(swb_state *s) {
+    if (s->plain() || s->host_fresh || s->fields_current) return SWB_OK;
+    CUDA_TRY(&s->err, swb::launch_moments(s->precision, s->a, s->stream));
+    s->fields_current = true;
+    return SWB_OK;
+}
+
+__global__ void set_fresh_kernel(Control *c) { c->fresh = 1; }
+__global__ void d2f_kernel(const double *src, float *dst, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        dst[i] = (float)src[i];
+}
+
+int set_fresh(swb_state *s) {
+    set_fresh_kernel<<<1, 1, 0, s->stream>>>(s->a.ctl);
+    swb::count_launches(1);
+    CUDA_TRY(&s->err, cudaGetLastError());
+    s->host_fresh = true;
+    s->fields_current = true;
+    return SWB_OK;
+}
+
+int check_nan(swb_state *s) {
+    int flag = 0;
+    if (s->plain()) return SWB_OK;
+    CUDA_TRY(&s->err, cudaMemcpyAsync(&flag, &s->a.ctl->nan_flag, sizeof(int),
+                                      cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(&s->err, cudaStreamSynchronize(s->stream));
+    if (flag) return fail(&s->err, SWB_ERR_NAN, "non-finite height detected during a step");
+    return SWB_OK;
+}
+
+// One plain iteration: the reference's op sequence, one kernel per op.
+int plain_iteration(swb_state *s) {
+    const long long t = s->steps + 1;
+    const swb_params &p = s->p;
+    PlainState &ps = s->ps;
+    if (s->plain_meas_mask) {
+        CUDA_TRY(&s->err, swb::launch_measure(ps.h, 1, p.Lx, p.Ly, s->a.hthresh, nullptr,
+                                              s->a.cos_theta, s->mscratch, s->mticket,
+                                              s->rec + (t - 1) % swb::kRecCap, t, s->stream));
+        s->plain_rec_head++;
+    }
+    const bool field = s->a.theta_mode == swb::THETA_FIELD;
+    CUDA_TRY(&s->err, swb::plain_filmpressure(ps, field ? s->plain_kapF : nullptr, s->a.kap,
+                                              p.gamma, p.n, p.m, p.hmin, p.hcrit, s->stream));
+    CUDA_TRY(&s->err, swb::plain_hgradp(ps, s->stream));
+    CUDA_TRY(&s->err, swb::plain_slippage(ps, p.delta, p.mu, s->stream));
+    CUDA_TRY(&s->err, swb::plain_force_sum(ps, s->stream));
+    if (s->incl) {
+        const double fac = incl_factor(s->incl_loop_time ? t : s->incl_t, s->incl_tstart,
+                                       s->incl_tsmooth);
+        CUDA_TRY(&s->err, swb::plain_inclination(ps, s->ax, s->ay, fac, s->stream));
+    }
+    CUDA_TRY(&s->err, swb::plain_equilibrium(ps, p.g, s->stream));
+    CUDA_TRY(&s->err, swb::plain_collide(ps, 1.0 - 1.0 / p.tau, 1.0 / p.tau, s->stream));
+    CUDA_TRY(&s->err, swb::plain_stream(ps, s->stream));
+    CUDA_TRY(&s->err, swb::plain_moments(ps, s->stream));
+    s->steps++;
+    return SWB_OK;
+}
+
+constexpr int kGraphSteps = 64;
+
+int fused_steps(swb_state *s, long long nsteps) {
+    long long left = nsteps;
+    if (left >= kGraphSteps) {
+        if (!s->gvalid) {
+            cudaGraph_t g = nullptr;
+            CUDA_TRY(&s->err, cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+            cudaError_t le = cudaSuccess;
+            for (int k = 0; k < kGraphSteps && le == cudaSuccess; ++k)
+                le = swb::launch_fused_step(s->precision, s->a, s->stream);
+            swb::count_launches(0ULL - (unsigned long long)kGraphSteps);  // captured, not run
+            cudaError_t ce = cudaStreamEndCapture(s->stream, &g);
+            if (le != cudaSuccess) {
+                if (g) cudaGraphDestroy(g);
+                return fail(&s->err, SWB_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(le));
+            }
+            CUDA_TRY(&s->err, ce);
+            cudaError_t ie = cudaGraphInstantiate(&s->gexec, g, 0);
+            cudaGraphDestroy(g);
+            CUDA_TRY(&s->err, ie);
+            s->gvalid = true;
+            s->gsteps = kGraphSteps;
+        }
+        while (left >= s->gsteps) {
+            CUDA_TRY(&s->err, cudaGraphLaunch(s->gexec, s->stream));
+            swb::count_launches(s->gsteps);
+            left -= s->gsteps;
+        }
+    }
+    for (; left > 0; --left) CUDA_TRY(&s->err, swb::launch_fused_step(s->precision, s->a, s->stream));
+    s->steps += nsteps;
+    if (nsteps > 0) {
+        s->host_fresh = false;
+        s->fields_current = false;
+    }
+    return SWB_OK;
+}
+
+void record_to_measure(const Record &r, swb_measure *m) {
+    m->t = r.t;
+    m->mass = r.mass;
+    m->wetted = (int64_t)r.wetted;
+    m->hmax = r.hmax;
+    m->hmin = r.hmin;
+    m->area = r.area;
+    m->energy = r.area - r.cos_sum;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ ABI
+extern "C" {
+
+int swb_abi_version(void) { return SWB_ABI_VERSION; }
+
+const char *swb_last_error(const swb_state *s) {
+    if (s && !s->err.empty()) return s->err.c_str();
+    return g_err.c_str();
+}
+
+const char *swb_status_string(int st) {
+    switch (st) {
+        case SWB_OK: return "ok";
+        case SWB_ERR_ARG: return "invalid argument";
+        case SWB_ERR_OOM: return "out of device memory";
+        case SWB_ERR_CUDA: return "CUDA error";
+        case SWB_ERR_NAN: return "non-finite height";
+        case SWB_ERR_UNSUPPORTED: return "unsupported in this mode";
+        case SWB_ERR_CANCELLED: return "cancelled";
+        case SWB_ERR_NOT_FOUND: return "not found";
+        default: return "unknown status";
+    }
+}
+
+int swb_state_bytes(const swb_params *p, int precision, size_t *bytes) {
+    int rc = check_params(p, nullptr);
+    if (rc) return rc;
+    if (!bytes) return fail(nullptr, SWB_ERR_ARG, "bytes is NULL");
+    const long long N = (long long)p->Lx * p->Ly, pitch = pitch_of(N);
+    const long long tiles = (long long)((p->Lx + swb::kTX - 1) / swb::kTX) * ((p->Ly + swb::kTY - 1) / swb::kTY);
+    size_t b = 0;
+    if (precision == SWB_PLAIN64) {
+        b = align256((size_t)27 * N * 8) + 11 * align256((size_t)N * 8);
+    } else if (precision == SWB_F64 || precision == SWB_F32 || precision == SWB_F16) {
+        b = 2 * align256(fbuf_bytes(precision, pitch)) + 3 * align256((size_t)N * real_bytes(precision)) +
+            align256((size_t)tiles * swb::kNPart * 8) + align256(sizeof(Control));
+    } else {
+        return fail(nullptr, SWB_ERR_ARG, "unknown precision");
+    }
+    b += align256((size_t)swb::kRecCap * sizeof(Record)) + align256(sizeof(Record)) +
+         align256((size_t)swb::measure_blocks(N) * swb::kNPart * 8) + 256;
+    *bytes = b;
+    return SWB_OK;
+}
+
+int swb_create(const swb_params *p, int precision, swb_state **out) {
+    if (!out) return fail(nullptr, SWB_ERR_ARG, "out is NULL");
+    *out = nullptr;
+    int rc = check_params(p, nullptr);
+    if (rc) return rc;
+    if (precision < SWB_F64 || precision > SWB_PLAIN64) return fail(nullptr, SWB_ERR_ARG, "unknown precision");
+    swb_state *s = new swb_state();
+    s->p = *p;
+    s->precision = precision;
+    s->N = (long long)p->Lx * p->Ly;
+    s->pitch = pitch_of(s->N);
+    fill_args_from_params(s->a, *p);
+    s->a.pitch = s->pitch;
+    s->a.mass_corr = (precision == SWB_F32 || precision == SWB_F16) ? 1 : 0;
+    auto bad = [&](int code) {
+        std::string m = s->err.empty() ? g_err : s->err;
+        delete s;
+        g_err = m;
+        return code;
+    };
+#define CREATE_TRY(expr)                                                                   \
+    do {                                                                                   \
+        cudaError_t e_ = (expr);                                                           \
+        if (e_ != cudaSuccess) {                                                           \
+            s->err = std::string(#expr) + ": " + cudaGetErrorString(e_);                   \
+            return bad(e_ == cudaErrorMemoryAllocation ? SWB_ERR_OOM : SWB_ERR_CUDA);      \
+        }                                                                                  \
+    } while (0)
+    CREATE_TRY(cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking));
+    s->stream = s->own_stream;
+    const long long N = s->N;
+    if (precision == SWB_PLAIN64) {
+        PlainState &ps = s->ps;
+        ps.Lx = p->Lx;
+        ps.Ly = p->Ly;
+        ps.N = N;
+        double **nine[3] = {&ps.fout, &ps.ftemp, &ps.feq};
+        for (auto q : nine) CREATE_TRY(s->alloc((void **)q, (size_t)9 * N * 8));
+        double **one[11] = {&ps.h, &ps.ux, &ps.uy, &ps.vsq, &ps.p, &ps.Fx,
+                            &ps.Fy, &ps.sx, &ps.sy, &ps.hgx, &ps.hgy};
+        for (auto q : one) CREATE_TRY(s->alloc((void **)q, (size_t)N * 8));
+        for (auto q : nine) CREATE_TRY(cudaMemsetAsync(*q, 0, (size_t)9 * N * 8, s->stream));
+        for (auto q : one) CREATE_TRY(cudaMemsetAsync(*q, 0, (size_t)N * 8, s->stream));
+        swb::count_launches(1);
+        fill_kernel<<<blocks_for(N), 256, 0, s->stream>>>(ps.h, N, 1.0);
+        CREATE_TRY(cudaGetLastError());
+        s->a.hF = ps.h;
+    } else {
+        StepArgs &a = s->a;
+        const size_t fb = fbuf_bytes(precision, s->pitch);
+        CREATE_TRY(s->alloc(&a.fa, fb));
+        CREATE_TRY(s->alloc(&a.fb, fb));
+        CREATE_TRY(cudaMemsetAsync(a.fa, 0, fb, s->stream));
+        CREATE_TRY(cudaMemsetAsync(a.fb, 0, fb, s->stream));
+        const size_t fbytes = (size_t)N * s->rb();
+        CREATE_TRY(s->alloc(&a.hF, fbytes));
+        CREATE_TRY(s->alloc(&a.uxF, fbytes));
+        CREATE_TRY(s->alloc(&a.uyF, fbytes));
+        CREATE_TRY(cudaMemsetAsync(a.uxF, 0, fbytes, s->stream));
+        CREATE_TRY(cudaMemsetAsync(a.uyF, 0, fbytes, s->stream));
+        swb::count_launches(1);
+        if (s->rb() == 8)
+            fill_kernel<<<blocks_for(N), 256, 0, s->stream>>>((double *)a.hF, N, 1.0);
+        else
+            fill_kernel_f<<<blocks_for(N), 256, 0, s->stream>>>((float *)a.hF, N, 1.0f);
+        CREATE_TRY(cudaGetLastError());
+        CREATE_TRY(s->alloc((void **)&a.partials, (size_t)a.tiles_x * a.tiles_y * swb::kNPart * 8));
+        CREATE_TRY(s->alloc((void **)&a.ctl, sizeof(Control)));
+        Control c0{};
+        c0.fresh = 1;
+        CREATE_TRY(cudaMemcpyAsync(a.ctl, &c0, sizeof(Control), cudaMemcpyHostToDevice, s->stream));
+    }
+    CREATE_TRY(s->alloc((void **)&s->rec, (size_t)swb::kRecCap * sizeof(Record)));
+    CREATE_TRY(s->alloc((void **)&s->mrec, sizeof(Record)));
+    CREATE_TRY(s->alloc((void **)&s->mscratch, (size_t)swb::measure_blocks(N) * swb::kNPart * 8));
+    CREATE_TRY(s->alloc((void **)&s->mticket, sizeof(unsigned int)));
+    CREATE_TRY(cudaMemsetAsync(s->mticket, 0, sizeof(unsigned int), s->stream));
+    s->a.records = s->rec;
+    s->a.rec_cap = swb::kRecCap;
+    CREATE_TRY(cudaStreamSynchronize(s->stream));
+#undef CREATE_TRY
+    *out = s;
+    return SWB_OK;
+}
+
+int swb_destroy(swb_state *s) {
+    delete s;
+    return SWB_OK;
+}
+
+int swb_get_params(const swb_state *s, swb_params *p, int *precision) {
+    if (!s) return fail(nullptr, SWB_ERR_ARG, "state is NULL");
+    if (p) *p = s->p;
+    if (precision) *precision = s->precision;
+    return SWB_OK;
+}
+
+int swb_set_field(swb_state *s, int field, const double *host) {
+    if (!s || !host) return fail(s ? &s->err : nullptr, SWB_ERR_ARG, "NULL argument");
+    const long long N = s->N;
+    if (s->plain()) {
+        PlainState &ps = s->ps;
+        double *dst = nullptr;
+        long long n = N;
+        switch (field) {
+            case SWB_FIELD_HEIGHT: dst = ps.h; break;
+            case SWB_FIELD_VELX: dst = ps.ux; break;
+            case SWB_FIELD_VELY: dst = ps.uy; break;
+            case SWB_FIELD_PRESSURE: dst = ps.p; break;
+            case SWB_FIELD_FOUT: dst = ps.fout; n = 9 * N; break;
+            case SWB_FIELD_FEQ: dst = ps.feq; n = 9 * N; break;
+            case SWB_FIELD_FX: dst = ps.Fx; break;
+            case SWB_FIELD_FY: dst = ps.Fy; break;
+            case SWB_FIELD_SLIPX: dst = ps.sx; break;
+            case SWB_FIELD_SLIPY: dst = ps.sy; break;
+            case SWB_FIELD_HGRADPX: dst = ps.hgx; break;
+            case SWB_FIELD_HGRADPY: dst = ps.hgy; break;
+            case SWB_FIELD_VSQ: dst = ps.vsq; break;
+            default: return fail(&s->err, SWB_ERR_ARG, "unknown field");
+        }
+        CUDA_TRY(&s->err, cudaMemcpyAsync(dst, host, n * 8, cudaMemcpyHostToDevice, s->stream));
+        // the reference's fout and ftemp are equal between steps
+        if (field == SWB_FIELD_FOUT)
+            CUDA_TRY(&s->err, cudaMemcpyAsync(ps.ftemp, host, n * 8, cudaMemcpyHostToDevice, s->stream));
+        CUDA_TRY(&s->err, cudaStreamSynchronize(s->stream));
+        return SWB_OK;
+    }
+    int rc = materialize(s);
+    if (rc) return rc;
+    StepArgs &a = s->a;
+    switch (field) {
+        case SWB_FIELD_HEIGHT: rc = upload_field(s, a.hF, host, N); break;
+        case SWB_FIELD_VELX: rc = upload_field(s, a.uxF, host, N); break;
+        case SWB_FIELD_VELY: rc = upload_field(s, a.uyF, host, N); break;
+        case SWB_FIELD_FOUT: {
+            rc = ensure_tmp(s, (size_t)9 * N * 8);
+            if (rc) return rc;
+            CUDA_TRY(&s->err, cudaMemcpyAsync(s->dtmp, host, (size_t)9 * N * 8, cudaMemcpyHostToDevice, s->stream));
+            const long long step = s->steps;
+            void *dst = (step & 1) ? a.fb : a.fa;  // the buffer the next step pulls from
+            swb::count_launches(1);
+            push_kernel<double><<<blocks_for(N), 256, 0, s->stream>>>(s->dtmp, dst, s->p.Lx, s->p.Ly,
+                                                                      s->pitch, s->precision);
+            CUDA_TRY(&s->err, cudaGetLastError());
+            break;
+        }
+        default: return fail(&s->err, SWB_ERR_UNSUPPORTED, "field cannot be set in a fused mode");
+    }
+    if (rc) return rc;
+    return set_fresh(s);
+}
+
+int swb_get_field(swb_state *s, int field, double *host) {
+    if (!s || !host) return fail(s ? &s->err : nullptr, SWB_ERR_ARG, "NULL argument");
+    const long long N = s->N;
+    if (s->plain()) {
+        PlainState &ps = s->ps;
+        const double *src = nullptr;
+        long long n = N;
+        switch (field) {
+            case SWB_FIELD_HEIGHT: src = ps.h; break;
+            case SWB_FIELD_VELX: src = ps.ux; break;
+            case SWB_FIELD_VELY: src = ps.uy; break;
+            case SWB_FIELD_PRESSURE: src = ps.p; break;
+            case SWB_FIELD_FOUT: src = ps.fout; n = 9 * N; break;
+            case SWB_FIELD_FEQ: src = ps.feq; n = 9 * N; break;
+            case SWB_FIELD_FX: src = ps.Fx; break;
+            case SWB_FIELD_FY: src = ps.Fy; break;
+            case SWB_FIELD_SLIPX: src = ps.sx; break;
+            case SWB_FIELD_SLIPY: src = ps.sy; break;
+            case SWB_FIELD_HGRADPX: src = ps.hgx; break;
+            case SWB_FIELD_HGRADPY: src = ps.hgy; break;
+            case SWB_FIELD_VSQ: src = ps.vsq; break;
+            default: return fail(&s->err, SWB_ERR_ARG, "unknown field");
+        }
+        return download_field(s, src, host, n, 8);
+    }
+    int rc = materialize(s);
+    if (rc) return rc;
+    StepArgs &a = s->a;
+    switch (field) {
+        case SWB_FIELD_HEIGHT: return download_field(s, a.hF, host, N, s->rb());
+        case SWB_FIELD_VELX: return download_field(s, a.uxF, host, N, s->rb());
+        case SWB_FIELD_VELY: return download_field(s, a.uyF, host, N, s->rb());
+        case SWB_FIELD_PRESSURE: {
+            rc = ensure_tmp(s, (size_t)N * 8);
+            if (rc) return rc;
+            CUDA_TRY(&s->err, swb::launch_pressure_now(s->precision, a, s->dtmp, s->stream));
+            return download_field(s, s->dtmp, host, N, 8);
+        }
+        case SWB_FIELD_FOUT: {
+            rc = ensure_tmp(s, (size_t)9 * N * 8);
+            if (rc) return rc;
+            CUDA_TRY(&s->err, swb::launch_fout(s->precision, a, s->dtmp, s->stream));
+            return download_field(s, s->dtmp, host, 9 * N, 8);
+        }
+        default: return fail(&s->err, SWB_ERR_UNSUPPORTED, "field not available in a fused mode");
+    }
+}
+
+int swb_set_theta(swb_state *s, double theta) {
+    if (!s) return fail(nullptr, SWB_ERR_ARG, "state is NULL");
+    if (s->a.theta_mode == swb::THETA_SCALAR && s->p.theta == theta) return SWB_OK;
+    s->p.theta = theta;
+    s->a.theta_mode = swb::THETA_SCALAR;
+    s->a.kap = host_kappa(theta, s->p.n, s->p.m, s->p.hmin);
+    s->a.cos_theta = host_cospi(theta);
+    s->invalidate_graph();
+    return SWB_OK;
+}
+
+int swb_set_theta_field(swb_state *s, const double *theta) {
+    if (!s) return fail(nullptr, SWB_ERR_ARG, "state is NULL");
+    if (!theta) return swb_set_theta(s, s->p.theta);
+    const long long N = s->N;
+    std::vector<double> kap(N), cs(N);
+    for (long long i = 0; i < N; ++i) {
+        kap[i] = host_kappa(theta[i], s->p.n, s->p.m, s->p.hmin);
+        cs[i] = host_cospi(theta[i]);
+    }
+    StepArgs &a = s->a;
+    if (s->plain()) {
+        if (!s->plain_kapF) CUDA_TRY(&s->err, s->alloc((void **)&s->plain_kapF, (size_t)N * 8));
+        CUDA_TRY(&s->err, cudaMemcpyAsync(s->plain_kapF, kap.data(), N * 8, cudaMemcpyHostToDevice, s->stream));
+        CUDA_TRY(&s->err, cudaStreamSynchronize(s->stream));
+    } else {
+        if (!a.kapF) {
+            void *k = nullptr, *c = nullptr;
+            CUDA_TRY(&s->err, s->alloc(&k, (size_t)N * s->rb()));
+            CUDA_TRY(&s->err, s->alloc(&c, (size_t)N * s->rb()));
+            a.kapF = k;
+            a.cosF = c;
+        }
+        int rc = upload_field(s, (void *)a.kapF, kap.data(), N);
+        if (rc) return rc;
+        rc = upload_field(s, (void *)a.cosF, cs.data(), N);
+        if (rc) return rc;
+    }
+    a.theta_mode = swb::THETA_FIELD;
+    s->invalidate_graph();
+    return SWB_OK;
+}
+
+int swb_set_theta_wave(swb_state *s, double theta0, double dtheta, double v) {
+    if (!s) return fail(nullptr, SWB_ERR_ARG, "state is NULL");
+    if (s->plain()) return fail(&s->err, SWB_ERR_UNSUPPORTED, "moving wettability needs a fused mode");
+    s->a.theta_mode = swb::THETA_WAVE;
+    s->a.theta0 = theta0;
+    s->a.dtheta = dtheta;
+    s->a.wave_v = v;
+    s->invalidate_graph();
+    return SWB_OK;
+}
+
+int swb_set_inclination(swb_state *s, double ax, double ay, int loop_time, int64_t t,
+                        int64_t tstart, int64_t tsmooth) {
+    if (!s) return fail(nullptr, SWB_ERR_ARG, "state is NULL");
+    if (tsmooth == 0) return fail(&s->err, SWB_ERR_ARG, "tsmooth must be nonzero");
+    const int on = (ax != 0.0 || ay != 0.0);
+    if (s->incl == on && s->ax == ax && s->ay == ay && s->incl_loop_time == loop_time &&
+        s->incl_t == t && s->incl_tstart == tstart && s->incl_tsmooth == tsmooth)
+        return SWB_OK;
+    s->incl = on;
+    s->ax = ax;
+    s->ay = ay;
+    s->incl_loop_time = loop_time;
+    s->incl_t = t;
+    s->incl_tstart = tstart;
+    s->incl_tsmooth = tsmooth;
+    StepArgs &a = s->a;
+    a.incl = on;
+    a.ax = ax;
+    a.ay = ay;
+    a.incl_loop_time = loop_time;
+    a.incl_fixed = incl_factor(t, tstart, tsmooth);
+    a.incl_tstart = tstart;
+    a.incl_tsmooth = tsmooth;
+    s->invalidate_graph();
+    return SWB_OK;
+}
+
+int swb_set_measures(swb_state *s, int mask, double hthresh) {
+    if (!s) return fail(nullptr, SWB_ERR_ARG, "state is NULL");
+    if (mask & ~SWB_MEAS_ALL) return fail(&s->err, SWB_ERR_ARG, "unknown measure bits");
+    if (s->a.meas_mask == mask && s->a.hthresh == hthresh) return SWB_OK;
+    s->a.meas_mask = mask;
+    s->a.hthresh = hthresh;
+    s->plain_meas_mask = mask;
+    s->invalidate_graph();
+    return SWB_OK;
+}
+
+int swb_step(swb_state *s, int64_t nsteps) {
+    if (!s) return fail(nullptr, SWB_ERR_ARG, "state is NULL");
+    if (nsteps < 0) return fail(&s->err, SWB_ERR_ARG, "nsteps must be >= 0");
+    if (s->plain()) {
+        for (int64_t k = 0; k < nsteps; ++k) {
+            int rc = plain_iteration(s);
+            if (rc) return rc;
+        }
+        return SWB_OK;
+    }
+    return fused_steps(s, nsteps);
+}
+
+int swb_sync(swb_state *s) {
+    if (!s) return fail(nullptr, SWB_ERR_ARG, "state is NULL");
+    CUDA_TRY(&s->err, cudaStreamSynchronize(s->stream));
+    return check_nan(s);
+}
+
+int swb_steps_done(swb_state *s, int64_t *t) {
+    if (!s || !t) return fail(s ? &s->err : nullptr, SWB_ERR_ARG, "NULL argument");
+    *t = s->steps;
+    return SWB_OK;
+}
+
+int swb_get_measures(swb_state *s, swb_measure *out, int64_t cap, int64_t *count) {
+    if (!s || !count) return fail(s ? &s->err : nullptr, SWB_ERR_ARG, "NULL argument");
+    *count = 0;
+    long long head = 0;
+    if (s->plain()) {
+        head = s->plain_rec_head;
+    } else {
+        CUDA_TRY(&s->err, cudaMemcpyAsync(&head, &s->a.ctl->rec_head, sizeof(long long),
+                                          cudaMemcpyDeviceToHost, s->stream));
+    }
+    CUDA_TRY(&s->err, cudaStreamSynchronize(s->stream));
+    long long first = s->rec_read;
+    if (head - first > swb::kRecCap) first = head - swb::kRecCap;  // older ones overwritten
+    long long n = head - first;
+    if (n > cap) n = cap;
+    std::vector<Record> tmp(n);
+    for (long long k = 0; k < n;) {
+        const long long slot = (first + k) % swb::kRecCap;
+        long long run = std::min<long long>(n - k, swb::kRecCap - slot);
+        CUDA_TRY(&s->err, cudaMemcpyAsync(tmp.data() + k, s->rec + slot, run * sizeof(Record),
+                                          cudaMemcpyDeviceToHost, s->stream));
+        k += run;
+    }
+    CUDA_TRY(&s->err, cudaStreamSynchronize(s->stream));
+    for (long long k = 0; k < n; ++k) record_to_measure(tmp[k], out + k);
+    s->rec_read = first + n;
+    *count = n;
+    return check_nan(s);
+}
+
+int swb_measure_now(swb_state *s, double hthresh, swb_measure *out) {
+    if (!s || !out) return fail(s ? &s->err : nullptr, SWB_ERR_ARG, "NULL argument");
+    int rc = materialize(s);
+    if (rc) return rc;
+    const void *cosF = (!s->plain() && s->a.theta_mode == swb::THETA_FIELD) ? s->a.cosF : nullptr;
+    CUDA_TRY(&s->err, swb::launch_measure(s->a.hF, s->rb() == 8, s->p.Lx, s->p.Ly, hthresh, cosF,
+                                          s->a.cos_theta, s->mscratch, s->mticket, s->mrec,
+                                          s->steps, s->stream));
+    Record r{};
+    CUDA_TRY(&s->err, cudaMemcpyAsync(&r, s->mrec, sizeof(Record), cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(&s->err, cudaStreamSynchronize(s->stream));
+    record_to_measure(r, out);
+    return SWB_OK;
+}
+
+int swb_set_field_device(swb_state *s, int field, const double *dptr) {
+    if (!s || !dptr) return fail(s ? &s->err : nullptr, SWB_ERR_ARG, "NULL argument");
+    if (field != SWB_FIELD_HEIGHT && field != SWB_FIELD_VELX && field != SWB_FIELD_VELY)
+        return fail(&s->err, SWB_ERR_UNSUPPORTED, "device upload supports height and velocities");
+    const long long N = s->N;
+    void *dst;
+    if (s->plain()) {
+        dst = field == SWB_FIELD_HEIGHT ? (void *)s->ps.h : field == SWB_FIELD_VELX ? (void *)s->ps.ux : (void *)s->ps.uy;
+        CUDA_TRY(&s->err, cudaMemcpyAsync(dst, dptr, N * 8, cudaMemcpyDeviceToDevice, s->stream));
+        return SWB_OK;
+    }
+    int rc = materialize(s);
+    if (rc) return rc;
+    dst = field == SWB_FIELD_HEIGHT ? s->a.hF : field == SWB_FIELD_VELX ? s->a.uxF : s->a.uyF;
+    if (s->rb() == 8) {
+        CUDA_TRY(&s->err, cudaMemcpyAsync(dst, dptr, N * 8, cudaMemcpyDeviceToDevice, s->stream));
+    } else {
+        d2f_kernel<<<blocks_for(N), 256, 0, s->stream>>>(dptr, (float *)dst, N);
+        swb::count_launches(1);
+        CUDA_TRY(&s->err, cudaGetLastError());
+    }
+    return set_fresh(s);
+}
+
+int swb_set_stream(swb_state *s, void *stream) {
+    if (!s) return fail(nullptr, SWB_ERR_ARG, "state is NULL");
+    cudaStream_t ns = stream ? (cudaStream_t)stream : s->own_stream;
+    if (ns != s->stream) {
+        CUDA_TRY(&s->err, cudaStreamSynchronize(s->stream));
+        s->stream = ns;
+    }
+    return SWB_OK;
+}
+
+int swb_get_stream(swb_state *s, void **stream) {
+    if (!s || !stream) return fail(s ? &s->err : nullptr, SWB_ERR_ARG, "NULL argument");
+    *stream = (void *)s->stream;
+    return SWB_OK;
+}
+
+int swb_launch_count(uint64_t *count) {
+    if (!count) return fail(nullptr, SWB_ERR_ARG, "NULL argument");
+    *count = swb::g_launches.load();
+    return SWB_OK;
+}
+
+// ---------------------------------------------------------------- per-op API
+#define PLAIN_ONLY(s)                                                                  \
+    do {                                                                               \
+        if (!(s)) return fail(nullptr, SWB_ERR_ARG, "state is NULL");                  \
+        if (!(s)->plain())                                                             \
+            return fail(&(s)->err, SWB_ERR_UNSUPPORTED, "per-op calls need SWB_PLAIN64"); \
+    } while (0)
+
+int swb_op_filmpressure(swb_state *s) {
+    PLAIN_ONLY(s);
+    const bool field = s->a.theta_mode == swb::THETA_FIELD;
+    CUDA_TRY(&s->err, swb::plain_filmpressure(s->ps, field ? s->plain_kapF : nullptr, s->a.kap,
+                                              s->p.gamma, s->p.n, s->p.m, s->p.hmin, s->p.hcrit,
+                                              s->stream));
+    return SWB_OK;
+}
+int swb_op_hgradp(swb_state *s) {
+    PLAIN_ONLY(s);
+    CUDA_TRY(&s->err, swb::plain_hgradp(s->ps, s->stream));
+    return SWB_OK;
+}
+int swb_op_slippage(swb_state *s) {
+    PLAIN_ONLY(s);
+    CUDA_TRY(&s->err, swb::plain_slippage(s->ps, s->p.delta, s->p.mu, s->stream));
+    return SWB_OK;
+}
+int swb_op_force_sum(swb_state *s) {
+    PLAIN_ONLY(s);
+    CUDA_TRY(&s->err, swb::plain_force_sum(s->ps, s->stream));
+    return SWB_OK;
+}
+int swb_op_inclination(swb_state *s, double ax, double ay, int64_t t, int64_t tstart,
+                       int64_t tsmooth) {
+    PLAIN_ONLY(s);
+    if (tsmooth == 0) return fail(&s->err, SWB_ERR_ARG, "tsmooth must be nonzero");
+    CUDA_TRY(&s->err, swb::plain_inclination(s->ps, ax, ay, incl_factor(t, tstart, tsmooth), s->stream));
+    return SWB_OK;
+}
+int swb_op_equilibrium(swb_state *s) {
+    PLAIN_ONLY(s);
+    CUDA_TRY(&s->err, swb::plain_equilibrium(s->ps, s->p.g, s->stream));
+    return SWB_OK;
+}
+int swb_op_bgk_stream(swb_state *s) {
+    PLAIN_ONLY(s);
+    CUDA_TRY(&s->err, swb::plain_collide(s->ps, 1.0 - 1.0 / s->p.tau, 1.0 / s->p.tau, s->stream));
+    CUDA_TRY(&s->err, swb::plain_stream(s->ps, s->stream));
+    return SWB_OK;
+}
+int swb_op_moments(swb_state *s) {
+    PLAIN_ONLY(s);
+    CUDA_TRY(&s->err, swb::plain_moments(s->ps, s->stream));
+    return SWB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,394 @@
+// swb_batch.cu -- batched ensembles: many lattices of uneven size and
+// parameters advanced together, one launch per time step over a packed tile
+// table (persistent CTAs walk the table), replayed from a captured CUDA graph.
+// The CTA count per launch is picked by timing the candidates on the first
+// steps (the timed steps are real steps of the simulation).
+#include <algorithm>
+#include <chrono>
+#include <string>
+#include <vector>
+
+#include "swb_lattice.h"
+
+using swb::Control;
+using swb::LatticeLayout;
+using swb::StepArgs;
+using swb::TileRef;
+
+namespace swb {
+
+namespace {
+thread_local std::string b_err;
+int bfail(std::string *slot, int code, const std::string &m) {
+    b_err = m;
+    set_global_error(m.c_str());
+    if (slot) *slot = m;
+    return code;
+}
+
+__global__ void fill_d(double *d, long long n, double v) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        d[i] = v;
+}
+__global__ void fill_f(float *d, long long n, float v) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        d[i] = v;
+}
+__global__ void d2f(const double *s, float *d, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        d[i] = (float)s[i];
+}
+__global__ void set_fresh_k(Control *c) { c->fresh = 1; }
+
+int nblk(long long n) {
+    long long b = (n + 255) / 256;
+    return (int)std::min<long long>(std::max<long long>(b, 1), 2048);
+}
+}  // namespace
+
+double host_cospi_shared(double x) {
+    if (!std::isfinite(x)) return NAN;
+    double r = std::fmod(std::fabs(x), 2.0);
+    if (r == 0.0) return 1.0;
+    if (r == 1.0) return -1.0;
+    if (r == 0.5 || r == 1.5) return 0.0;
+    const long double PI_L = 3.141592653589793238462643383279502884L;
+    return (double)cosl(PI_L * (long double)r);
+}
+
+double host_kappa_shared(double theta, int n, int m, double hmin) {
+    double a = 1.0 - host_cospi_shared(theta);
+    a = a * (double)(n - 1);
+    a = a * (double)(m - 1);
+    return a / ((double)(n - m) * hmin);
+}
+
+cudaError_t lattice_init(const StepArgs &a, int precision, const LatticeLayout &L,
+                         const double *h0_host, cudaStream_t st) {
+    const long long N = (long long)a.Lx * a.Ly;
+    cudaError_t e = cudaMemsetAsync(a.fa, 0, L.total, st);  // whole block is contiguous from fa
+    if (e != cudaSuccess) return e;
+    if (!h0_host) {
+        count_launches(1);
+        if (precision == SWB_F64)
+            fill_d<<<nblk(N), 256, 0, st>>>((double *)a.hF, N, 1.0);
+        else
+            fill_f<<<nblk(N), 256, 0, st>>>((float *)a.hF, N, 1.0f);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    Control c0{};
+    c0.fresh = 1;
+    // c0 lives on this stack frame: a pageable-memory copy is staged before return
+    e = cudaMemcpyAsync(a.ctl, &c0, sizeof(Control), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return e;
+    return cudaStreamSynchronize(st);
+}
+
+cudaError_t lattice_upload_height(const StepArgs &a, int precision, const double *h_host,
+                                  void *staging, cudaStream_t st) {
+    const long long N = (long long)a.Lx * a.Ly;
+    cudaError_t e;
+    if (precision == SWB_F64) {
+        e = cudaMemcpyAsync(a.hF, h_host, N * 8, cudaMemcpyHostToDevice, st);
+    } else {
+        e = cudaMemcpyAsync(staging, h_host, N * 8, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) {
+            count_launches(1);
+            d2f<<<nblk(N), 256, 0, st>>>((const double *)staging, (float *)a.hF, N);
+            e = cudaGetLastError();
+        }
+    }
+    if (e != cudaSuccess) return e;
+    count_launches(1);
+    set_fresh_k<<<1, 1, 0, st>>>(a.ctl);
+    return cudaGetLastError();
+}
+
+cudaError_t lattice_download_height(const StepArgs &a, int precision, bool fields_current,
+                                    double *h_host, cudaStream_t st) {
+    const long long N = (long long)a.Lx * a.Ly;
+    cudaError_t e = cudaSuccess;
+    if (!fields_current) {
+        e = launch_moments(precision, a, st);
+        if (e != cudaSuccess) return e;
+    }
+    if (precision == SWB_F64) {
+        e = cudaMemcpyAsync(h_host, a.hF, N * 8, cudaMemcpyDeviceToHost, st);
+        if (e != cudaSuccess) return e;
+        return cudaStreamSynchronize(st);
+    }
+    std::vector<float> tmp(N);
+    e = cudaMemcpyAsync(tmp.data(), a.hF, N * 4, cudaMemcpyDeviceToHost, st);
+    if (e != cudaSuccess) return e;
+    e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return e;
+    for (long long i = 0; i < N; ++i) h_host[i] = (double)tmp[i];
+    return cudaSuccess;
+}
+
+}  // namespace swb
+
+struct swb_batch {
+    int count = 0, precision = 0;
+    std::vector<swb_params> params;
+    std::vector<LatticeLayout> layouts;
+    std::vector<StepArgs> args;
+    std::vector<char> fields_current;
+    char *slab = nullptr;
+    size_t slab_bytes = 0;
+    double *staging = nullptr;
+    StepArgs *d_args = nullptr;
+    TileRef *d_tiles = nullptr;
+    int ntiles = 0;
+    cudaStream_t stream = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    int steps_per_graph = 32;
+    int grid = 0;
+    bool tuned = false, args_dirty = true, gvalid = false;
+    long long steps = 0;
+    std::string err;
+
+    void invalidate() {
+        if (gexec) cudaGraphExecDestroy(gexec);
+        gexec = nullptr;
+        gvalid = false;
+    }
+    ~swb_batch() {
+        invalidate();
+        if (stream) cudaStreamSynchronize(stream);
+        cudaFree(slab);
+        cudaFree(staging);
+        cudaFree(d_args);
+        cudaFree(d_tiles);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+#define B_TRY(b, expr)                                                                     \
+    do {                                                                                   \
+        cudaError_t e_ = (expr);                                                           \
+        if (e_ != cudaSuccess)                                                             \
+            return swb::bfail(&(b)->err, e_ == cudaErrorMemoryAllocation ? SWB_ERR_OOM : SWB_ERR_CUDA, \
+                              std::string(#expr) + ": " + cudaGetErrorString(e_));        \
+    } while (0)
+
+namespace {
+
+int upload_args(swb_batch *b) {
+    if (!b->args_dirty) return SWB_OK;
+    B_TRY(b, cudaMemcpyAsync(b->d_args, b->args.data(), b->args.size() * sizeof(StepArgs),
+                             cudaMemcpyHostToDevice, b->stream));
+    B_TRY(b, cudaStreamSynchronize(b->stream));
+    b->args_dirty = false;
+    b->invalidate();
+    return SWB_OK;
+}
+
+int launch_n(swb_batch *b, int n, int grid) {
+    for (int k = 0; k < n; ++k)
+        B_TRY(b, swb::launch_batch_step(b->precision, b->d_args, b->d_tiles, b->ntiles, grid, b->stream));
+    return SWB_OK;
+}
+
+// Picks the CTA count: one CTA per tile, or persistent CTAs (k per SM).
+int autotune(swb_batch *b, long long &left) {
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int occ = swb::batch_blocks_per_sm(b->precision);
+    std::vector<int> cands = {b->ntiles};
+    for (int k = 1; k <= occ; ++k) cands.push_back(std::min(b->ntiles, sms * k));
+    std::sort(cands.begin(), cands.end());
+    cands.erase(std::unique(cands.begin(), cands.end()), cands.end());
+    const int probe = 4;
+    if (left < (long long)probe * (long long)cands.size() + probe) {
+        b->grid = std::min(b->ntiles, sms * occ);
+        b->tuned = true;
+        return SWB_OK;
+    }
+    cudaEvent_t e0, e1;
+    B_TRY(b, cudaEventCreate(&e0));
+    B_TRY(b, cudaEventCreate(&e1));
+    float best = 1e30f;
+    int best_grid = cands.back();
+    int rc = launch_n(b, 1, cands.back());  // warm-up (a real step)
+    left -= 1;
+    for (int g : cands) {
+        if (rc) break;
+        cudaEventRecord(e0, b->stream);
+        rc = launch_n(b, probe, g);
+        cudaEventRecord(e1, b->stream);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best) {
+            best = ms;
+            best_grid = g;
+        }
+        left -= probe;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    b->grid = best_grid;
+    b->tuned = true;
+    return SWB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int swb_batch_create(const swb_params *params, int count, int precision, swb_batch **out) {
+    if (!out || !params || count < 1) return swb::bfail(nullptr, SWB_ERR_ARG, "bad arguments");
+    *out = nullptr;
+    if (precision != SWB_F64 && precision != SWB_F32 && precision != SWB_F16)
+        return swb::bfail(nullptr, SWB_ERR_ARG, "batch precision must be SWB_F64, SWB_F32 or SWB_F16");
+    for (int i = 0; i < count; ++i) {
+        const swb_params &p = params[i];
+        if (p.Lx < 1 || p.Ly < 1 || (long long)p.Lx * p.Ly * 9 >= (1LL << 31) || !(p.tau > 0) ||
+            p.n <= p.m || p.m < 1 || !(p.hmin > 0))
+            return swb::bfail(nullptr, SWB_ERR_ARG, "invalid params for lattice " + std::to_string(i));
+        if (p.kbt != 0.0) return swb::bfail(nullptr, SWB_ERR_UNSUPPORTED, "kbt != 0 is not supported");
+    }
+    swb_batch *b = new swb_batch();
+    b->count = count;
+    b->precision = precision;
+    b->params.assign(params, params + count);
+    size_t off = 0;
+    long long maxN = 0;
+    std::vector<size_t> offs;
+    for (int i = 0; i < count; ++i) {
+        LatticeLayout L = swb::lattice_layout(params[i], precision);
+        b->layouts.push_back(L);
+        offs.push_back(off);
+        off += L.total;
+        maxN = std::max<long long>(maxN, (long long)params[i].Lx * params[i].Ly);
+    }
+    auto bad = [&](int code) {
+        std::string m = b->err;
+        delete b;
+        swb::b_err = m;
+        swb::set_global_error(m.c_str());
+        return code;
+    };
+#define BC_TRY(expr)                                                                       \
+    do {                                                                                   \
+        cudaError_t e_ = (expr);                                                           \
+        if (e_ != cudaSuccess) {                                                           \
+            b->err = std::string(#expr) + ": " + cudaGetErrorString(e_);                   \
+            return bad(e_ == cudaErrorMemoryAllocation ? SWB_ERR_OOM : SWB_ERR_CUDA);      \
+        }                                                                                  \
+    } while (0)
+    BC_TRY(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+    b->slab_bytes = off;
+    BC_TRY(cudaMalloc((void **)&b->slab, off));
+    BC_TRY(cudaMalloc((void **)&b->staging, (size_t)maxN * 8));
+    std::vector<TileRef> tiles;
+    for (int i = 0; i < count; ++i) {
+        StepArgs a = swb::lattice_args(params[i], precision, b->slab + offs[i], b->layouts[i]);
+        b->args.push_back(a);
+        BC_TRY(swb::lattice_init(a, precision, b->layouts[i], nullptr, b->stream));
+        for (int ty = 0; ty < a.tiles_y; ++ty)
+            for (int tx = 0; tx < a.tiles_x; ++tx) tiles.push_back({i, tx, ty});
+    }
+    b->fields_current.assign(count, 1);
+    b->ntiles = (int)tiles.size();
+    BC_TRY(cudaMalloc((void **)&b->d_args, sizeof(StepArgs) * count));
+    BC_TRY(cudaMalloc((void **)&b->d_tiles, sizeof(TileRef) * tiles.size()));
+    BC_TRY(cudaMemcpy(b->d_tiles, tiles.data(), sizeof(TileRef) * tiles.size(), cudaMemcpyHostToDevice));
+#undef BC_TRY
+    *out = b;
+    return SWB_OK;
+}
+
+int swb_batch_destroy(swb_batch *b) {
+    delete b;
+    return SWB_OK;
+}
+
+int swb_batch_set_height(swb_batch *b, int idx, const double *host) {
+    if (!b || !host || idx < 0 || idx >= b->count) return swb::bfail(b ? &b->err : nullptr, SWB_ERR_ARG, "bad arguments");
+    StepArgs &a = b->args[idx];
+    if (!b->fields_current[idx]) {  // keep the velocities current
+        B_TRY(b, swb::launch_moments(b->precision, a, b->stream));
+    }
+    B_TRY(b, swb::lattice_upload_height(a, b->precision, host, b->staging, b->stream));
+    B_TRY(b, cudaStreamSynchronize(b->stream));
+    b->fields_current[idx] = 1;
+    return SWB_OK;
+}
+
+int swb_batch_get_height(swb_batch *b, int idx, double *host) {
+    if (!b || !host || idx < 0 || idx >= b->count) return swb::bfail(b ? &b->err : nullptr, SWB_ERR_ARG, "bad arguments");
+    B_TRY(b, swb::lattice_download_height(b->args[idx], b->precision, b->fields_current[idx], host, b->stream));
+    b->fields_current[idx] = 1;
+    return SWB_OK;
+}
+
+int swb_batch_set_theta_wave(swb_batch *b, int idx, double theta0, double dtheta, double v) {
+    if (!b || idx < 0 || idx >= b->count) return swb::bfail(b ? &b->err : nullptr, SWB_ERR_ARG, "bad arguments");
+    swb::set_wave(b->args[idx], theta0, dtheta, v);
+    b->args_dirty = true;
+    return SWB_OK;
+}
+
+int swb_batch_step(swb_batch *b, int64_t nsteps) {
+    if (!b || nsteps < 0) return swb::bfail(b ? &b->err : nullptr, SWB_ERR_ARG, "bad arguments");
+    if (nsteps == 0) return SWB_OK;
+    int rc = upload_args(b);
+    if (rc) return rc;
+    long long left = nsteps;
+    if (!b->tuned) {
+        rc = autotune(b, left);
+        if (rc) return rc;
+    }
+    if (left >= b->steps_per_graph) {
+        if (!b->gvalid) {
+            cudaGraph_t g = nullptr;
+            B_TRY(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+            cudaError_t le = cudaSuccess;
+            for (int k = 0; k < b->steps_per_graph && le == cudaSuccess; ++k)
+                le = swb::launch_batch_step(b->precision, b->d_args, b->d_tiles, b->ntiles, b->grid, b->stream);
+            cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
+            if (le != cudaSuccess) {
+                if (g) cudaGraphDestroy(g);
+                return swb::bfail(&b->err, SWB_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(le));
+            }
+            B_TRY(b, ce);
+            cudaError_t ie = cudaGraphInstantiate(&b->gexec, g, 0);
+            cudaGraphDestroy(g);
+            B_TRY(b, ie);
+            b->gvalid = true;
+        }
+        while (left >= b->steps_per_graph) {
+            B_TRY(b, cudaGraphLaunch(b->gexec, b->stream));
+            left -= b->steps_per_graph;
+        }
+    }
+    rc = launch_n(b, (int)left, b->grid);
+    if (rc) return rc;
+    b->steps += nsteps;
+    std::fill(b->fields_current.begin(), b->fields_current.end(), 0);
+    return SWB_OK;
+}
+
+int swb_batch_sync(swb_batch *b) {
+    if (!b) return swb::bfail(nullptr, SWB_ERR_ARG, "batch is NULL");
+    B_TRY(b, cudaStreamSynchronize(b->stream));
+    return SWB_OK;
+}
+
+int swb_batch_tile(swb_batch *b, int *tile_x, int *tile_y, int *steps_per_graph) {
+    if (!b) return swb::bfail(nullptr, SWB_ERR_ARG, "batch is NULL");
+    if (tile_x) *tile_x = b->tuned ? swb::kTX : 0;
+    if (tile_y) *tile_y = b->tuned ? swb::kTY : 0;
+    if (steps_per_graph) *steps_per_graph = b->tuned ? b->steps_per_graph : 0;
+    return SWB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,114 @@
+// swb_lattice.h -- device memory of one lattice inside a batch or a server:
+// layout, initialisation and host<->device field transfer.  Internal.
+#pragma once
+#include <cuda_fp16.h>
+
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "swb_internal.h"
+
+namespace swb {
+
+double host_cospi_shared(double x);
+double host_kappa_shared(double theta, int n, int m, double hmin);
+
+inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+inline long long pitch_for(long long N) { return (N + 63) / 64 * 64; }
+inline int real_bytes_of(int precision) { return precision == SWB_F64 ? 8 : 4; }
+inline size_t fbuf_bytes_of(int precision, long long pitch) {
+    switch (precision) {
+        case SWB_F64: return (size_t)9 * pitch * 8;
+        case SWB_F32: return (size_t)9 * pitch * 4;
+        default: return (size_t)pitch * 4 + (size_t)8 * pitch * 2;
+    }
+}
+
+// Byte offsets of one lattice's buffers inside a contiguous block.
+struct LatticeLayout {
+    size_t fa, fb, h, ux, uy, partials, ctl, total;
+};
+
+inline LatticeLayout lattice_layout(const swb_params &p, int precision) {
+    const long long N = (long long)p.Lx * p.Ly, pitch = pitch_for(N);
+    const int tiles = ((p.Lx + kTX - 1) / kTX) * ((p.Ly + kTY - 1) / kTY);
+    LatticeLayout L{};
+    size_t o = 0;
+    const size_t fb = align256(fbuf_bytes_of(precision, pitch));
+    const size_t fld = align256((size_t)N * real_bytes_of(precision));
+    L.fa = o; o += fb;
+    L.fb = o; o += fb;
+    L.h = o; o += fld;
+    L.ux = o; o += fld;
+    L.uy = o; o += fld;
+    L.partials = o; o += align256((size_t)tiles * kNPart * 8);
+    L.ctl = o; o += align256(sizeof(Control));
+    L.total = o;
+    return L;
+}
+
+// Step arguments of a lattice whose buffers start at `base`.
+inline StepArgs lattice_args(const swb_params &p, int precision, char *base, const LatticeLayout &L) {
+    StepArgs a{};
+    a.Lx = p.Lx;
+    a.Ly = p.Ly;
+    a.pitch = pitch_for((long long)p.Lx * p.Ly);
+    a.fa = base + L.fa;
+    a.fb = base + L.fb;
+    a.hF = base + L.h;
+    a.uxF = base + L.ux;
+    a.uyF = base + L.uy;
+    a.partials = (double *)(base + L.partials);
+    a.ctl = (Control *)(base + L.ctl);
+    a.gamma = p.gamma;
+    a.hmin = p.hmin;
+    a.hcrit = p.hcrit;
+    a.delta = p.delta;
+    a.mu = p.mu;
+    a.g = p.g;
+    a.invtau = 1.0 / p.tau;
+    a.omeg = 1.0 - 1.0 / p.tau;
+    a.tau_is_one = (p.tau == 1.0);
+    a.n = p.n;
+    a.m = p.m;
+    a.theta_mode = THETA_SCALAR;
+    a.kap = host_kappa_shared(p.theta, p.n, p.m, p.hmin);
+    a.cos_theta = host_cospi_shared(p.theta);
+    a.tiles_x = (p.Lx + kTX - 1) / kTX;
+    a.tiles_y = (p.Ly + kTY - 1) / kTY;
+    a.hthresh = 0.055;
+    a.mass_corr = (precision == SWB_F32 || precision == SWB_F16) ? 1 : 0;
+    a.records = nullptr;
+    a.rec_cap = 0;
+    a.meas_mask = 0;
+    return a;
+}
+
+inline void set_wave(StepArgs &a, double theta0, double dtheta, double v) {
+    if (dtheta == 0.0 && v == 0.0) {
+        a.theta_mode = THETA_SCALAR;
+        a.kap = host_kappa_shared(theta0, a.n, a.m, a.hmin);
+        a.cos_theta = host_cospi_shared(theta0);
+    } else {
+        a.theta_mode = THETA_WAVE;
+        a.theta0 = theta0;
+        a.dtheta = dtheta;
+        a.wave_v = v;
+    }
+}
+
+// Zero populations, h = 1 (or h0), u = 0, fresh control block.  Async on st.
+cudaError_t lattice_init(const StepArgs &a, int precision, const LatticeLayout &L,
+                         const double *h0_host, cudaStream_t st);
+// Upload a host Float64 height into the field (converted to the compute type)
+// and mark the lattice fresh.  Async on st; `staging` must stay alive until
+// the stream passes this point (pinned or synchronised by the caller).
+cudaError_t lattice_upload_height(const StepArgs &a, int precision, const double *h_host,
+                                  void *staging, cudaStream_t st);
+// Height of the lattice into host memory (runs the moments kernel first
+// unless the fields are the current source).  Synchronises st.
+cudaError_t lattice_download_height(const StepArgs &a, int precision, bool fields_current,
+                                    double *h_host, cudaStream_t st);
+
+}  // namespace swb

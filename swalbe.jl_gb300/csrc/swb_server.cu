@@ -1,0 +1,404 @@
+// swb_server.cu -- serving: a request loop that admits thin-film solves by
+// their HBM footprint, keeps their state resident, and advances every
+// resident solve together (continuous batching: requests that arrive while
+// others run are admitted at the next tick, and finished ones leave).
+//
+// One worker thread owns the GPU stream.  A tick runs `steps_per_tick` time
+// steps (fewer if a resident request finishes sooner) as one batched launch
+// per step over the packed tile table of all resident lattices.  Each
+// lattice's arithmetic is independent of which others share the launch, so
+// a result is bit-identical alone and in the mix.
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "swb_lattice.h"
+
+using swb::LatticeLayout;
+using swb::StepArgs;
+using swb::TileRef;
+
+namespace {
+
+struct Req {
+    int64_t id = 0;
+    swb_params p{};
+    std::vector<double> h0;
+    double theta0 = 0, dtheta = 0, v = 0;
+    int64_t nsteps = 0, done = 0;
+    int status = 0;  // 0 queued, 1 running, 2 done, <0 error
+    double t_submit = 0, t_admit = 0, t_done = 0;
+    std::vector<double> result;
+    char *dev = nullptr;
+    LatticeLayout L{};
+    StepArgs a{};
+    size_t bytes = 0;
+    bool cancel = false;
+};
+
+thread_local std::string s_err;
+int sfail(int code, const std::string &m) {
+    s_err = m;
+    swb::set_global_error(m.c_str());
+    return code;
+}
+
+}  // namespace
+
+struct swb_server {
+    size_t budget = 0, in_use = 0;
+    int precision = SWB_F32;
+    int steps_per_tick = 100;
+    int device = 0;
+    std::mutex mu;
+    std::condition_variable cv;
+    std::deque<int64_t> queue;
+    std::map<int64_t, std::unique_ptr<Req>> reqs;
+    std::vector<Req *> active;
+    std::thread worker;
+    bool stop = false;
+    int64_t next_id = 1;
+    cudaStream_t stream = nullptr;
+    cudaMemPool_t pool = nullptr;
+    StepArgs *d_args = nullptr;
+    TileRef *d_tiles = nullptr;
+    size_t cap_args = 0, cap_tiles = 0;
+    double *staging = nullptr;
+    size_t staging_elems = 0;
+    swb_server_stats st{};
+    std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+    std::string err;
+
+    double now() const {
+        return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
+};
+
+namespace {
+
+void set_error(swb_server *sv, const std::string &m) {
+    std::lock_guard<std::mutex> g(sv->mu);
+    sv->err = m;
+}
+
+// Worker-side: allocate and initialise newly admitted requests.
+bool admit_device(swb_server *sv, Req *r) {
+    cudaError_t e = cudaMallocFromPoolAsync((void **)&r->dev, r->bytes, sv->pool, sv->stream);
+    if (e != cudaSuccess) {
+        set_error(sv, std::string("admit: ") + cudaGetErrorString(e));
+        return false;
+    }
+    r->a = swb::lattice_args(r->p, sv->precision, r->dev, r->L);
+    swb::set_wave(r->a, r->theta0, r->dtheta, r->v);
+    const long long N = (long long)r->p.Lx * r->p.Ly;
+    if ((size_t)N > sv->staging_elems) {
+        cudaStreamSynchronize(sv->stream);
+        cudaFree(sv->staging);
+        sv->staging = nullptr;
+        if (cudaMalloc((void **)&sv->staging, (size_t)N * 8) != cudaSuccess) {
+            sv->staging_elems = 0;
+            set_error(sv, "admit: staging allocation failed");
+            return false;
+        }
+        sv->staging_elems = N;
+    }
+    e = swb::lattice_init(r->a, sv->precision, r->L, r->h0.data(), sv->stream);
+    if (e == cudaSuccess) e = swb::lattice_upload_height(r->a, sv->precision, r->h0.data(), sv->staging, sv->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(sv->stream);
+    if (e != cudaSuccess) {
+        set_error(sv, std::string("admit: ") + cudaGetErrorString(e));
+        return false;
+    }
+    return true;
+}
+
+bool upload_table(swb_server *sv) {
+    std::vector<StepArgs> args;
+    std::vector<TileRef> tiles;
+    for (size_t i = 0; i < sv->active.size(); ++i) {
+        const StepArgs &a = sv->active[i]->a;
+        args.push_back(a);
+        for (int ty = 0; ty < a.tiles_y; ++ty)
+            for (int tx = 0; tx < a.tiles_x; ++tx) tiles.push_back({(int)i, tx, ty});
+    }
+    if (args.size() > sv->cap_args) {
+        cudaFree(sv->d_args);
+        sv->cap_args = std::max<size_t>(args.size(), 2 * sv->cap_args);
+        if (cudaMalloc((void **)&sv->d_args, sv->cap_args * sizeof(StepArgs)) != cudaSuccess) return false;
+    }
+    if (tiles.size() > sv->cap_tiles) {
+        cudaFree(sv->d_tiles);
+        sv->cap_tiles = std::max<size_t>(tiles.size(), 2 * sv->cap_tiles);
+        if (cudaMalloc((void **)&sv->d_tiles, sv->cap_tiles * sizeof(TileRef)) != cudaSuccess) return false;
+    }
+    if (cudaMemcpyAsync(sv->d_args, args.data(), args.size() * sizeof(StepArgs), cudaMemcpyHostToDevice, sv->stream) != cudaSuccess)
+        return false;
+    if (cudaMemcpyAsync(sv->d_tiles, tiles.data(), tiles.size() * sizeof(TileRef), cudaMemcpyHostToDevice, sv->stream) != cudaSuccess)
+        return false;
+    return cudaStreamSynchronize(sv->stream) == cudaSuccess;
+}
+
+int count_tiles(swb_server *sv) {
+    int n = 0;
+    for (Req *r : sv->active) n += r->a.tiles_x * r->a.tiles_y;
+    return n;
+}
+
+void worker_main(swb_server *sv) {
+    cudaSetDevice(sv->device);
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, sv->device);
+    const int occ = swb::batch_blocks_per_sm(sv->precision);
+    for (;;) {
+        std::vector<Req *> admitted;
+        bool changed = false;
+        {
+            std::unique_lock<std::mutex> lk(sv->mu);
+            sv->cv.wait(lk, [&] { return sv->stop || !sv->queue.empty() || !sv->active.empty(); });
+            if (sv->stop) break;
+            // drop cancelled residents
+            for (auto it = sv->active.begin(); it != sv->active.end();) {
+                if ((*it)->cancel) {
+                    (*it)->status = SWB_ERR_CANCELLED;
+                    (*it)->t_done = sv->now();
+                    cudaFreeAsync((*it)->dev, sv->stream);
+                    (*it)->dev = nullptr;
+                    sv->in_use -= (*it)->bytes;
+                    it = sv->active.erase(it);
+                    changed = true;
+                } else {
+                    ++it;
+                }
+            }
+            // FIFO admission by HBM footprint
+            while (!sv->queue.empty()) {
+                Req *r = sv->reqs[sv->queue.front()].get();
+                if (r->cancel) {
+                    r->status = SWB_ERR_CANCELLED;
+                    r->t_done = sv->now();
+                    sv->queue.pop_front();
+                    continue;
+                }
+                if (sv->in_use + r->bytes > sv->budget) break;
+                sv->queue.pop_front();
+                sv->in_use += r->bytes;
+                r->status = 1;
+                r->t_admit = sv->now();
+                admitted.push_back(r);
+                sv->st.admitted++;
+            }
+        }
+        for (Req *r : admitted) {
+            if (admit_device(sv, r)) {
+                std::lock_guard<std::mutex> g(sv->mu);
+                sv->active.push_back(r);
+                changed = true;
+            } else {
+                std::lock_guard<std::mutex> g(sv->mu);
+                r->status = SWB_ERR_OOM;
+                r->t_done = sv->now();
+                sv->in_use -= r->bytes;
+                sv->st.rejected++;
+            }
+        }
+        if (sv->active.empty()) continue;
+        if (changed && !upload_table(sv)) {
+            set_error(sv, "tile table upload failed");
+            std::this_thread::sleep_for(std::chrono::milliseconds(10));
+            continue;
+        }
+        int64_t tick = sv->steps_per_tick;
+        for (Req *r : sv->active) tick = std::min<int64_t>(tick, r->nsteps - r->done);
+        const int ntiles = count_tiles(sv);
+        const int grid = std::min(ntiles, sms * occ);
+        const double tb = sv->now();
+        cudaError_t e = cudaSuccess;
+        for (int64_t k = 0; k < tick && e == cudaSuccess; ++k)
+            e = swb::launch_batch_step(sv->precision, sv->d_args, sv->d_tiles, ntiles, grid, sv->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(sv->stream);
+        double lu = 0.0;
+        std::vector<Req *> finished;
+        {
+            std::lock_guard<std::mutex> g(sv->mu);
+            for (Req *r : sv->active) {
+                r->done += tick;
+                lu += (double)r->p.Lx * r->p.Ly * (double)tick;
+                if (r->done >= r->nsteps) finished.push_back(r);
+            }
+        }
+        for (Req *r : finished) {
+            r->result.resize((size_t)r->p.Lx * r->p.Ly);
+            cudaError_t de = swb::lattice_download_height(r->a, sv->precision, false, r->result.data(), sv->stream);
+            cudaFreeAsync(r->dev, sv->stream);
+            r->dev = nullptr;
+            std::lock_guard<std::mutex> g(sv->mu);
+            r->status = (e == cudaSuccess && de == cudaSuccess) ? 2 : SWB_ERR_CUDA;
+            r->t_done = sv->now();
+            sv->in_use -= r->bytes;
+            sv->st.completed++;
+            r->h0.clear();
+            r->h0.shrink_to_fit();
+        }
+        {
+            std::lock_guard<std::mutex> g(sv->mu);
+            if (!finished.empty()) {
+                sv->active.erase(std::remove_if(sv->active.begin(), sv->active.end(),
+                                                [](Req *r) { return r->status != 1; }),
+                                 sv->active.end());
+                changed = true;
+            }
+            sv->st.lattice_updates += lu;
+            sv->st.busy_seconds += sv->now() - tb;
+            sv->st.ticks++;
+            if (e != cudaSuccess) sv->err = std::string("tick: ") + cudaGetErrorString(e);
+        }
+        if (!finished.empty() && !sv->active.empty()) upload_table(sv);
+    }
+    cudaStreamSynchronize(sv->stream);
+}
+
+}  // namespace
+
+extern "C" {
+
+int swb_server_create(size_t hbm_budget, int precision, int steps_per_tick, swb_server **out) {
+    if (!out || hbm_budget == 0 || steps_per_tick < 1) return sfail(SWB_ERR_ARG, "bad arguments");
+    if (precision != SWB_F64 && precision != SWB_F32 && precision != SWB_F16)
+        return sfail(SWB_ERR_ARG, "server precision must be SWB_F64, SWB_F32 or SWB_F16");
+    *out = nullptr;
+    swb_server *sv = new swb_server();
+    sv->budget = hbm_budget;
+    sv->precision = precision;
+    sv->steps_per_tick = steps_per_tick;
+    cudaGetDevice(&sv->device);
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = sv->device;
+    cudaError_t e = cudaStreamCreateWithFlags(&sv->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMemPoolCreate(&sv->pool, &props);
+    if (e == cudaSuccess) {
+        uint64_t thr = UINT64_MAX;  // keep freed blocks cached in this pool
+        e = cudaMemPoolSetAttribute(sv->pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+    if (e != cudaSuccess) {
+        if (sv->stream) cudaStreamDestroy(sv->stream);
+        delete sv;
+        return sfail(SWB_ERR_CUDA, std::string("server create: ") + cudaGetErrorString(e));
+    }
+    sv->st.hbm_budget = hbm_budget;
+    sv->worker = std::thread(worker_main, sv);
+    *out = sv;
+    return SWB_OK;
+}
+
+int swb_server_destroy(swb_server *sv) {
+    if (!sv) return SWB_OK;
+    {
+        std::lock_guard<std::mutex> g(sv->mu);
+        sv->stop = true;
+    }
+    sv->cv.notify_all();
+    if (sv->worker.joinable()) sv->worker.join();
+    for (auto &kv : sv->reqs)
+        if (kv.second->dev) cudaFreeAsync(kv.second->dev, sv->stream);
+    cudaStreamSynchronize(sv->stream);
+    cudaFree(sv->d_args);
+    cudaFree(sv->d_tiles);
+    cudaFree(sv->staging);
+    if (sv->pool) cudaMemPoolDestroy(sv->pool);
+    cudaStreamDestroy(sv->stream);
+    delete sv;
+    return SWB_OK;
+}
+
+int swb_server_submit(swb_server *sv, const swb_params *p, const double *h0, double theta0,
+                      double dtheta, double v, int64_t nsteps, int64_t *id) {
+    if (!sv || !p || !h0 || !id || nsteps < 1) return sfail(SWB_ERR_ARG, "bad arguments");
+    if (p->Lx < 1 || p->Ly < 1 || (long long)p->Lx * p->Ly * 9 >= (1LL << 31) || !(p->tau > 0) ||
+        p->n <= p->m || p->m < 1 || !(p->hmin > 0))
+        return sfail(SWB_ERR_ARG, "invalid params");
+    if (p->kbt != 0.0) return sfail(SWB_ERR_UNSUPPORTED, "kbt != 0 is not supported");
+    auto r = std::make_unique<Req>();
+    r->p = *p;
+    r->h0.assign(h0, h0 + (size_t)p->Lx * p->Ly);
+    r->theta0 = theta0;
+    r->dtheta = dtheta;
+    r->v = v;
+    r->nsteps = nsteps;
+    r->L = swb::lattice_layout(*p, sv->precision);
+    r->bytes = r->L.total;
+    {
+        std::lock_guard<std::mutex> g(sv->mu);
+        r->t_submit = sv->now();
+        r->id = sv->next_id++;
+        *id = r->id;
+        sv->st.submitted++;
+        if (r->bytes > sv->budget) {
+            r->status = SWB_ERR_OOM;
+            r->t_done = r->t_submit;
+            sv->st.rejected++;
+        } else {
+            sv->queue.push_back(r->id);
+        }
+        sv->reqs[r->id] = std::move(r);
+    }
+    sv->cv.notify_all();
+    return SWB_OK;
+}
+
+int swb_server_poll(swb_server *sv, int64_t id, double *h_out, swb_request_info *info) {
+    if (!sv) return sfail(SWB_ERR_ARG, "server is NULL");
+    std::lock_guard<std::mutex> g(sv->mu);
+    auto it = sv->reqs.find(id);
+    if (it == sv->reqs.end()) return sfail(SWB_ERR_NOT_FOUND, "unknown request id");
+    Req *r = it->second.get();
+    if (info) {
+        info->id = r->id;
+        info->status = r->status;
+        info->steps_done = r->done;
+        info->t_submit = r->t_submit;
+        info->t_admit = r->t_admit;
+        info->t_done = r->t_done;
+    }
+    if (r->status == 2) {
+        if (h_out) std::copy(r->result.begin(), r->result.end(), h_out);
+        return 1;
+    }
+    if (r->status < 0) return r->status;
+    return 0;
+}
+
+int swb_server_cancel(swb_server *sv, int64_t id) {
+    if (!sv) return sfail(SWB_ERR_ARG, "server is NULL");
+    {
+        std::lock_guard<std::mutex> g(sv->mu);
+        auto it = sv->reqs.find(id);
+        if (it == sv->reqs.end()) return sfail(SWB_ERR_NOT_FOUND, "unknown request id");
+        it->second->cancel = true;
+    }
+    sv->cv.notify_all();
+    return SWB_OK;
+}
+
+int swb_server_stats_get(swb_server *sv, swb_server_stats *out) {
+    if (!sv || !out) return sfail(SWB_ERR_ARG, "bad arguments");
+    std::lock_guard<std::mutex> g(sv->mu);
+    *out = sv->st;
+    out->queued = (int64_t)sv->queue.size();
+    out->running = (int64_t)sv->active.size();
+    out->hbm_in_use = sv->in_use;
+    out->hbm_budget = sv->budget;
+    return SWB_OK;
+}
+
+double swb_server_clock(swb_server *sv) { return sv ? sv->now() : 0.0; }
+
+}  // extern "C"

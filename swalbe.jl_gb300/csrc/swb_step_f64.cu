@@ -1,0 +1,302 @@
+// swb_step_f64.cu -- Float64 kernels.  Compiled with --fmad=false so that no
+// a*b+c is contracted into an FMA: the reference (Julia broadcasts) rounds
+// every operation, and this translation unit reproduces it bit for bit.
+//
+// Contents: the fused step in Float64 (literal arithmetic), the plain
+// one-kernel-per-reference-op path, and the standalone measure reduction.
+#include "swb_step_impl.cuh"
+
+namespace swb {
+
+// ------------------------------------------------------------ fused, Float64
+cudaError_t launch_fused_step_f64(const StepArgs &a, cudaStream_t st) {
+    dim3 grid(a.tiles_x, a.tiles_y);
+    fused_step_kernel<StoreF64><<<grid, kThreads, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+static int grid_for(long long n, int threads) {
+    long long b = (n + threads - 1) / threads;
+    if (b > 152LL * 32) b = 152LL * 32;
+    return (int)(b < 1 ? 1 : b);
+}
+
+cudaError_t launch_moments_f64(const StepArgs &a, cudaStream_t st) {
+    moments_kernel<StoreF64><<<grid_for((long long)a.Lx * a.Ly, 256), 256, 0, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fout_f64(const StepArgs &a, double *out, cudaStream_t st) {
+    fout_kernel<StoreF64><<<grid_for((long long)a.Lx * a.Ly, 256), 256, 0, st>>>(a, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pressure_now_f64(const StepArgs &a, double *out, cudaStream_t st) {
+    pressure_now_kernel<StoreF64><<<grid_for((long long)a.Lx * a.Ly, 256), 256, 0, st>>>(a, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_step_f64(const StepArgs *d_args, const TileRef *d_tiles, int ntiles,
+                                  int grid, cudaStream_t st) {
+    batch_step_kernel<StoreF64><<<grid, kThreads, 0, st>>>(d_args, d_tiles, ntiles);
+    return cudaGetLastError();
+}
+
+int batch_blocks_per_sm_f64() {
+    int n = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_step_kernel<StoreF64>, kThreads, 0);
+    return n < 1 ? 1 : n;
+}
+
+// ------------------------------------------------------------ plain path
+// One kernel per reference function, Float64, same per-element operations.
+// Neighbour (i±1, j±1) indexing replaces the reference's circshift! copies.
+#define PLAIN_LOOP(s)                                                              \
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < (s).N; \
+         c += (long long)gridDim.x * blockDim.x)
+
+struct Nb {
+    long long c, ip, im, jp, jm, ipjp, imjp, imjm, ipjm;  // reference names
+};
+__device__ __forceinline__ Nb neighbours(long long c, int Lx, int Ly) {
+    const int i = (int)(c % Lx), j = (int)(c / Lx);
+    const int im1 = i == 0 ? Lx - 1 : i - 1, ip1 = i == Lx - 1 ? 0 : i + 1;
+    const int jm1 = j == 0 ? Ly - 1 : j - 1, jp1 = j == Ly - 1 ? 0 : j + 1;
+    Nb n;
+    n.c = c;
+    n.ip = (long long)j * Lx + im1;      // h[i-1, j]
+    n.im = (long long)j * Lx + ip1;      // h[i+1, j]
+    n.jp = (long long)jm1 * Lx + i;      // h[i, j-1]
+    n.jm = (long long)jp1 * Lx + i;      // h[i, j+1]
+    n.ipjp = (long long)jm1 * Lx + im1;  // h[i-1, j-1]
+    n.imjp = (long long)jm1 * Lx + ip1;  // h[i+1, j-1]
+    n.imjm = (long long)jp1 * Lx + ip1;  // h[i+1, j+1]
+    n.ipjm = (long long)jp1 * Lx + im1;  // h[i-1, j+1]
+    return n;
+}
+
+__global__ void k_filmpressure(PlainState s, const double *kapF, double kap, double gamma, int n,
+                               int m, double hmin, double hcrit) {
+    PLAIN_LOOP(s) {
+        const Nb b = neighbours(c, s.Lx, s.Ly);
+        const double *h = s.h;
+        s.p[c] = pressure_cell<true, double>(h[c], h[b.ip], h[b.jp], h[b.im], h[b.jm], h[b.ipjp],
+                                             h[b.imjp], h[b.imjm], h[b.ipjm],
+                                             kapF ? kapF[c] : kap, gamma, hmin, hcrit, n, m);
+    }
+}
+
+__global__ void k_hgradp(PlainState s) {
+    PLAIN_LOOP(s) {
+        const Nb b = neighbours(c, s.Lx, s.Ly);
+        const double *p = s.p;
+        double gx, gy;
+        grad9<double>(p[b.ip], p[b.jp], p[b.im], p[b.jm], p[b.ipjp], p[b.imjp], p[b.imjm],
+                      p[b.ipjm], gx, gy);
+        s.hgx[c] = s.h[c] * gx;
+        s.hgy[c] = s.h[c] * gy;
+    }
+}
+
+__global__ void k_slippage(PlainState s, double delta6, double delta3sq, double mu6) {
+    PLAIN_LOOP(s) {
+        const double h = s.h[c];
+        s.sx[c] = (mu6 * h * s.ux[c]) / (2.0 * (h * h) + delta6 * h + delta3sq);
+        s.sy[c] = (mu6 * h * s.uy[c]) / (2.0 * (h * h) + delta6 * h + delta3sq);
+    }
+}
+
+__global__ void k_force_sum(PlainState s) {
+    PLAIN_LOOP(s) {
+        s.Fx[c] = -s.hgx[c] - s.sx[c];
+        s.Fy[c] = -s.hgy[c] - s.sy[c];
+    }
+}
+
+__global__ void k_inclination(PlainState s, double ax, double ay, double fac) {
+    PLAIN_LOOP(s) {
+        s.Fx[c] = s.Fx[c] + (s.h[c] * ax) * fac;
+        s.Fy[c] = s.Fy[c] + (s.h[c] * ay) * fac;
+    }
+}
+
+__global__ void k_equilibrium(PlainState s, double g) {
+    PLAIN_LOOP(s) {
+        double fe[9];
+        const double ux = s.ux[c], uy = s.uy[c];
+        feq_literal<double>(s.h[c], ux, uy, g, fe);
+        s.vsq[c] = ux * ux + uy * uy;
+        for (int q = 0; q < 9; ++q) s.feq[q * s.N + c] = fe[q];
+    }
+}
+
+__global__ void k_collide(PlainState s, double omeg, double invtau) {
+    PLAIN_LOOP(s) {
+        const double Fx = s.Fx[c], Fy = s.Fy[c];
+        for (int q = 0; q < 9; ++q) {
+            double v = omeg * s.ftemp[q * s.N + c] + invtau * s.feq[q * s.N + c];
+            if (q > 0) v = v + source<double>(q, Fx, Fy);
+            s.fout[q * s.N + c] = v;
+        }
+    }
+}
+
+__global__ void k_stream(PlainState s) {  // circshift!(ft_q, fo_q, c_q)
+    const int CX[9] = {0, 1, 0, -1, 0, 1, -1, -1, 1};
+    const int CY[9] = {0, 0, 1, 0, -1, 1, 1, -1, -1};
+    PLAIN_LOOP(s) {
+        const int i = (int)(c % s.Lx), j = (int)(c / s.Lx);
+        for (int q = 0; q < 9; ++q) {
+            const int si = wrapc(i - CX[q], s.Lx), sj = wrapc(j - CY[q], s.Ly);
+            s.ftemp[q * s.N + c] = s.fout[q * s.N + (long long)sj * s.Lx + si];
+        }
+    }
+}
+
+__global__ void k_moments(PlainState s) {
+    PLAIN_LOOP(s) {
+        double f[9], h, jx, jy, ux, uy;
+        for (int q = 0; q < 9; ++q) f[q] = s.fout[q * s.N + c];
+        moments9<true>(f, h, jx, jy);
+        velocity<true>(h, jx, jy, ux, uy);
+        s.h[c] = h;
+        s.ux[c] = ux;
+        s.uy[c] = uy;
+    }
+}
+
+#define PLAIN_LAUNCH(kernel, s, st, ...)                                  \
+    do {                                                                  \
+        count_launches(1);                                                \
+        kernel<<<grid_for((s).N, 256), 256, 0, st>>>(s, ##__VA_ARGS__);   \
+        return cudaGetLastError();                                        \
+    } while (0)
+
+cudaError_t plain_filmpressure(const PlainState &s, const double *kapF, double kap, double gamma,
+                               int n, int m, double hmin, double hcrit, cudaStream_t st) {
+    PLAIN_LAUNCH(k_filmpressure, s, st, kapF, kap, gamma, n, m, hmin, hcrit);
+}
+cudaError_t plain_hgradp(const PlainState &s, cudaStream_t st) { PLAIN_LAUNCH(k_hgradp, s, st); }
+cudaError_t plain_slippage(const PlainState &s, double delta, double mu, cudaStream_t st) {
+    PLAIN_LAUNCH(k_slippage, s, st, 6.0 * delta, 3.0 * (delta * delta), 6.0 * mu);
+}
+cudaError_t plain_force_sum(const PlainState &s, cudaStream_t st) {
+    PLAIN_LAUNCH(k_force_sum, s, st);
+}
+cudaError_t plain_inclination(const PlainState &s, double ax, double ay, double fac,
+                              cudaStream_t st) {
+    PLAIN_LAUNCH(k_inclination, s, st, ax, ay, fac);
+}
+cudaError_t plain_equilibrium(const PlainState &s, double g, cudaStream_t st) {
+    PLAIN_LAUNCH(k_equilibrium, s, st, g);
+}
+cudaError_t plain_collide(const PlainState &s, double omeg, double invtau, cudaStream_t st) {
+    PLAIN_LAUNCH(k_collide, s, st, omeg, invtau);
+}
+cudaError_t plain_stream(const PlainState &s, cudaStream_t st) {
+    count_launches(1);
+    k_stream<<<grid_for(s.N, 256), 256, 0, st>>>(s);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    // fout .= ftemp (src/collide.jl:294)
+    return cudaMemcpyAsync(s.fout, s.ftemp, 9 * s.N * sizeof(double), cudaMemcpyDeviceToDevice,
+                           st);
+}
+cudaError_t plain_moments(const PlainState &s, cudaStream_t st) { PLAIN_LAUNCH(k_moments, s, st); }
+
+// ------------------------------------------------------------ measures
+// Grid-stride partials per block, then the last block (ticket) reduces the
+// partials in a fixed order and writes one Record.
+template <class R>
+__global__ void __launch_bounds__(256) measure_kernel(const R *h, int Lx, int Ly, R thr,
+                                                      const R *cosF, double cos_theta,
+                                                      double *scratch, unsigned int *ticket,
+                                                      Record *rec, long long t) {
+    __shared__ PartT<R> red[8];
+    __shared__ PartT<double> redd[8];
+    __shared__ int last;
+    const long long N = (long long)Lx * Ly;
+    PartT<R> p;
+    part_init(p);
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < N;
+         c += (long long)gridDim.x * blockDim.x) {
+        const R v = h[c];
+        mass_add(p, v);
+        const bool wet = v > thr;
+        p.wet += wet ? 1 : 0;
+        p.hmax = fmax(p.hmax, v);
+        p.hmin = fmin(p.hmin, v);
+        if (wet) {
+            const Nb b = neighbours(c, Lx, Ly);
+            R gx, gy;
+            grad9<R>(h[b.ip], h[b.jp], h[b.im], h[b.jm], h[b.ipjp], h[b.imjp], h[b.imjm],
+                     h[b.ipjm], gx, gy);
+            p.area += sqrt(gx * gx + gy * gy + R(1));
+            if (cosF) p.cossum += cosF[c];
+        }
+    }
+    PartT<R> tot = block_reduce<256>(p, red);
+    if (threadIdx.x == 0) {
+        double *pp = scratch + (size_t)blockIdx.x * kNPart;
+        pp[0] = (double)tot.mhi + (double)tot.mlo;
+        pp[1] = (double)tot.wet;
+        pp[2] = (double)tot.hmax;
+        pp[3] = (double)tot.hmin;
+        pp[4] = (double)tot.area;
+        pp[5] = (double)tot.cossum;
+        __threadfence();
+        last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    PartT<double> acc;
+    part_init(acc);
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
+        const double *pp = scratch + (size_t)b * kNPart;
+        PartT<double> q;
+        q.mhi = __ldcg(pp + 0);
+        q.mlo = 0.0;
+        q.wet = (int)__ldcg(pp + 1);
+        q.hmax = __ldcg(pp + 2);
+        q.hmin = __ldcg(pp + 3);
+        q.area = __ldcg(pp + 4);
+        q.cossum = __ldcg(pp + 5);
+        part_merge(acc, q);
+    }
+    acc = block_reduce<256>(acc, redd);
+    if (threadIdx.x == 0) {
+        rec->t = t;
+        rec->mass = acc.mhi + acc.mlo;
+        rec->wetted = (double)acc.wet;
+        rec->hmax = acc.hmax;
+        rec->hmin = acc.hmin;
+        rec->area = acc.area;
+        rec->cos_sum = cosF ? acc.cossum : (double)acc.wet * cos_theta;
+        *ticket = 0u;
+    }
+}
+
+int measure_blocks(long long N) {
+    long long b = (N + 255) / 256;
+    if (b > 1024) b = 1024;
+    return (int)(b < 1 ? 1 : b);
+}
+
+cudaError_t launch_measure(const void *h, int is_double, int Lx, int Ly, double hthresh,
+                           const void *cosF, double cos_theta, double *scratch, unsigned int *ticket,
+                           Record *rec, long long t, cudaStream_t st) {
+    const int blocks = measure_blocks((long long)Lx * Ly);
+    count_launches(1);
+    if (is_double)
+        measure_kernel<double><<<blocks, 256, 0, st>>>((const double *)h, Lx, Ly, hthresh,
+                                                       (const double *)cosF, cos_theta, scratch, ticket,
+                                                       rec, t);
+    else
+        measure_kernel<float><<<blocks, 256, 0, st>>>((const float *)h, Lx, Ly, (float)hthresh,
+                                                      (const float *)cosF, cos_theta, scratch, ticket,
+                                                      rec, t);
+    return cudaGetLastError();
+}
+
+}  // namespace swb

@@ -1,0 +1,759 @@
+// swb_step_impl.cuh -- the fused D2Q9 thin-film step, one CTA per tile.
+//
+// One launch performs one iteration of the reference's time loop
+// (src/simulate.jl:15-22) on a lattice:
+//
+//   pull-stream  f(t-1)_q(x) = fpost(t-1)_q(x - c_q)        BGKandStream! streaming
+//   moments      h, u of f(t-1)                              moments!
+//   pressure     p = Π(h) - γ ∇²h on the tile + 1 halo        filmpressure!
+//   force        F = -h∇p - slip (+ inclination)              h∇p!, slippage!, inclination!
+//   collision    fpost(t)_q = (1-1/τ) f_q + feq_q/τ + S_q     equilibrium!, BGKandStream!
+//
+// Storage is the reference's own layout: nine SoA population planes,
+// column-major (x fastest).  The kernel keeps post-collision populations and
+// pulls them at the start of the next step, so a step reads 9 and writes 9
+// values per cell; the pressure's radius-2 dependence on h is served from a
+// (TX+4)x(TY+4) shared-memory tile of heights computed from the pulled
+// populations (halo reads come from L2).
+//
+// Two arithmetic variants:
+//   Literal (Float64): the reference's operations in its association order,
+//     compiled with --fmad=false; bit-identical to the CPU oracle.
+//   Fast (FP32): the same physics with fewer operations; f0 is stored as
+//     h - Σ_{q>0} f_q (using the values as stored) so that storage rounding
+//     does not leak mass, plus an optional FP64-measured mass correction.
+#pragma once
+#include <cuda_fp16.h>
+
+#include "swb_internal.h"
+
+namespace swb {
+
+// ------------------------------------------------------------ storage
+struct StoreF64 {
+    using real = double;
+    static constexpr bool kLiteral = true;
+    static constexpr bool kHalf = false;
+    __device__ __forceinline__ static double ld(const void *b, long long pitch, int q, int i) {
+        return __ldg(reinterpret_cast<const double *>(b) + q * pitch + i);
+    }
+    __device__ __forceinline__ static void st(void *b, long long pitch, int q, int i, double v) {
+        reinterpret_cast<double *>(b)[q * pitch + i] = v;
+    }
+    __device__ __forceinline__ static double rt(int, double v) { return v; }
+};
+
+struct StoreF32 {
+    using real = float;
+    static constexpr bool kLiteral = false;
+    static constexpr bool kHalf = false;
+    __device__ __forceinline__ static float ld(const void *b, long long pitch, int q, int i) {
+        return __ldg(reinterpret_cast<const float *>(b) + q * pitch + i);
+    }
+    __device__ __forceinline__ static void st(void *b, long long pitch, int q, int i, float v) {
+        reinterpret_cast<float *>(b)[q * pitch + i] = v;
+    }
+    __device__ __forceinline__ static float rt(int, float v) { return v; }
+};
+
+// f0 as an FP32 plane, f1..f8 as FP16 planes holding 2^10 f_q (the scale
+// keeps populations of order 1e-5..1e-2 in the normal FP16 range).
+struct StoreF16 {
+    using real = float;
+    static constexpr bool kLiteral = false;
+    static constexpr bool kHalf = true;
+    static constexpr float kScale = 1024.0f;
+    static constexpr float kInv = 1.0f / 1024.0f;
+    __device__ __forceinline__ static const __half *hp(const void *b, long long pitch) {
+        return reinterpret_cast<const __half *>(reinterpret_cast<const float *>(b) + pitch);
+    }
+    __device__ __forceinline__ static float ld(const void *b, long long pitch, int q, int i) {
+        if (q == 0) return __ldg(reinterpret_cast<const float *>(b) + i);
+        return __half2float(__ldg(hp(b, pitch) + (q - 1) * pitch + i)) * kInv;
+    }
+    __device__ __forceinline__ static void st(void *b, long long pitch, int q, int i, float v) {
+        if (q == 0) {
+            reinterpret_cast<float *>(b)[i] = v;
+        } else {
+            __half *h = const_cast<__half *>(hp(b, pitch));
+            h[(q - 1) * pitch + i] = __float2half_rn(v * kScale);
+        }
+    }
+    __device__ __forceinline__ static float rt(int q, float v) {
+        return q == 0 ? v : __half2float(__float2half_rn(v * kScale)) * kInv;
+    }
+};
+
+// ------------------------------------------------------------ helpers
+__device__ __forceinline__ int wrapc(int x, int L) {
+    while (x < 0) x += L;
+    while (x >= L) x -= L;
+    return x;
+}
+
+template <class R>
+__device__ __forceinline__ R pow_loop(R x, int n) {  // power_broad (src/pressure.jl:363-369)
+    R t = R(1);
+    for (int i = 0; i < n; ++i) t *= x;
+    return t;
+}
+
+__device__ __forceinline__ double cospi_r(double x) { return cospi(x); }
+__device__ __forceinline__ float cospi_r(float x) { return cospif(x); }
+__device__ __forceinline__ double sinpi_r(double x) { return sinpi(x); }
+__device__ __forceinline__ float sinpi_r(float x) { return sinpif(x); }
+__device__ __forceinline__ double tanh_r(double x) { return tanh(x); }
+__device__ __forceinline__ float tanh_r(float x) { return tanhf(x); }
+
+// kappa prefactor ((1 - cospi θ)(n-1)(m-1))/((n-m) hmin), left to right as
+// in src/pressure.jl:141-147.
+template <class R>
+__device__ __forceinline__ R kappa_of(R theta, int n, int m, R hmin) {
+    R a = R(1) - cospi_r(theta);
+    a = a * R(n - 1);
+    a = a * R(m - 1);
+    return a / (R(n - m) * hmin);
+}
+
+// Pull the nine populations of cell (gx, gy) from the post-collision buffer:
+// f_q(x) = fpost_q(x - c_q), c_q as in src/collide.jl:283-291.
+template <class S>
+__device__ __forceinline__ void pull9(const void *src, long long pitch, int Lx, int gx, int gy,
+                                      int gxm, int gxp, int gym, int gyp,
+                                      typename S::real ft[9]) {
+    const int rc = gy * Lx, rm = gym * Lx, rp = gyp * Lx;
+    ft[0] = S::ld(src, pitch, 0, rc + gx);
+    ft[1] = S::ld(src, pitch, 1, rc + gxm);
+    ft[2] = S::ld(src, pitch, 2, rm + gx);
+    ft[3] = S::ld(src, pitch, 3, rc + gxp);
+    ft[4] = S::ld(src, pitch, 4, rp + gx);
+    ft[5] = S::ld(src, pitch, 5, rm + gxm);
+    ft[6] = S::ld(src, pitch, 6, rm + gxp);
+    ft[7] = S::ld(src, pitch, 7, rp + gxp);
+    ft[8] = S::ld(src, pitch, 8, rp + gxm);
+}
+
+// Sum of the eight moving populations (pairwise).
+template <class R>
+__device__ __forceinline__ R small8(const R f[9]) {
+    return ((f[1] + f[3]) + (f[2] + f[4])) + ((f[5] + f[7]) + (f[6] + f[8]));
+}
+
+// moments! (src/moments.jl:43-51): h and the momentum numerators.
+template <bool LIT, class R>
+__device__ __forceinline__ void moments9(const R f[9], R &h, R &jx, R &jy) {
+    if constexpr (LIT) {
+        R s = R(0);
+#pragma unroll
+        for (int q = 0; q < 9; ++q) s = s + f[q];
+        h = s;
+        jx = f[1] - f[3] + f[5] - f[6] - f[7] + f[8];
+        jy = f[2] - f[4] + f[5] + f[6] - f[7] - f[8];
+    } else {
+        h = f[0] + small8(f);
+        jx = (f[1] - f[3]) + (f[5] - f[7]) + (f[8] - f[6]);
+        jy = (f[2] - f[4]) + (f[5] - f[7]) + (f[6] - f[8]);
+    }
+}
+
+// Rounding error of h = f0 + small8(f) (Fast2Sum: exact when |f0| >= |small|,
+// which holds for thin-film populations where f0 ~ h dominates).
+template <class R>
+__device__ __forceinline__ R moments_lo(const R f[9], R h) {
+    return small8(f) - (h - f[0]);
+}
+
+template <bool LIT, class R>
+__device__ __forceinline__ void velocity(R h, R jx, R jy, R &ux, R &uy) {
+    if constexpr (LIT) {
+        ux = jx / h;
+        uy = jy / h;
+    } else {
+        R inv = R(1) / h;
+        ux = jx * inv;
+        uy = jy * inv;
+    }
+}
+
+// filmpressure! for one cell (src/pressure.jl:141-153).  Neighbour names
+// follow the reference: ip = h[i-1,j], im = h[i+1,j], jp = h[i,j-1], ...
+template <bool LIT, class R>
+__device__ __forceinline__ R pressure_cell(R h, R ip, R jp, R im, R jm, R ipjp, R imjp, R imjm,
+                                           R ipjm, R kap, R gamma, R hmin, R hcrit, int n,
+                                           int m) {
+    R x = hmin / (h + hcrit);
+    R pn, pm;
+    if (!LIT && n == 9 && m == 3) {
+        R x3 = x * x * x;
+        pn = x3 * x3 * x3;
+        pm = x3;
+    } else {
+        pn = pow_loop(x, n);
+        pm = pow_loop(x, m);
+    }
+    R p = -gamma * (kap * (pn - pm));
+    R lap = R(2.0 / 3.0) * (((jp + ip) + im) + jm) + R(1.0 / 6.0) * (((ipjp + imjp) + imjm) + ipjm) -
+            R(10.0 / 3.0) * h;
+    return p - gamma * lap;
+}
+
+// Gradient stencil of h∇p! / ∇f_simple! (src/forcing.jl:181-184).
+template <class R>
+__device__ __forceinline__ void grad9(R ip, R jp, R im, R jm, R ipjp, R imjp, R imjm, R ipjm,
+                                      R &gx, R &gy) {
+    gx = R(-1.0 / 3.0) * (ip - im) - R(1.0 / 12.0) * (((ipjp - imjp) - imjm) + ipjm);
+    gy = R(-1.0 / 3.0) * (jp - jm) - R(1.0 / 12.0) * (((ipjp + imjp) - imjm) - ipjm);
+}
+
+// equilibrium! for one cell, literal (src/equilibrium.jl:67-114).
+template <class R>
+__device__ __forceinline__ void feq_literal(R h, R ux, R uy, R g, R fe[9]) {
+    const R g0 = R(1.5) * g, w1 = R(1.0 / 9.0), w5 = R(1.0 / 36.0);
+    R vsq = ux * ux + uy * uy;
+    fe[0] = h * ((R(1) - R(5.0 / 6.0) * g * h) - R(2.0 / 3.0) * vsq);
+    fe[1] = w1 * h * (g0 * h + R(3) * ux + R(4.5) * (ux * ux) - R(1.5) * vsq);
+    fe[2] = w1 * h * (g0 * h + R(3) * uy + R(4.5) * (uy * uy) - R(1.5) * vsq);
+    fe[3] = w1 * h * (g0 * h - R(3) * ux + R(4.5) * (ux * ux) - R(1.5) * vsq);
+    fe[4] = w1 * h * (g0 * h - R(3) * uy + R(4.5) * (uy * uy) - R(1.5) * vsq);
+    fe[5] = w5 * h * (g0 * h + R(3) * (ux + uy) + R(4.5) * ((ux + uy) * (ux + uy)) - R(1.5) * vsq);
+    fe[6] = w5 * h * (g0 * h + R(3) * (uy - ux) + R(4.5) * ((uy - ux) * (uy - ux)) - R(1.5) * vsq);
+    fe[7] = w5 * h * (g0 * h - R(3) * (ux + uy) + R(4.5) * ((ux + uy) * (ux + uy)) - R(1.5) * vsq);
+    fe[8] = w5 * h * (g0 * h + R(3) * (ux - uy) + R(4.5) * ((ux - uy) * (ux - uy)) - R(1.5) * vsq);
+}
+
+// equilibrium for q = 1..8, FP32 (same polynomial, shared subexpressions).
+__device__ __forceinline__ void feq_fast(float h, float ux, float uy, float g, float fe[9]) {
+    const float vsq = ux * ux + uy * uy;
+    const float base = 1.5f * g * h - 1.5f * vsq;
+    const float w1h = h * (1.0f / 9.0f), w5h = h * (1.0f / 36.0f);
+    const float a = ux + uy, b = uy - ux;
+    const float ux2 = 4.5f * ux * ux, uy2 = 4.5f * uy * uy;
+    const float a2 = 4.5f * a * a, b2 = 4.5f * b * b;
+    fe[1] = w1h * (base + ux2 + 3.0f * ux);
+    fe[3] = w1h * (base + ux2 - 3.0f * ux);
+    fe[2] = w1h * (base + uy2 + 3.0f * uy);
+    fe[4] = w1h * (base + uy2 - 3.0f * uy);
+    fe[5] = w5h * (base + a2 + 3.0f * a);
+    fe[7] = w5h * (base + a2 - 3.0f * a);
+    fe[6] = w5h * (base + b2 + 3.0f * b);
+    fe[8] = w5h * (base + b2 - 3.0f * b);
+    fe[0] = 0.0f;  // f0 is closed by mass conservation in the fast path
+}
+
+// Force source of BGKandStream! (src/collide.jl:272-280).
+template <class R>
+__device__ __forceinline__ R source(int q, R Fx, R Fy) {
+    switch (q) {
+        case 1: return R(1.0 / 3.0) * Fx;
+        case 2: return R(1.0 / 3.0) * Fy;
+        case 3: return -(R(1.0 / 3.0) * Fx);
+        case 4: return -(R(1.0 / 3.0) * Fy);
+        case 5: return R(1.0 / 24.0) * (Fx + Fy);
+        case 6: return R(1.0 / 24.0) * (Fy - Fx);
+        case 7: return -(R(1.0 / 24.0) * (Fx + Fy));
+        case 8: return R(1.0 / 24.0) * (Fx - Fy);
+        default: return R(0);
+    }
+}
+
+__device__ __forceinline__ unsigned int mix32(unsigned int a, unsigned int b) {
+    unsigned int x = a * 0x9E3779B9u ^ (b * 0x85EBCA6Bu + 0x27d4eb2fu);
+    x ^= x >> 16;
+    x *= 0x7FEB352Du;
+    x ^= x >> 15;
+    x *= 0x846CA68Bu;
+    x ^= x >> 16;
+    return x;
+}
+
+// v + c with stochastic rounding to the ulp of v (c is far below one ulp:
+// the per-cell share of the mass correction).
+__device__ __forceinline__ float add_stochastic(float v, float c, unsigned int rnd) {
+    int ex = (__float_as_int(v) >> 23) & 0xff;
+    float ulp = __int_as_float(max(ex - 23, 1) << 23);
+    float r = c * __frcp_rn(ulp);
+    float fl = floorf(r);
+    float u = (float)(rnd >> 8) * (1.0f / 16777216.0f);
+    float k = fl + ((u < r - fl) ? 1.0f : 0.0f);
+    return v + k * ulp;
+}
+
+// ------------------------------------------------------------ reductions
+// Per-block partial measures in the compute type R.  The mass is a two-term
+// (hi + lo) compensated sum so that FP32 blocks keep FP64-grade mass; only the
+// per-block result is converted to double, which keeps FP64 instructions (1/64
+// of the FP32 rate on GB300) out of the per-cell path.
+template <class R>
+struct PartT {
+    R mhi, mlo;
+    int wet;
+    R hmax, hmin, area, cossum;
+};
+
+template <class R>
+__device__ __forceinline__ void part_init(PartT<R> &p) {
+    p.mhi = R(0);
+    p.mlo = R(0);
+    p.wet = 0;
+    p.hmax = R(-INFINITY);
+    p.hmin = R(INFINITY);
+    p.area = R(0);
+    p.cossum = R(0);
+}
+
+// (s, e) = a + b exactly (Knuth's TwoSum).
+template <class R>
+__device__ __forceinline__ void two_sum(R a, R b, R &s, R &e) {
+    s = a + b;
+    R bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+template <class R>
+__device__ __forceinline__ void mass_add(PartT<R> &p, R v) {
+    R s, e;
+    two_sum(p.mhi, v, s, e);
+    p.mhi = s;
+    p.mlo = p.mlo + e;
+}
+
+template <class R>
+__device__ __forceinline__ void part_merge(PartT<R> &a, const PartT<R> &b) {
+    R s, e;
+    two_sum(a.mhi, b.mhi, s, e);
+    a.mhi = s;
+    a.mlo = a.mlo + b.mlo + e;
+    a.wet += b.wet;
+    a.hmax = fmax(a.hmax, b.hmax);
+    a.hmin = fmin(a.hmin, b.hmin);
+    a.area += b.area;
+    a.cossum += b.cossum;
+}
+
+template <class R>
+__device__ __forceinline__ PartT<R> part_shfl(const PartT<R> &p, int off) {
+    PartT<R> o;
+    o.mhi = __shfl_down_sync(0xffffffffu, p.mhi, off);
+    o.mlo = __shfl_down_sync(0xffffffffu, p.mlo, off);
+    o.wet = __shfl_down_sync(0xffffffffu, p.wet, off);
+    o.hmax = __shfl_down_sync(0xffffffffu, p.hmax, off);
+    o.hmin = __shfl_down_sync(0xffffffffu, p.hmin, off);
+    o.area = __shfl_down_sync(0xffffffffu, p.area, off);
+    o.cossum = __shfl_down_sync(0xffffffffu, p.cossum, off);
+    return o;
+}
+
+// Block-wide reduction; the result is valid in thread 0.  red: NT/32 slots.
+template <int NT, class R>
+__device__ __forceinline__ PartT<R> block_reduce(PartT<R> p, PartT<R> *red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) part_merge(p, part_shfl(p, off));
+    if (lane == 0) red[warp] = p;
+    __syncthreads();
+    if (warp == 0) {
+        PartT<R> q;
+        part_init(q);
+        if (lane < NT / 32) q = red[lane];
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) part_merge(q, part_shfl(q, off));
+        p = q;
+    }
+    __syncthreads();
+    return p;
+}
+
+// ------------------------------------------------------------ the tile step
+template <class S, int TX, int TY>
+struct TileSmem {
+    using R = typename S::real;
+    R h[TY + 4][TX + 4];
+    R jx[TY][TX];
+    R jy[TY][TX];
+    R hlo[TY][TX];  // FP32 paths: rounding error of the pulled height
+    R p[TY + 2][TX + 2];
+    R kapc[TX + 2];
+    R cosc[TX];
+    PartT<R> red[kThreads / 32];
+    PartT<double> redd[kThreads / 32];
+    int last;
+};
+
+// Finishes a launch for one lattice: block partials, ticket, and in the last
+// CTA the lattice-wide reduction (Float64, fixed order: deterministic), the
+// per-step record and the control update.  No CTA ever waits on another.
+template <int NT, class R>
+__device__ void finish_lattice(const StepArgs &a, const PartT<R> &part, int any_nan,
+                               long long step, int fresh, double corr, int nblocks, int blin,
+                               PartT<R> *red, PartT<double> *redd, int *s_last) {
+    const bool need = (a.meas_mask != 0) || a.mass_corr;
+    PartT<R> tot;
+    if (need) tot = block_reduce<NT>(part, red);
+    if (threadIdx.x == 0) {
+        if (any_nan) a.ctl->nan_flag = 1;
+        if (need) {
+            double *pp = a.partials + (size_t)blin * kNPart;
+            pp[0] = (double)tot.mhi + (double)tot.mlo;
+            pp[1] = (double)tot.wet;
+            pp[2] = (double)tot.hmax;
+            pp[3] = (double)tot.hmin;
+            pp[4] = (double)tot.area;
+            pp[5] = (double)tot.cossum;
+        }
+        __threadfence();
+        unsigned int prev = atomicAdd(&a.ctl->ticket, 1u);
+        *s_last = (prev == (unsigned int)(nblocks - 1));
+    }
+    __syncthreads();
+    if (!*s_last) return;
+    __threadfence();
+    PartT<double> acc;
+    part_init(acc);
+    if (need) {
+        for (int b = threadIdx.x; b < nblocks; b += NT) {
+            const double *pp = a.partials + (size_t)b * kNPart;
+            PartT<double> q;
+            q.mhi = __ldcg(pp + 0);
+            q.mlo = 0.0;
+            q.wet = (int)__ldcg(pp + 1);
+            q.hmax = __ldcg(pp + 2);
+            q.hmin = __ldcg(pp + 3);
+            q.area = __ldcg(pp + 4);
+            q.cossum = __ldcg(pp + 5);
+            part_merge(acc, q);
+        }
+        acc = block_reduce<NT>(acc, redd);
+    }
+    if (threadIdx.x == 0) {
+        const long long t = step + 1;
+        const double mass = acc.mhi + acc.mlo;
+        if (a.meas_mask) {
+            Record &r = a.records[(t - 1) % a.rec_cap];
+            r.t = t;
+            r.mass = mass;
+            r.wetted = (double)acc.wet;
+            r.hmax = acc.hmax;
+            r.hmin = acc.hmin;
+            r.area = acc.area;
+            r.cos_sum = a.theta_mode == THETA_SCALAR ? (double)acc.wet * a.cos_theta : acc.cossum;
+            a.ctl->rec_head = a.ctl->rec_head + 1;
+        }
+        if (a.mass_corr) {
+            if (fresh) a.ctl->mass_target = mass;
+            a.ctl->mass_last = mass;
+            a.ctl->corr_last = corr;
+        }
+        a.ctl->fresh = 0;
+        a.ctl->ticket = 0u;
+        __threadfence();
+        a.ctl->step = t;
+    }
+}
+
+// One time_loop iteration on tile (bx, by) of the lattice described by `a`.
+template <class S, int TX, int TY, int NT>
+__device__ __forceinline__ void step_tile(const StepArgs &a, int bx, int by,
+                                          TileSmem<S, TX, TY> &sm) {
+    using R = typename S::real;
+    constexpr bool LIT = S::kLiteral;
+    const int tid = threadIdx.x;
+    const int Lx = a.Lx, Ly = a.Ly;
+    const long long pitch = a.pitch;
+    const long long step = a.ctl->step;
+    const int fresh = a.ctl->fresh;
+    const long long t = step + 1;  // 1-based time_loop iteration
+    const void *src = (step & 1) ? a.fb : a.fa;
+    void *dst = (step & 1) ? a.fa : a.fb;
+    const int x0 = bx * TX, y0 = by * TY;
+    const R gamma = R(a.gamma), hmin = R(a.hmin), hcrit = R(a.hcrit);
+
+    // FP32/FP16: per-cell share of the mass correction, from the mass of the
+    // previous step's height and the correction applied then.
+    double corr = 0.0;
+    if (!LIT && a.mass_corr && !fresh) {
+        const double N = (double)Lx * (double)Ly;
+        corr = (a.ctl->mass_target - a.ctl->mass_last - N * a.ctl->corr_last) / N;
+    }
+
+    // ---- phase A: heights on the tile + 2 halo (moments of pulled f) ----
+    constexpr int AW = TX + 4, AH = TY + 4;
+    for (int idx = tid; idx < AW * AH; idx += NT) {
+        const int lx = idx % AW, ly = idx / AW;
+        const int gx = wrapc(x0 - 2 + lx, Lx), gy = wrapc(y0 - 2 + ly, Ly);
+        R h, jx = R(0), jy = R(0), lo = R(0);
+        if (fresh) {
+            h = reinterpret_cast<const R *>(a.hF)[gy * Lx + gx];
+        } else {
+            const int gxm = gx == 0 ? Lx - 1 : gx - 1, gxp = gx == Lx - 1 ? 0 : gx + 1;
+            const int gym = gy == 0 ? Ly - 1 : gy - 1, gyp = gy == Ly - 1 ? 0 : gy + 1;
+            R ft[9];
+            pull9<S>(src, pitch, Lx, gx, gy, gxm, gxp, gym, gyp, ft);
+            moments9<LIT>(ft, h, jx, jy);
+            if constexpr (!LIT) lo = moments_lo(ft, h);
+        }
+        sm.h[ly][lx] = h;
+        const int ix = lx - 2, iy = ly - 2;
+        if (ix >= 0 && ix < TX && iy >= 0 && iy < TY) {
+            sm.jx[iy][ix] = jx;
+            sm.jy[iy][ix] = jy;
+            sm.hlo[iy][ix] = lo;
+        }
+    }
+    // θ(x, t) of the moving-wettability mode depends on x only: one kappa
+    // per tile column.
+    if (a.theta_mode == THETA_WAVE) {
+        for (int c = tid; c < TX + 2; c += NT) {
+            const int gx = wrapc(x0 - 1 + c, Lx);
+            R th = R(a.theta0) + R(a.dtheta) * sinpi_r(R(2) * (R(gx) - R(a.wave_v) * R(t)) / R(Lx));
+            sm.kapc[c] = kappa_of(th, a.n, a.m, hmin);
+            if (c >= 1 && c <= TX) sm.cosc[c - 1] = cospi_r(th);
+        }
+    }
+    __syncthreads();
+
+    // ---- phase B: film pressure on the tile + 1 halo ----
+    constexpr int BW = TX + 2, BH = TY + 2;
+    for (int idx = tid; idx < BW * BH; idx += NT) {
+        const int lx = idx % BW, ly = idx / BW;
+        const int ax = lx + 1, ay = ly + 1;
+        R kap;
+        if (a.theta_mode == THETA_SCALAR) {
+            kap = R(a.kap);
+        } else if (a.theta_mode == THETA_FIELD) {
+            const int gx = wrapc(x0 - 1 + lx, Lx), gy = wrapc(y0 - 1 + ly, Ly);
+            kap = reinterpret_cast<const R *>(a.kapF)[gy * Lx + gx];
+        } else {
+            kap = sm.kapc[lx];
+        }
+        sm.p[ly][lx] = pressure_cell<LIT, R>(
+            sm.h[ay][ax], sm.h[ay][ax - 1], sm.h[ay - 1][ax], sm.h[ay][ax + 1], sm.h[ay + 1][ax],
+            sm.h[ay - 1][ax - 1], sm.h[ay - 1][ax + 1], sm.h[ay + 1][ax + 1],
+            sm.h[ay + 1][ax - 1], kap, gamma, hmin, hcrit, a.n, a.m);
+    }
+    __syncthreads();
+
+    // ---- phase C: forces, equilibrium, collision on the interior ----
+    R incl_fac = R(0);
+    if (a.incl) {
+        incl_fac = a.incl_loop_time
+                       ? R(0.5) + R(0.5) * tanh_r(R(t - a.incl_tstart) / R(a.incl_tsmooth))
+                       : R(a.incl_fixed);
+    }
+    const R delta6 = R(6.0 * a.delta), delta3sq = R(3.0 * (a.delta * a.delta)), mu6 = R(6.0 * a.mu);
+    const R omeg = R(a.omeg), invtau = R(a.invtau), g = R(a.g);
+    const R thr = R(a.hthresh);
+    PartT<R> part;
+    part_init(part);
+    int any_nan = 0;
+    constexpr int ROWS = NT / TX;
+#pragma unroll 1
+    for (int k = 0; k < TY / ROWS; ++k) {
+        const int lx = tid % TX, ly = tid / TX + k * ROWS;
+        const int gx = x0 + lx, gy = y0 + ly;
+        if (gx >= Lx || gy >= Ly) continue;
+        const int cell = gy * Lx + gx;
+        const R h = sm.h[ly + 2][lx + 2];
+        R ux, uy;
+        if (fresh) {
+            ux = reinterpret_cast<const R *>(a.uxF)[cell];
+            uy = reinterpret_cast<const R *>(a.uyF)[cell];
+        } else {
+            velocity<LIT>(h, sm.jx[ly][lx], sm.jy[ly][lx], ux, uy);
+        }
+        // h∇p! (src/forcing.jl:181-184)
+        R gpx, gpy;
+        grad9<R>(sm.p[ly + 1][lx], sm.p[ly][lx + 1], sm.p[ly + 1][lx + 2], sm.p[ly + 2][lx + 1],
+                 sm.p[ly][lx], sm.p[ly][lx + 2], sm.p[ly + 2][lx + 2], sm.p[ly + 2][lx], gpx, gpy);
+        const R hgx = h * gpx, hgy = h * gpy;
+        // slippage! (src/forcing.jl:43-44) and the force sum (src/simulate.jl:18-19)
+        R sx, sy;
+        if constexpr (LIT) {
+            const R den = R(2) * (h * h) + delta6 * h + delta3sq;
+            sx = (mu6 * h * ux) / den;
+            sy = (mu6 * h * uy) / den;
+        } else {
+            const R inv = R(1) / ((R(2) * h + delta6) * h + delta3sq);
+            const R c = mu6 * h * inv;
+            sx = c * ux;
+            sy = c * uy;
+        }
+        R Fx = -hgx - sx, Fy = -hgy - sy;
+        if (a.incl) {  // inclination! (src/forcing.jl:364-365)
+            Fx = Fx + (h * R(a.ax)) * incl_fac;
+            Fy = Fy + (h * R(a.ay)) * incl_fac;
+        }
+        // collision (src/collide.jl:267-280); ftemp only matters for τ != 1
+        R ft[9];
+        R hft = h;
+        if (!a.tau_is_one) {
+            const int gxm = gx == 0 ? Lx - 1 : gx - 1, gxp = gx == Lx - 1 ? 0 : gx + 1;
+            const int gym = gy == 0 ? Ly - 1 : gy - 1, gyp = gy == Ly - 1 ? 0 : gy + 1;
+            pull9<S>(src, pitch, Lx, gx, gy, gxm, gxp, gym, gyp, ft);
+            if (!LIT) hft = ft[0] + small8(ft);
+        }
+        if constexpr (LIT) {
+            R fe[9];
+            feq_literal<R>(h, ux, uy, g, fe);
+#pragma unroll
+            for (int q = 0; q < 9; ++q) {
+                R v = a.tau_is_one ? fe[q] : omeg * ft[q] + invtau * fe[q];
+                if (q > 0) v = v + source<R>(q, Fx, Fy);
+                S::st(dst, pitch, q, cell, v);
+            }
+        } else {
+            // FP32 arithmetic.  f0 closes the mass balance with the values as
+            // stored: f0 = M - Σ_{q>0} f_q, where M (the pulled mass, hi + lo)
+            // is what the cell must hold.  FP32 populations: f0's own rounding
+            // error, the lo part of M and the FP64-measured correction are
+            // folded into f1 and f3 equally (momentum unchanged), where they
+            // are resolved to ~ulp(f1).  FP16 populations: f0 takes lo and the
+            // correction, the latter by stochastic rounding.
+            R fe[9], fo[9];
+            feq_fast(h, ux, uy, g, fe);
+#pragma unroll
+            for (int q = 1; q < 9; ++q) {
+                R v = a.tau_is_one ? fe[q] : omeg * ft[q] + invtau * fe[q];
+                fo[q] = S::rt(q, v + source<R>(q, Fx, Fy));
+            }
+            const R hlo = fresh ? R(0) : sm.hlo[ly][lx];
+            // Σ_q fpost_q = (1-1/τ) Σ ft + Σ feq/τ = h once h is the pulled mass
+            const R mc = (a.tau_is_one || !fresh) ? h : omeg * hft + invtau * h;
+            const R ssum = small8(fo);
+            R f0 = mc - ssum;
+            if constexpr (!S::kHalf) {
+                const R e = (mc - f0) - ssum;  // exact error of f0 (Fast2Sum)
+                const R d = R(0.5) * (e + hlo + R(corr));
+                fo[1] = fo[1] + d;
+                fo[3] = fo[3] + d;
+            } else {
+                f0 = f0 + hlo;
+                if (corr != 0.0)
+                    f0 = add_stochastic((float)f0, (float)corr, mix32((unsigned)cell, (unsigned)t));
+            }
+            fo[0] = f0;
+#pragma unroll
+            for (int q = 0; q < 9; ++q) S::st(dst, pitch, q, cell, fo[q]);
+        }
+        // measures of the height at the start of this iteration
+        if (!isfinite(h)) any_nan = 1;
+        if (a.meas_mask || a.mass_corr) {
+            mass_add(part, h);
+            if constexpr (!LIT) {
+                if (!fresh) part.mlo += sm.hlo[ly][lx];
+            }
+            const bool wet = h > thr;
+            part.wet += wet ? 1 : 0;
+            part.hmax = fmax(part.hmax, h);
+            part.hmin = fmin(part.hmin, h);
+            if ((a.meas_mask & SWB_MEAS_AREA) && wet) {
+                const int ax = lx + 2, ay = ly + 2;
+                R gx2, gy2;
+                grad9<R>(sm.h[ay][ax - 1], sm.h[ay - 1][ax], sm.h[ay][ax + 1], sm.h[ay + 1][ax],
+                         sm.h[ay - 1][ax - 1], sm.h[ay - 1][ax + 1], sm.h[ay + 1][ax + 1],
+                         sm.h[ay + 1][ax - 1], gx2, gy2);
+                part.area += sqrt(gx2 * gx2 + gy2 * gy2 + R(1));
+                if (a.theta_mode == THETA_FIELD)
+                    part.cossum += reinterpret_cast<const R *>(a.cosF)[cell];
+                else if (a.theta_mode == THETA_WAVE)
+                    part.cossum += sm.cosc[lx];
+            }
+        }
+    }
+    any_nan = __syncthreads_or(any_nan);
+    const int nblocks = a.tiles_x * a.tiles_y;
+    finish_lattice<NT, R>(a, part, any_nan, step, fresh, corr, nblocks, by * a.tiles_x + bx,
+                          sm.red, sm.redd, &sm.last);
+}
+
+// Single lattice: one CTA per tile.
+template <class S>
+__global__ void __launch_bounds__(kThreads) fused_step_kernel(const StepArgs a) {
+    __shared__ TileSmem<S, kTX, kTY> sm;
+    step_tile<S, kTX, kTY, kThreads>(a, blockIdx.x, blockIdx.y, sm);
+}
+
+// Batch: persistent CTAs walk a packed table of tiles of many lattices.
+template <class S>
+__global__ void __launch_bounds__(kThreads) batch_step_kernel(const StepArgs *__restrict__ args,
+                                                              const TileRef *__restrict__ tiles,
+                                                              int ntiles) {
+    __shared__ TileSmem<S, kTX, kTY> sm;
+    __shared__ StepArgs sa;
+    for (int k = blockIdx.x; k < ntiles; k += gridDim.x) {
+        const TileRef tr = tiles[k];
+        if (threadIdx.x == 0) sa = args[tr.lattice];
+        __syncthreads();
+        step_tile<S, kTX, kTY, kThreads>(sa, tr.tx, tr.ty, sm);
+        __syncthreads();
+    }
+}
+
+// moments! into the fields (used when the host reads h/u).
+template <class S>
+__global__ void moments_kernel(const StepArgs a) {
+    using R = typename S::real;
+    const int Lx = a.Lx, Ly = a.Ly;
+    const long long step = a.ctl->step;
+    const void *src = (step & 1) ? a.fb : a.fa;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < (long long)Lx * Ly;
+         c += (long long)gridDim.x * blockDim.x) {
+        const int gx = (int)(c % Lx), gy = (int)(c / Lx);
+        const int gxm = gx == 0 ? Lx - 1 : gx - 1, gxp = gx == Lx - 1 ? 0 : gx + 1;
+        const int gym = gy == 0 ? Ly - 1 : gy - 1, gyp = gy == Ly - 1 ? 0 : gy + 1;
+        R ft[9], h, jx, jy, ux, uy;
+        pull9<S>(src, a.pitch, Lx, gx, gy, gxm, gxp, gym, gyp, ft);
+        moments9<S::kLiteral>(ft, h, jx, jy);
+        velocity<S::kLiteral>(h, jx, jy, ux, uy);
+        reinterpret_cast<R *>(a.hF)[c] = h;
+        reinterpret_cast<R *>(a.uxF)[c] = ux;
+        reinterpret_cast<R *>(a.uyF)[c] = uy;
+    }
+}
+
+// Streamed populations (the reference's fout) into a Float64 array.
+template <class S>
+__global__ void fout_kernel(const StepArgs a, double *out) {
+    using R = typename S::real;
+    const int Lx = a.Lx, Ly = a.Ly;
+    const long long N = (long long)Lx * Ly;
+    const long long step = a.ctl->step;
+    const void *src = (step & 1) ? a.fb : a.fa;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < N;
+         c += (long long)gridDim.x * blockDim.x) {
+        const int gx = (int)(c % Lx), gy = (int)(c / Lx);
+        const int gxm = gx == 0 ? Lx - 1 : gx - 1, gxp = gx == Lx - 1 ? 0 : gx + 1;
+        const int gym = gy == 0 ? Ly - 1 : gy - 1, gyp = gy == Ly - 1 ? 0 : gy + 1;
+        R ft[9];
+        pull9<S>(src, a.pitch, Lx, gx, gy, gxm, gxp, gym, gyp, ft);
+        for (int q = 0; q < 9; ++q) out[q * N + c] = (double)ft[q];
+    }
+}
+
+// Film pressure of the current height field (filmpressure! applied now).
+template <class S>
+__global__ void pressure_now_kernel(const StepArgs a, double *out) {
+    using R = typename S::real;
+    const int Lx = a.Lx, Ly = a.Ly;
+    const R *h = reinterpret_cast<const R *>(a.hF);
+    const long long t = a.ctl->step + 1;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < (long long)Lx * Ly;
+         c += (long long)gridDim.x * blockDim.x) {
+        const int i = (int)(c % Lx), j = (int)(c / Lx);
+        const int im1 = i == 0 ? Lx - 1 : i - 1, ip1 = i == Lx - 1 ? 0 : i + 1;
+        const int jm1 = j == 0 ? Ly - 1 : j - 1, jp1 = j == Ly - 1 ? 0 : j + 1;
+        R kap;
+        if (a.theta_mode == THETA_SCALAR)
+            kap = R(a.kap);
+        else if (a.theta_mode == THETA_FIELD)
+            kap = reinterpret_cast<const R *>(a.kapF)[c];
+        else
+            kap = kappa_of(R(a.theta0) + R(a.dtheta) * sinpi_r(R(2) * (R(i) - R(a.wave_v) * R(t)) / R(Lx)),
+                           a.n, a.m, R(a.hmin));
+        out[c] = (double)pressure_cell<S::kLiteral, R>(
+            h[c], h[j * Lx + im1], h[jm1 * Lx + i], h[j * Lx + ip1], h[jp1 * Lx + i],
+            h[jm1 * Lx + im1], h[jm1 * Lx + ip1], h[jp1 * Lx + ip1], h[jp1 * Lx + im1], kap,
+            R(a.gamma), R(a.hmin), R(a.hcrit), a.n, a.m);
+    }
+}
+
+}  // namespace swb

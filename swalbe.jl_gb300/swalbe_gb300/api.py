@@ -1,0 +1,551 @@
+"""Host-side mirror of Swalbe.jl's Julia API over the C ABI.
+
+Names, arguments and defaults follow the reference (paths relative to the
+Swalbe.jl project root) so that a script written against `Swalbe` reads the
+same: ``Sys(sys, "GB300")`` instead of ``Sys(sys, "GPU")``, then
+``time_loop``, the ``run_*`` drivers and the per-op functions.  Julia's
+``!``-suffixed mutating functions end in ``_`` here (``filmpressure_``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from typing import Callable, Optional, Sequence
+
+import numpy as np
+
+from . import _lib as L
+from ._lib import check, lib
+
+_GREEK = {"τ": "tau", "cₛ": "cs", "μ": "mu", "δ": "delta", "γ": "gamma", "θ": "theta"}
+
+
+class Taumucs:
+    """Run-time constants (src/initialize.jl:43-60).  θ is in units of π."""
+
+    def __init__(self, **kw):
+        kw = {_GREEK.get(k, k): v for k, v in kw.items()}
+        self.Tmax = int(kw.pop("Tmax", 1000))
+        self.tdump = int(kw.pop("tdump", self.Tmax // 10))
+        self.tau = float(kw.pop("tau", 1.0))
+        self.cs = float(kw.pop("cs", 1 / math.sqrt(3.0)))
+        self.mu = float(kw.pop("mu", self.cs ** 2 * (self.tau - 0.5)))
+        self.delta = float(kw.pop("delta", 1.0))
+        self.kbt = float(kw.pop("kbt", 0.0))
+        self.gamma = float(kw.pop("gamma", 0.01))
+        self.n = int(kw.pop("n", 9))
+        self.m = int(kw.pop("m", 3))
+        self.hmin = float(kw.pop("hmin", 0.1))
+        self.hcrit = float(kw.pop("hcrit", 0.05))
+        self.theta = float(kw.pop("theta", 1 / 9))
+        self.g = float(kw.pop("g", 0.0))
+        if kw:
+            raise TypeError(f"unknown Taumucs fields {sorted(kw)}")
+
+    # Greek aliases as in the reference
+    τ = property(lambda s: s.tau)
+    μ = property(lambda s: s.mu)
+    δ = property(lambda s: s.delta)
+    γ = property(lambda s: s.gamma)
+    θ = property(lambda s: s.theta)
+
+    def replace(self, **kw):
+        d = dict(Tmax=self.Tmax, tdump=self.tdump, tau=self.tau, cs=self.cs, mu=self.mu,
+                 delta=self.delta, kbt=self.kbt, gamma=self.gamma, n=self.n, m=self.m,
+                 hmin=self.hmin, hcrit=self.hcrit, theta=self.theta, g=self.g)
+        d.update({_GREEK.get(k, k): v for k, v in kw.items()})
+        return Taumucs(**d)
+
+
+class SysConst:
+    """Lattice size + constants (src/initialize.jl:76-81)."""
+
+    def __init__(self, Lx: int = 256, Ly: int = 256, param: Optional[Taumucs] = None):
+        self.Lx, self.Ly = int(Lx), int(Ly)
+        self.param = param if param is not None else Taumucs()
+
+    def c_params(self) -> L.Params:
+        p = self.param
+        return L.Params(self.Lx, self.Ly, p.Tmax, p.tdump, p.tau, p.cs, p.mu, p.delta, p.kbt,
+                        p.gamma, p.n, p.m, p.hmin, p.hcrit, p.theta, p.g)
+
+
+def cospi(x: float) -> float:
+    r = math.fmod(abs(float(x)), 2.0)
+    if r == 0.0:
+        return 1.0
+    if r == 1.0:
+        return -1.0
+    if r in (0.5, 1.5):
+        return 0.0
+    return math.cos(math.pi * r)
+
+
+def _precision(device: str, T) -> int:
+    if device in ("GB300-plain", "GPU-plain"):
+        if np.dtype(T) != np.float64:
+            raise ValueError("the plain per-op path is Float64 only")
+        return L.SWB_PLAIN64
+    if device not in ("GB300", "GPU"):
+        raise ValueError(f"device {device!r}: this package runs on 'GB300' (or 'GB300-plain')")
+    dt = np.dtype(T)
+    if dt == np.float64:
+        return L.SWB_F64
+    if dt == np.float32:
+        return L.SWB_F32
+    if dt == np.float16:
+        return L.SWB_F16
+    raise ValueError(f"unsupported element type {T}")
+
+
+def _f64(a, shape) -> np.ndarray:
+    a = np.asfortranarray(np.broadcast_to(np.asarray(a, dtype=np.float64), shape))
+    return a
+
+
+class GB300State:
+    """A simulation resident on the GPU: the `State` of src/initialize.jl:149-168.
+
+    Fields read (``state.height``) copy the current values to the host;
+    assignment (``state.height = h`` or ``state.height[...] = ...`` via
+    ``set``) uploads them.
+    """
+
+    def __init__(self, sysc: SysConst, precision: int):
+        self.sys = sysc
+        self.precision = precision
+        self._p = sysc.c_params()
+        h = C.c_void_p()
+        check(lib().swb_create(C.byref(self._p), precision, C.byref(h)))
+        self._h = h
+        self.shape = (sysc.Lx, sysc.Ly)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                lib().swb_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    close = __del__
+
+    @property
+    def handle(self):
+        return self._h
+
+    def _chk(self, st):
+        return check(st, self._h)
+
+    # ---- fields
+    def get(self, name: str) -> np.ndarray:
+        shape = self.shape + ((9,) if name in ("fout", "feq") else ())
+        out = np.empty(shape, dtype=np.float64, order="F")
+        self._chk(lib().swb_get_field(self._h, L.FIELD[name], out.ctypes.data))
+        return out
+
+    def set(self, name: str, values) -> None:
+        shape = self.shape + ((9,) if name in ("fout", "feq") else ())
+        a = _f64(values, shape)
+        self._chk(lib().swb_set_field(self._h, L.FIELD[name], a.ctypes.data))
+
+    height = property(lambda s: s.get("height"), lambda s, v: s.set("height", v))
+    velx = property(lambda s: s.get("velx"), lambda s, v: s.set("velx", v))
+    vely = property(lambda s: s.get("vely"), lambda s, v: s.set("vely", v))
+    pressure = property(lambda s: s.get("pressure"), lambda s, v: s.set("pressure", v))
+    fout = property(lambda s: s.get("fout"), lambda s, v: s.set("fout", v))
+    feq = property(lambda s: s.get("feq"), lambda s, v: s.set("feq", v))
+    Fx = property(lambda s: s.get("Fx"), lambda s, v: s.set("Fx", v))
+    Fy = property(lambda s: s.get("Fy"), lambda s, v: s.set("Fy", v))
+    slipx = property(lambda s: s.get("slipx"), lambda s, v: s.set("slipx", v))
+    slipy = property(lambda s: s.get("slipy"), lambda s, v: s.set("slipy", v))
+    h_grad_px = property(lambda s: s.get("h∇px"), lambda s, v: s.set("h∇px", v))
+    h_grad_py = property(lambda s: s.get("h∇py"), lambda s, v: s.set("h∇py", v))
+    vsq = property(lambda s: s.get("vsq"), lambda s, v: s.set("vsq", v))
+
+    def set_device(self, name: str, device_ptr: int) -> None:
+        """Field from a Float64 column-major device array (no host copy)."""
+        self._chk(lib().swb_set_field_device(self._h, L.FIELD[name], C.c_void_p(device_ptr)))
+
+    def set_stream(self, stream_ptr: Optional[int]) -> None:
+        self._chk(lib().swb_set_stream(self._h, None if not stream_ptr else C.c_void_p(stream_ptr)))
+
+    def stream(self) -> int:
+        p = C.c_void_p()
+        self._chk(lib().swb_get_stream(self._h, C.byref(p)))
+        return p.value or 0
+
+    # ---- configuration
+    def set_theta(self, theta) -> None:
+        if np.ndim(theta) == 0:
+            self._chk(lib().swb_set_theta(self._h, float(theta)))
+        else:
+            t = _f64(theta, self.shape)
+            self._chk(lib().swb_set_theta_field(self._h, t.ctypes.data))
+
+    def set_theta_wave(self, theta0: float, dtheta: float, v: float) -> None:
+        self._chk(lib().swb_set_theta_wave(self._h, theta0, dtheta, v))
+
+    def set_inclination(self, alpha, t=1000, tstart=0, tsmooth=1, loop_time=False) -> None:
+        self._chk(lib().swb_set_inclination(self._h, float(alpha[0]), float(alpha[1]),
+                                            int(loop_time), int(t), int(tstart), int(tsmooth)))
+
+    def set_measures(self, mask: int, hthresh: float = 0.055) -> None:
+        self._chk(lib().swb_set_measures(self._h, int(mask), float(hthresh)))
+
+    # ---- stepping
+    def step(self, nsteps: int) -> None:
+        self._chk(lib().swb_step(self._h, int(nsteps)))
+
+    def sync(self) -> None:
+        self._chk(lib().swb_sync(self._h))
+
+    def steps_done(self) -> int:
+        t = C.c_int64()
+        self._chk(lib().swb_steps_done(self._h, C.byref(t)))
+        return t.value
+
+    def measures(self, cap: int = 1 << 16):
+        buf = (L.Measure * cap)()
+        n = C.c_int64()
+        self._chk(lib().swb_get_measures(self._h, buf, cap, C.byref(n)))
+        return [buf[k] for k in range(n.value)]
+
+    def measure_now(self, hthresh: float = 0.055) -> L.Measure:
+        m = L.Measure()
+        self._chk(lib().swb_measure_now(self._h, hthresh, C.byref(m)))
+        return m
+
+
+def Sys(sysc: SysConst, device: str = "GB300", T=np.float64, kind: str = "simple") -> GB300State:
+    """Sys(sysc, device; T, kind) (src/initialize.jl:491-572): zero populations, h = 1."""
+    if kind != "simple":
+        raise NotImplementedError(f"kind={kind!r}: only 'simple' states run on the GB300 path")
+    return GB300State(sysc, _precision(device, T))
+
+
+def launch_count() -> int:
+    """Kernel launches the library has issued since it was loaded."""
+    n = C.c_uint64()
+    check(lib().swb_launch_count(C.byref(n)))
+    return n.value
+
+
+# ------------------------------------------------------------------ per-op API
+def filmpressure_(state: GB300State, sysc: SysConst, θ=None, theta=None) -> None:
+    """filmpressure!(state, sys; θ) (src/pressure.jl:119-155)."""
+    th = θ if θ is not None else theta
+    state.set_theta(sysc.param.theta if th is None else th)
+    state._chk(lib().swb_op_filmpressure(state.handle))
+
+
+def h_grad_p_(state: GB300State) -> None:
+    """h∇p!(state) (src/forcing.jl:168-187)."""
+    state._chk(lib().swb_op_hgradp(state.handle))
+
+
+def slippage_(state: GB300State, sysc: SysConst) -> None:
+    """slippage!(state, sys) (src/forcing.jl:48-56)."""
+    state._chk(lib().swb_op_slippage(state.handle))
+
+
+def force_sum_(state: GB300State) -> None:
+    """state.Fx .= -state.h∇px .- state.slipx, likewise y (src/simulate.jl:18-19)."""
+    state._chk(lib().swb_op_force_sum(state.handle))
+
+
+def inclination_(α, state: GB300State, t: int = 1000, tstart: int = 0, tsmooth: int = 1) -> None:
+    """inclination!(α, state; t, tstart, tsmooth) (src/forcing.jl:363-368)."""
+    state._chk(lib().swb_op_inclination(state.handle, float(α[0]), float(α[1]), int(t),
+                                        int(tstart), int(tsmooth)))
+
+
+def equilibrium_(state: GB300State, sysc: SysConst) -> None:
+    """equilibrium!(state, sys) (src/equilibrium.jl:118-119)."""
+    state._chk(lib().swb_op_equilibrium(state.handle))
+
+
+def BGKandStream_(state: GB300State, sysc: SysConst) -> None:
+    """BGKandStream!(state, sys) (src/collide.jl:342-343)."""
+    state._chk(lib().swb_op_bgk_stream(state.handle))
+
+
+def moments_(state: GB300State) -> None:
+    """moments!(state) (src/moments.jl:64)."""
+    state._chk(lib().swb_op_moments(state.handle))
+
+
+def wetted_(area_size: list, state: GB300State, hthresh: float = 0.055) -> None:
+    """wetted!(area_size, state) (src/measures.jl:13-17)."""
+    area_size.append(int(state.measure_now(hthresh).wetted))
+
+
+def surfacearea_(state: GB300State, hthresh: float = 0.055):
+    """(area_lv, red_energy) of surfacearea! (src/measures.jl:126-168) for the θ set."""
+    m = state.measure_now(hthresh)
+    return m.area, m.energy
+
+
+# ------------------------------------------------------------------ time loop
+def time_loop(sysc: SysConst, state: GB300State, *args, verbose: bool = False):
+    """time_loop(sys, state[, θ | Δh | f, measure]) (src/simulate.jl:6-96).
+
+    - ``time_loop(sys, state)``: θ = sys.param.θ;
+    - ``time_loop(sys, state, θ)``: θ a number or an Lx x Ly array;
+    - ``time_loop(sys, state, Δh)``: Δh a list, max(h) - min(h) pushed every step;
+    - ``time_loop(sys, state, f, measure)``: the callback runs after the forces
+      each step; ``wetted_`` and ``inclination_`` run fused on the device, any
+      other callable needs a ``"GB300-plain"`` state (it is called between ops).
+    """
+    P = sysc.param
+    Tmax = P.Tmax
+    mask = L.MEAS_MASS
+    dh = None
+    callback = None
+    measure = None
+    state.set_theta(P.theta)
+    if len(args) == 1 and isinstance(args[0], list):
+        dh = args[0]
+        mask |= L.MEAS_MAXMIN
+    elif len(args) == 1:
+        state.set_theta(args[0])
+    elif len(args) == 2:
+        callback, measure = args
+        if callback is wetted_:
+            mask |= L.MEAS_WETTED
+        elif callback is inclination_:
+            state.set_inclination(measure)
+        elif state.precision != L.SWB_PLAIN64:
+            raise NotImplementedError("arbitrary callbacks need device='GB300-plain'")
+    elif args:
+        raise TypeError("time_loop(sys, state[, θ | Δh | f, measure])")
+    state.set_measures(mask)
+    if callback is not None and callback not in (wetted_, inclination_):
+        for _ in range(Tmax):
+            _plain_iteration_with_callback(sysc, state, callback, measure)
+    else:
+        state.step(Tmax)
+    recs = state.measures(cap=max(Tmax, 1))
+    for r in recs:
+        t = r.t
+        if P.tdump > 0 and t % P.tdump == 0 and verbose:
+            print(f"Time step {t} mass is {round(r.mass, 3)}")
+        if dh is not None:
+            dh.append(r.hmax - r.hmin)
+        if callback is wetted_:
+            measure.append(int(r.wetted))
+    if callback is inclination_:
+        state.set_inclination((0.0, 0.0))
+    state.sync()
+    if callback is not None:
+        return state, measure
+    return state
+
+
+def _plain_iteration_with_callback(sysc, state, f: Callable, measure):
+    filmpressure_(state, sysc)
+    h_grad_p_(state)
+    slippage_(state, sysc)
+    force_sum_(state)
+    f(measure, state)
+    equilibrium_(state, sysc)
+    BGKandStream_(state, sysc)
+    moments_(state)
+
+
+# ------------------------------------------------------------------ initial values
+def singledroplet(height: np.ndarray, radius, θ, center) -> np.ndarray:
+    """singledroplet(height, radius, θ, center) (src/initialvalues.jl:203-224); 1-based center."""
+    lx, ly = height.shape
+    i = np.arange(1, lx + 1, dtype=np.float64)[:, None]
+    j = np.arange(1, ly + 1, dtype=np.float64)[None, :]
+    circ = np.sqrt((i - center[0]) ** 2 + (j - center[1]) ** 2)
+    with np.errstate(invalid="ignore"):
+        cap = (np.cos(np.arcsin(np.minimum(circ / radius, 1.0))) - cospi(θ)) * radius
+    h = np.where(circ <= radius, cap, 0.05)
+    h = np.where(h < 0, 0.05, h)
+    height[...] = h
+    return height
+
+
+def randinterface_(height: np.ndarray, h0: float, ϵ: float, rng=None) -> None:
+    """randinterface!(height, h₀, ϵ) (src/initialvalues.jl:23-33) with a seeded numpy RNG."""
+    rng = np.random.default_rng(0) if rng is None else rng
+    height[...] = h0 * (1.0 + ϵ * rng.standard_normal(height.shape))
+
+
+def two_caps(Lx: int, Ly: int, r1, r2, θ1, θ2, c1, c2) -> np.ndarray:
+    """Two spherical caps combined as two_droplets does in 1D
+    (src/initialvalues.jl:277-323): h1 + h2 - 0.05, negatives clamped."""
+    a = singledroplet(np.zeros((Lx, Ly)), r1, θ1, c1)
+    b = singledroplet(np.zeros((Lx, Ly)), r2, θ2, c2)
+    h = a + b - 0.05
+    return np.asfortranarray(np.where(h < 0, 0.05, h))
+
+
+# ------------------------------------------------------------------ run_* drivers
+def _new(sysc, device, T):
+    return Sys(sysc, device, T=T)
+
+
+def run_flat(sysc: SysConst, device: str = "GB300", verbos: bool = True, T=np.float64):
+    """run_flat(sys, device) (src/simulate.jl:236-245)."""
+    state = _new(sysc, device, T)
+    state.height = np.ones(state.shape)
+    time_loop(sysc, state, verbose=verbos)
+    return state.height
+
+
+def run_random(sysc: SysConst, device: str = "GB300", h0=1.0, ϵ=0.01, verbos=True, T=np.float64,
+               rng=None):
+    """run_random(sys, device; h₀, ϵ) (src/simulate.jl:286-294); θ = 1/9 as there."""
+    state = _new(sysc, device, T)
+    h = np.zeros(state.shape)
+    randinterface_(h, h0, ϵ, rng)
+    state.height = h
+    time_loop(sysc, state, 1 / 9, verbose=verbos)
+    return state.height
+
+
+def run_rayleightaylor(sysc: SysConst, device: str = "GB300", kx=15, ky=18, h0=1.0, ϵ=0.001,
+                       verbos=True, T=np.float64):
+    """run_rayleightaylor(sys, device; kx, ky, h₀, ϵ) (src/simulate.jl:338-358)."""
+    state = _new(sysc, device, T)
+    i = np.arange(1, sysc.Lx + 1)[:, None]
+    j = np.arange(1, sysc.Ly + 1)[None, :]
+    state.height = h0 * (1 + ϵ * np.sin(2 * np.pi * kx * i / (sysc.Lx - 1)) *
+                         np.sin(2 * np.pi * ky * j / (sysc.Ly - 1)))
+    diff = []
+    time_loop(sysc, state, diff, verbose=verbos)
+    return state.height, diff
+
+
+def run_dropletrelax(sysc: SysConst, device: str = "GB300", radius=20, theta0=1 / 6, center=None,
+                     verbos=True, T=np.float64):
+    """run_dropletrelax(sys, device; radius, theta0, center) (src/simulate.jl:384-399)."""
+    center = (sysc.Lx // 2, sysc.Ly // 2) if center is None else center
+    state = _new(sysc, device, T)
+    state.height = singledroplet(np.zeros(state.shape), radius, theta0, center)
+    area = []
+    time_loop(sysc, state, wetted_, area, verbose=verbos)
+    return state.height, area
+
+
+def run_dropletpatterned(sysc: SysConst, device: str = "GB300", radius=20, theta0=1 / 6, center=None,
+                         θₛ=None, verbos=True, T=np.float64):
+    """run_dropletpatterned(sys, device; radius, θ₀, center, θₛ) (src/simulate.jl:422-439)."""
+    center = (sysc.Lx // 2, sysc.Ly // 2) if center is None else center
+    θₛ = np.full((sysc.Lx, sysc.Ly), 1 / 9) if θₛ is None else θₛ
+    state = _new(sysc, device, T)
+    state.height = singledroplet(np.zeros(state.shape), radius, theta0, center)
+    time_loop(sysc, state, θₛ, verbose=verbos)
+    return state.height
+
+
+def run_dropletforced(sysc: SysConst, device: str = "GB300", radius=20, theta0=1 / 6, center=None,
+                      fx=0.0, fy=0.0, verbos=True, T=np.float64):
+    """run_dropletforced(sys, device; radius, θ₀, center, fx, fy) (src/simulate.jl:462-484)."""
+    center = (sysc.Lx // 2, sysc.Ly // 2) if center is None else center
+    state = _new(sysc, device, T)
+    state.height = singledroplet(np.zeros(state.shape), radius, theta0, center)
+    time_loop(sysc, state, inclination_, [fx, fy], verbose=verbos)
+    return state.height, state.velx, state.vely
+
+
+# ------------------------------------------------------------------ batch / server
+class Batch:
+    """Many simulations advanced together (one launch per step, packed tiles)."""
+
+    def __init__(self, systems: Sequence[SysConst], T=np.float32):
+        self.systems = list(systems)
+        prec = _precision("GB300", T)
+        arr = (L.Params * len(self.systems))(*[s.c_params() for s in self.systems])
+        h = C.c_void_p()
+        check(lib().swb_batch_create(arr, len(self.systems), prec, C.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                lib().swb_batch_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    close = __del__
+
+    def set_height(self, i: int, h) -> None:
+        s = self.systems[i]
+        a = _f64(h, (s.Lx, s.Ly))
+        check(lib().swb_batch_set_height(self._h, i, a.ctypes.data))
+
+    def get_height(self, i: int) -> np.ndarray:
+        s = self.systems[i]
+        out = np.empty((s.Lx, s.Ly), order="F")
+        check(lib().swb_batch_get_height(self._h, i, out.ctypes.data))
+        return out
+
+    def set_theta_wave(self, i: int, theta0: float, dtheta: float, v: float) -> None:
+        check(lib().swb_batch_set_theta_wave(self._h, i, theta0, dtheta, v))
+
+    def step(self, n: int) -> None:
+        check(lib().swb_batch_step(self._h, int(n)))
+
+    def sync(self) -> None:
+        check(lib().swb_batch_sync(self._h))
+
+    def tile(self):
+        a, b, c = C.c_int(), C.c_int(), C.c_int()
+        check(lib().swb_batch_tile(self._h, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
+
+
+class Server:
+    """Request loop with HBM-footprint admission and continuous batching."""
+
+    def __init__(self, hbm_budget: int, T=np.float32, steps_per_tick: int = 100):
+        h = C.c_void_p()
+        check(lib().swb_server_create(int(hbm_budget), _precision("GB300", T), int(steps_per_tick),
+                                      C.byref(h)))
+        self._h = h
+
+    def close(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            lib().swb_server_destroy(h)
+            self._h = None
+
+    __del__ = close
+
+    def submit(self, sysc: SysConst, h0, nsteps: int, theta0=None, dtheta=0.0, v=0.0) -> int:
+        p = sysc.c_params()
+        a = _f64(h0, (sysc.Lx, sysc.Ly))
+        th0 = sysc.param.theta if theta0 is None else theta0
+        rid = C.c_int64()
+        check(lib().swb_server_submit(self._h, C.byref(p), a.ctypes.data, float(th0), float(dtheta),
+                                      float(v), int(nsteps), C.byref(rid)))
+        return rid.value
+
+    def poll(self, rid: int, shape=None):
+        """(done, height or None, info).  A failed or cancelled request is
+        reported through info.status < 0, not raised."""
+        info = L.RequestInfo()
+        out = None if shape is None else np.empty(shape, order="F")
+        st = lib().swb_server_poll(self._h, int(rid), None if out is None else out.ctypes.data,
+                                   C.byref(info))
+        if st in (L.SWB_ERR_ARG, L.SWB_ERR_NOT_FOUND):
+            check(st)
+        return st == 1, (out if st == 1 else None), info
+
+    def cancel(self, rid: int) -> None:
+        check(lib().swb_server_cancel(self._h, int(rid)))
+
+    def stats(self) -> L.ServerStats:
+        s = L.ServerStats()
+        check(lib().swb_server_stats_get(self._h, C.byref(s)))
+        return s
+
+    def clock(self) -> float:
+        return lib().swb_server_clock(self._h)

@@ -1,0 +1,117 @@
+"""Seeded synthetic inputs for the five benchmark configurations.
+
+The reference publishes no benchmark inputs; these generators produce the
+shapes, sizes and value distributions each configuration describes, from
+fixed seeds (numpy PCG64, identical on every platform), so that the CPU
+oracle and the GPU read the same bytes.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+from typing import List, Optional, Tuple
+
+import numpy as np
+
+from .api import SysConst, Taumucs, cospi, singledroplet, two_caps
+
+
+def droplet_relax_256():
+    """Config 1: 256², Float64, τ=1, γ=0.01, δ=1, θ=1/9, n=9, m=3, hmin=0.1,
+    hcrit=0.05; h = max(0.05, cap) of a sphere R=60 centred at (128, 128)
+    (1-based) with apex height 20 ⇒ θ0 = acos(1 - 20/60)/π; 10,000 steps.
+
+    The max(0.05, ·) clamp follows the configuration's wording; the reference's
+    singledroplet (src/initialvalues.jl:203-224) clamps only negative heights,
+    which leaves rim cells of ~1e-15 height where u = j/h diverges.
+    """
+    sysc = SysConst(256, 256, Taumucs(Tmax=10000, tdump=1000))
+    th0 = math.acos(1 - 20 / 60) / math.pi
+    cap = singledroplet(np.zeros((256, 256)), 60, th0, (128, 128))
+    return sysc, np.asfortranarray(np.maximum(0.05, cap)), 10000
+
+
+def rayleigh_taylor_512(seed: int = 2):
+    """Config 2: 512², g=-0.001, γ=0.0005, θ=1/9, h = 1 + U[-0.01, 0.01]."""
+    sysc = SysConst(512, 512, Taumucs(Tmax=50000, tdump=5000, g=-0.001, gamma=0.0005))
+    rng = np.random.default_rng(seed)
+    return sysc, np.asfortranarray(1.0 + rng.uniform(-0.01, 0.01, (512, 512))), 50000
+
+
+def spinodal_2048(seed: int = 3):
+    """Config 3: 2048², γ=0.01, θ=1/9, h = 1 + U[-0.1, 0.1], 100,000 steps."""
+    sysc = SysConst(2048, 2048, Taumucs(Tmax=100000, tdump=10000))
+    rng = np.random.default_rng(seed)
+    return sysc, np.asfortranarray(1.0 + rng.uniform(-0.1, 0.1, (2048, 2048))), 100000
+
+
+@dataclass
+class EnsembleMember:
+    sysc: SysConst
+    h0: np.ndarray
+
+
+def ensemble(count: int = 512, seed: int = 4, steps: int = 20000) -> Tuple[List[EnsembleMember], int]:
+    """Config 4: `count` coalescence instances; sizes from {128², 256², 512²,
+    1024x256}; two caps of radii U[0.15, 0.40]·Ly separated by an edge gap of
+    U{2..10} cells; θ ~ U[1/18, 1/4] for the caps and the substrate; FP32."""
+    rng = np.random.default_rng(seed)
+    sizes = [(128, 128), (256, 256), (512, 512), (1024, 256)]
+    out = []
+    for _ in range(count):
+        Lx, Ly = sizes[rng.integers(0, 4)]
+        th = float(rng.uniform(1 / 18, 1 / 4))
+        r1, r2 = rng.uniform(0.15, 0.40, 2) * Ly
+        gap = int(rng.integers(2, 11))
+        # contact radii of the caps: R sin(πθ); centre them along x
+        a1, a2 = r1 * math.sin(math.pi * th), r2 * math.sin(math.pi * th)
+        cx = Lx / 2
+        c1 = (cx - gap / 2 - a1, Ly / 2)
+        c2 = (cx + gap / 2 + a2, Ly / 2)
+        h0 = two_caps(Lx, Ly, r1, r2, th, th, c1, c2)
+        out.append(EnsembleMember(SysConst(Lx, Ly, Taumucs(Tmax=steps, theta=th)), h0))
+    return out, steps
+
+
+@dataclass
+class Request:
+    t_arrival: float
+    sysc: SysConst
+    nsteps: int
+    theta0: float
+    seed: int
+    h_amp: float
+    dtheta: float = 1 / 36
+    v: float = 1 / 98
+
+    def height(self) -> np.ndarray:
+        """The request's initial film (generated on demand from its seed)."""
+        rng = np.random.default_rng(self.seed)
+        shape = (self.sysc.Lx, self.sysc.Ly)
+        return np.asfortranarray(1.0 + rng.uniform(-self.h_amp, self.h_amp, shape))
+
+
+def serving_stream(rate: float = 200.0, duration: float = 10.0, seed: int = 5,
+                   side_choices: Optional[List[int]] = None, step_range=(1000, 100000),
+                   h_amp: float = 0.05) -> List[Request]:
+    """Config 5: Poisson arrivals (mean `rate`/s); Lx, Ly uniform on multiples
+    of 64 in [64, 2048]; steps uniform in `step_range`; θ0 ~ U[1/18, 1/4];
+    g ~ U[-1e-3, 0]; moving wettability θ(x,t) = θ0 + Δθ sin(2π(x - v t)/Lx)
+    with Δθ = 1/36, v = 1/98 (scripts/Moving_wettability_structs.jl:183-186);
+    films h = 1 + U[-h_amp, h_amp]."""
+    rng = np.random.default_rng(seed)
+    sides = side_choices or list(range(64, 2049, 64))
+    t = 0.0
+    reqs = []
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t > duration:
+            break
+        Lx, Ly = int(rng.choice(sides)), int(rng.choice(sides))
+        steps = int(rng.integers(step_range[0], step_range[1] + 1))
+        th0 = float(rng.uniform(1 / 18, 1 / 4))
+        g = float(rng.uniform(-1e-3, 0.0))
+        sub = int(rng.integers(0, 2 ** 31))
+        reqs.append(Request(t, SysConst(Lx, Ly, Taumucs(Tmax=steps, theta=th0, g=g)), steps, th0,
+                            sub, h_amp))
+    return reqs

@@ -1,0 +1,91 @@
+"""CPU-side checks of the boundary: the library loads without a GPU, exports
+every function include/swalbe_gb300.h declares, and rejects bad arguments on
+the host before touching the device."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import swalbe_gb300 as sw
+from swalbe_gb300 import _lib as L
+
+
+@pytest.fixture(scope="module")
+def lib():
+    sw.build()
+    return sw.lib()
+
+
+def test_exports_every_declared_symbol(lib):
+    names = L.header_functions()
+    assert len(names) >= 40
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert missing == []
+
+
+def test_abi_version(lib):
+    assert lib.swb_abi_version() == 1
+
+
+@pytest.mark.parametrize("bad", [dict(Lx=0), dict(tau=0.0), dict(n=3, m=3), dict(hmin=0.0),
+                                 dict(Lx=100000, Ly=100000)])
+def test_create_rejects_bad_params(lib, bad):
+    kw = dict(Lx=8, Ly=8)
+    kw.update(bad)
+    s = sw.SysConst(kw.pop("Lx"), kw.pop("Ly"), sw.Taumucs(**kw))
+    h = C.c_void_p()
+    p = s.c_params()
+    st = lib.swb_create(C.byref(p), L.SWB_F64, C.byref(h))
+    assert st == L.SWB_ERR_ARG
+    assert h.value is None
+    assert lib.swb_last_error(None)
+
+
+def test_thermal_is_unsupported(lib):
+    s = sw.SysConst(8, 8, sw.Taumucs(kbt=1e-6))
+    h = C.c_void_p()
+    p = s.c_params()
+    assert lib.swb_create(C.byref(p), L.SWB_F32, C.byref(h)) == L.SWB_ERR_UNSUPPORTED
+
+
+def test_state_bytes(lib):
+    s = sw.SysConst(512, 512)
+    b = C.c_size_t()
+    p = s.c_params()
+    assert lib.swb_state_bytes(C.byref(p), L.SWB_F32, C.byref(b)) == 0
+    # two FP32 population buffers dominate: 2 * 9 * 4 B per cell
+    assert 72 * 512 * 512 <= b.value < 100 * 512 * 512 + (8 << 20)
+    assert lib.swb_state_bytes(C.byref(p), L.SWB_F16, C.byref(b)) == 0
+    assert 40 * 512 * 512 <= b.value
+
+
+def test_null_arguments(lib):
+    assert lib.swb_step(None, 1) == L.SWB_ERR_ARG
+    assert lib.swb_set_field(None, 0, None) == L.SWB_ERR_ARG
+    assert lib.swb_batch_step(None, 1) == L.SWB_ERR_ARG
+    assert lib.swb_server_poll(None, 1, None, None) == L.SWB_ERR_ARG
+
+
+def test_taumucs_defaults():
+    # src/initialize.jl:43-60
+    p = sw.Taumucs()
+    assert p.Tmax == 1000 and p.tdump == 100 and p.tau == 1.0
+    assert p.mu == pytest.approx(1 / 6) and p.n == 9 and p.m == 3 and p.theta == 1 / 9
+    q = sw.Taumucs(τ=0.8, γ=0.02, θ=0.25)
+    assert q.tau == 0.8 and q.gamma == 0.02 and q.θ == 0.25
+    assert q.mu == pytest.approx((1 / 3) * 0.3)
+
+
+def test_host_initial_values_match_oracle(orc):
+    h = sw.singledroplet(np.zeros((60, 50)), 20, 1 / 6, (30, 25))
+    ref = orc.singledroplet(60, 50, 20, 1 / 6, (30, 25))
+    assert np.allclose(h, ref, rtol=0, atol=1e-13)
+    two = sw.two_caps(80, 40, 15, 12, 1 / 6, 1 / 5, (25, 20), (55, 20))
+    assert two.min() > 0 and two.max() > 1  # only negatives are clamped, as in the reference
+
+
+def test_device_strings():
+    with pytest.raises(ValueError):
+        sw.Sys(sw.SysConst(4, 4), "CPU")
+    with pytest.raises(NotImplementedError):
+        sw.Sys(sw.SysConst(4, 4), "GB300", kind="thermal")
