@@ -170,6 +170,19 @@ int swb_steps_done(swb_state *s, int64_t *t);
 int swb_get_measures(swb_state *s, swb_measure *out, int64_t cap, int64_t *count);
 /* Measures of the current height now (mass, wetted, max/min, area). */
 int swb_measure_now(swb_state *s, double hthresh, swb_measure *out);
+/* The same measures of a caller's Float64 column-major DEVICE height field,
+ * without any device allocation by the library.  No counterpart in the
+ * reference: it serves callers that must not allocate (a host that has
+ * committed its whole HBM budget, or whose own memory pool owns the device).
+ * Scratch is a fixed 48 KiB array compiled into the library; lattices up to
+ * 2^28 cells (larger: SWB_ERR_ARG).  d_cos_theta: per-cell cospi(θ) on the
+ * device or NULL (then cos_theta is used for the energy).  Runs on `stream`
+ * (NULL: the default stream) and synchronises it.  The first call on each
+ * device looks up the array's address, so make it before any stream capture.
+ * All calls share the array: calls that overlap on the GPU race. */
+int swb_measure_field_noalloc(const double *d_height, int Lx, int Ly, double hthresh,
+                              const double *d_cos_theta, double cos_theta, void *stream,
+                              swb_measure *out);
 
 /* ---------------------------------------------------------------------- */
 /* Per-op API, SWB_PLAIN64 only: one kernel per reference op on the full   */

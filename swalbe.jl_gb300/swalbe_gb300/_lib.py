@@ -100,6 +100,7 @@ def lib() -> C.CDLL:
             "swb_steps_done": (i, [p, C.POINTER(i64)]),
             "swb_get_measures": (i, [p, C.POINTER(Measure), i64, C.POINTER(i64)]),
             "swb_measure_now": (i, [p, d, C.POINTER(Measure)]),
+            "swb_measure_field_noalloc": (i, [p, i, i, d, p, d, p, C.POINTER(Measure)]),
             "swb_op_filmpressure": (i, [p]),
             "swb_op_hgradp": (i, [p]),
             "swb_op_slippage": (i, [p]),

@@ -25,6 +25,7 @@ UNITS = {
     "swb_api.cu": [],
     "swb_batch.cu": [],
     "swb_server.cu": [],
+    "swb_noalloc.cu": [],
 }
 
 
