@@ -154,6 +154,12 @@ int swb_set_theta_wave(swb_state *s, double theta0, double dtheta, double v);
 int swb_set_inclination(swb_state *s, double ax, double ay, int loop_time, int64_t t,
                         int64_t tstart, int64_t tsmooth);
 
+/* SWB_F32 / SWB_F16: hold the total mass at its value when the fields were
+ * last set, by an FP64-measured correction spread over the cells (default:
+ * on for SWB_F16; off for SWB_F32, whose compensated f0 closure already
+ * conserves mass to ~1e-12; no effect in SWB_F64, the reference's arithmetic). */
+int swb_set_mass_correction(swb_state *s, int on);
+
 /* Which measures swb_step records each iteration (SWB_MEAS_* mask). */
 int swb_set_measures(swb_state *s, int mask, double hthresh);
 

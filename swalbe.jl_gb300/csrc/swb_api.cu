@@ -474,7 +474,7 @@ int swb_create(const swb_params *p, int precision, swb_state **out) {
     s->pitch = pitch_of(s->N);
     fill_args_from_params(s->a, *p);
     s->a.pitch = s->pitch;
-    s->a.mass_corr = (precision == SWB_F32 || precision == SWB_F16) ? 1 : 0;
+    s->a.mass_corr = (precision == SWB_F16) ? 1 : 0;
     auto bad = [&](int code) {
         std::string m = s->err.empty() ? g_err : s->err;
         delete s;
@@ -739,6 +739,16 @@ int swb_set_inclination(swb_state *s, double ax, double ay, int loop_time, int64
     a.incl_tstart = tstart;
     a.incl_tsmooth = tsmooth;
     s->invalidate_graph();
+    return SWB_OK;
+}
+
+int swb_set_mass_correction(swb_state *s, int on) {
+    if (!s) return fail(nullptr, SWB_ERR_ARG, "state is NULL");
+    const int v = (on && (s->precision == SWB_F32 || s->precision == SWB_F16)) ? 1 : 0;
+    if (s->a.mass_corr != v) {
+        s->a.mass_corr = v;
+        s->invalidate_graph();
+    }
     return SWB_OK;
 }
 

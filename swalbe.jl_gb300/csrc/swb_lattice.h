@@ -78,7 +78,7 @@ inline StepArgs lattice_args(const swb_params &p, int precision, char *base, con
     a.tiles_x = (p.Lx + kTX - 1) / kTX;
     a.tiles_y = (p.Ly + kTY - 1) / kTY;
     a.hthresh = 0.055;
-    a.mass_corr = (precision == SWB_F32 || precision == SWB_F16) ? 1 : 0;
+    a.mass_corr = (precision == SWB_F16) ? 1 : 0;
     a.records = nullptr;
     a.rec_cap = 0;
     a.meas_mask = 0;

@@ -603,11 +603,13 @@ __device__ __forceinline__ void step_tile(const StepArgs &a, int bx, int by,
         } else {
             // FP32 arithmetic.  f0 closes the mass balance with the values as
             // stored: f0 = M - Σ_{q>0} f_q, where M (the pulled mass, hi + lo)
-            // is what the cell must hold.  FP32 populations: f0's own rounding
-            // error, the lo part of M and the FP64-measured correction are
-            // folded into f1 and f3 equally (momentum unchanged), where they
-            // are resolved to ~ulp(f1).  FP16 populations: f0 takes lo and the
-            // correction, the latter by stochastic rounding.
+            // is what the cell must hold.  e, the exact rounding error of f0
+            // (Fast2Sum), the lo part of M and the FP64-measured correction
+            // are then put back: FP32 populations fold them into f1 and f3
+            // equally (momentum unchanged), resolved to ~ulp(f1); FP16
+            // populations add them to f0 by stochastic rounding, so that the
+            // per-cell storage error is unbiased (round-to-nearest would drop
+            // the sub-ulp term every step and drift).
             R fe[9], fo[9];
             feq_fast(h, ux, uy, g, fe);
 #pragma unroll
@@ -620,15 +622,14 @@ __device__ __forceinline__ void step_tile(const StepArgs &a, int bx, int by,
             const R mc = (a.tau_is_one || !fresh) ? h : omeg * hft + invtau * h;
             const R ssum = small8(fo);
             R f0 = mc - ssum;
+            const R e = (mc - f0) - ssum;
             if constexpr (!S::kHalf) {
-                const R e = (mc - f0) - ssum;  // exact error of f0 (Fast2Sum)
                 const R d = R(0.5) * (e + hlo + R(corr));
                 fo[1] = fo[1] + d;
                 fo[3] = fo[3] + d;
             } else {
-                f0 = f0 + hlo;
-                if (corr != 0.0)
-                    f0 = add_stochastic((float)f0, (float)corr, mix32((unsigned)cell, (unsigned)t));
+                f0 = add_stochastic((float)f0, (float)(e + hlo + R(corr)),
+                                    mix32((unsigned)cell, (unsigned)t));
             }
             fo[0] = f0;
 #pragma unroll

@@ -95,6 +95,7 @@ def lib() -> C.CDLL:
             "swb_set_theta_wave": (i, [p, d, d, d]),
             "swb_set_inclination": (i, [p, d, d, i, i64, i64, i64]),
             "swb_set_measures": (i, [p, i, d]),
+            "swb_set_mass_correction": (i, [p, i]),
             "swb_step": (i, [p, i64]),
             "swb_sync": (i, [p]),
             "swb_steps_done": (i, [p, C.POINTER(i64)]),

@@ -191,6 +191,9 @@ class GB300State:
         self._chk(lib().swb_set_inclination(self._h, float(alpha[0]), float(alpha[1]),
                                             int(loop_time), int(t), int(tstart), int(tsmooth)))
 
+    def set_mass_correction(self, on: bool) -> None:
+        self._chk(lib().swb_set_mass_correction(self._h, int(bool(on))))
+
     def set_measures(self, mask: int, hthresh: float = 0.055) -> None:
         self._chk(lib().swb_set_measures(self._h, int(mask), float(hthresh)))
 

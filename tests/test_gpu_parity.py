@@ -221,11 +221,14 @@ def test_low_precision_droplet(T, tol):
     h = st.height
     assert rel_l2(h, ref.height) < tol
     recs = st.measures()
-    m0, m1 = recs[0].mass, recs[-1].mass
-    # FP32 storage rounds each cell's f0 to ~6e-8: the stored mass has a noise
-    # floor of ~sqrt(N)*6e-8; the FP64-measured correction keeps the drift at
-    # that floor instead of letting it accumulate.
-    assert abs(m1 - m0) / m0 < 1e-9
+    m = np.array([r.mass for r in recs])
+    drift = np.abs(m - m[0]).max() / m[0]
+    # FP32 populations: f0's rounding error is folded into f1/f3, mass is kept
+    # to ~1e-12 (measured 3e-12).  FP16 populations: f0 (FP32) is stochastically
+    # rounded, each cell's storage error is ~ulp(h)/2 and unbiased; on 96² cells
+    # the FP64-measured correction holds the mass at that noise floor
+    # (sqrt(N) * 5e-8 / M ≈ 4e-9; measured max 5.6e-9 over 300 steps).
+    assert drift < (1e-10 if T == np.float32 else 2e-8)
     assert abs(h.sum() - h0.sum()) / h0.sum() < 1e-6
 
 
@@ -235,10 +238,11 @@ def test_low_precision_mass_drift_large(T):
     n = 2048
     s = sysc(n, n)
     st = gpu_run(s, rough(n, n, 17, amp=0.1), 600, T=T, meas=L.MEAS_MASS)
-    recs = st.measures()
-    m0 = recs[0].mass
-    drift = max(abs(r.mass - m0) for r in recs) / m0
-    assert drift < 1e-10
+    m = np.array([r.mass for r in st.measures()])
+    drift = np.abs(m - m[0]) / m[0]
+    assert drift[-1] < 1e-10
+    # FP16: the per-step noise floor is ~2.4e-11 on 2048² cells
+    assert drift.max() < (1e-10 if T == np.float32 else 2e-10)
 
 
 def test_fp32_rayleigh_taylor_short():
