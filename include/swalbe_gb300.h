@@ -154,6 +154,16 @@ int swb_set_theta_wave(swb_state *s, double theta0, double dtheta, double v);
 int swb_set_inclination(swb_state *s, double ax, double ay, int loop_time, int64_t t,
                         int64_t tstart, int64_t tsmooth);
 
+/* Strip geometry of the fused step: CTAs of nt threads (64, 128, 256) own
+ * strips of nt-4 columns and h rows (4..512).  By default SWB_F64 / SWB_F32
+ * states autotune it on their first swb_step of >= 256 steps (timing a few
+ * geometries on those real steps; remembered per lattice size), and SWB_F16
+ * states use a size rule.  Setting it (or (0, 0): the size rule) turns the
+ * autotuner off.  Results do not depend on it, except through the order of
+ * the FP64 mass sum that drives the SWB_F16 mass correction. */
+int swb_set_geometry(swb_state *s, int nt, int h);
+int swb_get_geometry(swb_state *s, int *nt, int *h);
+
 /* SWB_F32 / SWB_F16: hold the total mass at its value when the fields were
  * last set, by an FP64-measured correction spread over the cells (default:
  * on for SWB_F16; off for SWB_F32, whose compensated f0 closure already

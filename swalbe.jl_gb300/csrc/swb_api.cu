@@ -5,6 +5,7 @@
 // are launched asynchronously; repeated launches are captured once into a
 // CUDA graph and replayed (the step counter lives on the device, so the
 // same graph serves every chunk of steps).
+#include <array>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -113,8 +114,6 @@ void fill_args_from_params(StepArgs &a, const swb_params &p) {
     a.theta_mode = swb::THETA_SCALAR;
     a.kap = host_kappa(p.theta, p.n, p.m, p.hmin);
     a.cos_theta = host_cospi(p.theta);
-    a.tiles_x = (p.Lx + swb::kTX - 1) / swb::kTX;
-    a.tiles_y = (p.Ly + swb::kTY - 1) / swb::kTY;
     a.hthresh = 0.055;
 }
 
@@ -173,9 +172,10 @@ void set_global_error(const char *msg) { g_err = msg; }
 static std::atomic<unsigned long long> g_launches{0};
 void count_launches(unsigned long long n) { g_launches += n; }
 
-cudaError_t launch_fused_step(int precision, const StepArgs &a, cudaStream_t st) {
+cudaError_t launch_fused_step(int precision, const StepArgs &a, int k, cudaStream_t st) {
     count_launches(1);
-    return precision == SWB_F64 ? launch_fused_step_f64(a, st) : launch_fused_step_f32(precision, a, st);
+    return precision == SWB_F64 ? launch_fused_step_f64(a, k, st)
+                                : launch_fused_step_f32(precision, a, k, st);
 }
 cudaError_t launch_moments(int precision, const StepArgs &a, cudaStream_t st) {
     count_launches(1);
@@ -190,14 +190,36 @@ cudaError_t launch_pressure_now(int precision, const StepArgs &a, double *out, c
     return precision == SWB_F64 ? launch_pressure_now_f64(a, out, st)
                                 : launch_pressure_now_f32(precision, a, out, st);
 }
-cudaError_t launch_batch_step(int precision, const StepArgs *d_args, const TileRef *d_tiles,
-                              int ntiles, int grid, cudaStream_t st) {
+cudaError_t launch_batch_step(int precision, int nt, const StepArgs *d_args,
+                              const TileRef *d_tiles, int ntiles, int grid, int k,
+                              cudaStream_t st) {
     count_launches(1);
-    return precision == SWB_F64 ? launch_batch_step_f64(d_args, d_tiles, ntiles, grid, st)
-                                : launch_batch_step_f32(precision, d_args, d_tiles, ntiles, grid, st);
+    return precision == SWB_F64 ? launch_batch_step_f64(nt, d_args, d_tiles, ntiles, grid, k, st)
+                                : launch_batch_step_f32(precision, nt, d_args, d_tiles, ntiles, grid, k, st);
 }
-int batch_blocks_per_sm(int precision) {
-    return precision == SWB_F64 ? batch_blocks_per_sm_f64() : batch_blocks_per_sm_f32(precision);
+int batch_blocks_per_sm(int precision, int nt) {
+    return precision == SWB_F64 ? batch_blocks_per_sm_f64(nt) : batch_blocks_per_sm_f32(precision, nt);
+}
+
+// Default strip geometry by lattice size (from sweeps on GB300): narrow
+// strips (64 threads) and as many rows per strip as still leave ~1000 CTAs;
+// FP16 small lattices prefer 128-thread strips.
+void default_geometry(int Lx, int Ly, int precision, int *nt, int *h) {
+    int n = *nt;
+    if (!n) n = (precision == SWB_F16 && (long long)Lx * Ly <= 512LL * 512) ? 128 : 64;
+    const long long strips = (Lx + n - 5) / (n - 4);
+    const long long want = precision == SWB_F64 ? 600 : 1000;
+    int hh = kMinRows;
+    for (int cand : {32, 16, 8}) {
+        if (precision != SWB_F64 && cand > 16) continue;
+        if (strips * ((Ly + cand - 1) / cand) >= want) {
+            hh = cand;
+            break;
+        }
+    }
+    if (hh > Ly) hh = Ly < kMinRows ? kMinRows : Ly;
+    *nt = n;
+    *h = hh;
 }
 }  // namespace swb
 
@@ -228,6 +250,9 @@ struct swb_state {
     int incl = 0, incl_loop_time = 0;
     double ax = 0, ay = 0;
     long long incl_t = 1000, incl_tstart = 0, incl_tsmooth = 1;
+    // strip geometry: autotuned on the first long run unless set explicitly
+    bool tuned = false;
+    bool autotune = true;
     // graph cache
     cudaGraphExec_t gexec = nullptr;
     int gsteps = 0;
@@ -309,7 +334,13 @@ int materialize(swb_state *s) {
     return SWB_OK;
 }
 
-__global__ void set_fresh_kernel(Control *c) { c->fresh = 1; }
+// The next iteration takes h, u from the fields; the FP16 mass correction
+// restarts from the mass of that iteration.
+__global__ void set_fresh_kernel(Control *c) {
+    c->fresh_step = c->step_base + 1;
+    c->corr[0] = 0.0;
+    c->corr[1] = 0.0;
+}
 __global__ void d2f_kernel(const double *src, float *dst, long long n) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x)
@@ -367,16 +398,103 @@ int plain_iteration(swb_state *s) {
 
 constexpr int kGraphSteps = 64;
 
+// Geometries chosen by the autotuner, per (Lx, Ly, precision), process-wide.
+std::mutex g_tune_mu;
+std::vector<std::array<int, 5>> g_tuned;  // Lx, Ly, precision, nt, h
+
+bool tuned_lookup(int Lx, int Ly, int prec, int *nt, int *h) {
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    for (auto &e : g_tuned)
+        if (e[0] == Lx && e[1] == Ly && e[2] == prec) {
+            *nt = e[3];
+            *h = e[4];
+            return true;
+        }
+    return false;
+}
+
+// n step launches (k = 0..n-1) and the advance kernel that closes them.
+cudaError_t launch_sequence(swb_state *s, int n) {
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < n && e == cudaSuccess; ++k)
+        e = swb::launch_fused_step(s->precision, s->a, k, s->stream);
+    if (e == cudaSuccess) e = swb::launch_advance(s->a, n, s->stream);
+    return e;
+}
+
+// Autotuner: times a few strip geometries on real steps (each probe is a
+// complete launch sequence, so nothing is wasted) and keeps the fastest.
+// Only for SWB_F64 / SWB_F32, whose results do not depend on the geometry.
+constexpr int kTuneMinSteps = 256;
+constexpr int kTuneProbe = 8;
+
+int autotune_geometry(swb_state *s, long long &left) {
+    int nt = 0, h = 0;
+    if (tuned_lookup(s->p.Lx, s->p.Ly, s->precision, &nt, &h)) {
+        swb::set_geometry(s->a, nt, h);
+        s->invalidate_graph();
+        s->tuned = true;
+        return SWB_OK;
+    }
+    const int cands[][2] = {{64, 4}, {64, 8}, {64, 16}, {64, 32}, {128, 4}, {128, 16}, {256, 16}};
+    cudaEvent_t e0, e1;
+    CUDA_TRY(&s->err, cudaEventCreate(&e0));
+    CUDA_TRY(&s->err, cudaEventCreate(&e1));
+    float best = 1e30f;
+    int bnt = s->a.march_nt, bh = s->a.march_h;
+    int rc = SWB_OK;
+    bool first = true;
+    for (auto &c : cands) {
+        if (c[1] > s->p.Ly && c[1] != swb::kMinRows) continue;
+        swb::set_geometry(s->a, c[0], c[1]);
+        if (first) {  // warm-up with the first candidate
+            cudaError_t e = launch_sequence(s, kTuneProbe);
+            if (e != cudaSuccess) { rc = fail(&s->err, SWB_ERR_CUDA, cudaGetErrorString(e)); break; }
+            left -= kTuneProbe;
+            s->steps += kTuneProbe;
+            first = false;
+        }
+        cudaEventRecord(e0, s->stream);
+        cudaError_t e = launch_sequence(s, kTuneProbe);
+        cudaEventRecord(e1, s->stream);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        if (e != cudaSuccess) { rc = fail(&s->err, SWB_ERR_CUDA, cudaGetErrorString(e)); break; }
+        left -= kTuneProbe;
+        s->steps += kTuneProbe;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best) {
+            best = ms;
+            bnt = c[0];
+            bh = c[1];
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    swb::set_geometry(s->a, bnt, bh);
+    s->invalidate_graph();
+    s->tuned = true;
+    if (rc == SWB_OK) {
+        std::lock_guard<std::mutex> g(g_tune_mu);
+        g_tuned.push_back({s->p.Lx, s->p.Ly, s->precision, bnt, bh});
+    }
+    return rc;
+}
+
 int fused_steps(swb_state *s, long long nsteps) {
     long long left = nsteps;
+    const long long steps0 = s->steps;
+    if (!s->tuned && s->autotune && left >= kTuneMinSteps &&
+        (s->precision == SWB_F64 || s->precision == SWB_F32)) {
+        int rc = autotune_geometry(s, left);
+        if (rc) return rc;
+    }
     if (left >= kGraphSteps) {
         if (!s->gvalid) {
             cudaGraph_t g = nullptr;
             CUDA_TRY(&s->err, cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
-            cudaError_t le = cudaSuccess;
-            for (int k = 0; k < kGraphSteps && le == cudaSuccess; ++k)
-                le = swb::launch_fused_step(s->precision, s->a, s->stream);
-            swb::count_launches(0ULL - (unsigned long long)kGraphSteps);  // captured, not run
+            cudaError_t le = launch_sequence(s, kGraphSteps);
+            swb::count_launches(0ULL - (unsigned long long)(kGraphSteps + 1));  // captured, not run
             cudaError_t ce = cudaStreamEndCapture(s->stream, &g);
             if (le != cudaSuccess) {
                 if (g) cudaGraphDestroy(g);
@@ -391,12 +509,12 @@ int fused_steps(swb_state *s, long long nsteps) {
         }
         while (left >= s->gsteps) {
             CUDA_TRY(&s->err, cudaGraphLaunch(s->gexec, s->stream));
-            swb::count_launches(s->gsteps);
+            swb::count_launches(s->gsteps + 1);
             left -= s->gsteps;
         }
     }
-    for (; left > 0; --left) CUDA_TRY(&s->err, swb::launch_fused_step(s->precision, s->a, s->stream));
-    s->steps += nsteps;
+    if (left > 0) CUDA_TRY(&s->err, launch_sequence(s, (int)left));
+    s->steps = steps0 + nsteps;
     if (nsteps > 0) {
         s->host_fresh = false;
         s->fields_current = false;
@@ -445,13 +563,13 @@ int swb_state_bytes(const swb_params *p, int precision, size_t *bytes) {
     if (rc) return rc;
     if (!bytes) return fail(nullptr, SWB_ERR_ARG, "bytes is NULL");
     const long long N = (long long)p->Lx * p->Ly, pitch = pitch_of(N);
-    const long long tiles = (long long)((p->Lx + swb::kTX - 1) / swb::kTX) * ((p->Ly + swb::kTY - 1) / swb::kTY);
+    const long long tiles = swb::max_tiles(p->Lx, p->Ly);
     size_t b = 0;
     if (precision == SWB_PLAIN64) {
         b = align256((size_t)27 * N * 8) + 11 * align256((size_t)N * 8);
     } else if (precision == SWB_F64 || precision == SWB_F32 || precision == SWB_F16) {
         b = 2 * align256(fbuf_bytes(precision, pitch)) + 3 * align256((size_t)N * real_bytes(precision)) +
-            align256((size_t)tiles * swb::kNPart * 8) + align256(sizeof(Control));
+            align256((size_t)2 * tiles * swb::kNPart * 8) + align256(sizeof(Control));
     } else {
         return fail(nullptr, SWB_ERR_ARG, "unknown precision");
     }
@@ -527,10 +645,14 @@ int swb_create(const swb_params *p, int precision, swb_state **out) {
         else
             fill_kernel_f<<<blocks_for(N), 256, 0, s->stream>>>((float *)a.hF, N, 1.0f);
         CREATE_TRY(cudaGetLastError());
-        CREATE_TRY(s->alloc((void **)&a.partials, (size_t)a.tiles_x * a.tiles_y * swb::kNPart * 8));
+        int gnt = 0, gh = 0;
+        swb::default_geometry(p->Lx, p->Ly, precision, &gnt, &gh);
+        swb::set_geometry(a, gnt, gh);
+        a.part_stride = (int)swb::max_tiles(p->Lx, p->Ly);
+        CREATE_TRY(s->alloc((void **)&a.partials, (size_t)2 * a.part_stride * swb::kNPart * 8));
         CREATE_TRY(s->alloc((void **)&a.ctl, sizeof(Control)));
         Control c0{};
-        c0.fresh = 1;
+        c0.fresh_step = 1;
         CREATE_TRY(cudaMemcpyAsync(a.ctl, &c0, sizeof(Control), cudaMemcpyHostToDevice, s->stream));
     }
     CREATE_TRY(s->alloc((void **)&s->rec, (size_t)swb::kRecCap * sizeof(Record)));
@@ -739,6 +861,31 @@ int swb_set_inclination(swb_state *s, double ax, double ay, int loop_time, int64
     a.incl_tstart = tstart;
     a.incl_tsmooth = tsmooth;
     s->invalidate_graph();
+    return SWB_OK;
+}
+
+int swb_set_geometry(swb_state *s, int nt, int h) {
+    if (!s) return fail(nullptr, SWB_ERR_ARG, "state is NULL");
+    if (s->plain()) return SWB_OK;
+    if (nt == 0 && h == 0) {
+        swb::default_geometry(s->p.Lx, s->p.Ly, s->precision, &nt, &h);  // nt == 0: choose
+    } else if ((nt != 64 && nt != 128 && nt != 256) || h < swb::kMinRows || h > swb::kMaxRows) {
+        return fail(&s->err, SWB_ERR_ARG, "geometry: nt must be 64, 128 or 256 and 4 <= h <= 512");
+    }
+    s->autotune = false;  // an explicit geometry (or the default) is kept
+    s->tuned = true;
+    if (s->a.march_nt != nt || s->a.march_h != h) {
+        CUDA_TRY(&s->err, cudaStreamSynchronize(s->stream));
+        swb::set_geometry(s->a, nt, h);
+        s->invalidate_graph();
+    }
+    return SWB_OK;
+}
+
+int swb_get_geometry(swb_state *s, int *nt, int *h) {
+    if (!s || !nt || !h) return fail(s ? &s->err : nullptr, SWB_ERR_ARG, "NULL argument");
+    *nt = s->a.march_nt;
+    *h = s->a.march_h;
     return SWB_OK;
 }
 

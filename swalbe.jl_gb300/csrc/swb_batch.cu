@@ -41,7 +41,11 @@ __global__ void d2f(const double *s, float *d, long long n) {
          i += (long long)gridDim.x * blockDim.x)
         d[i] = (float)s[i];
 }
-__global__ void set_fresh_k(Control *c) { c->fresh = 1; }
+__global__ void set_fresh_k(Control *c) {
+    c->fresh_step = c->step_base + 1;
+    c->corr[0] = 0.0;
+    c->corr[1] = 0.0;
+}
 
 int nblk(long long n) {
     long long b = (n + 255) / 256;
@@ -81,7 +85,7 @@ cudaError_t lattice_init(const StepArgs &a, int precision, const LatticeLayout &
         if (e != cudaSuccess) return e;
     }
     Control c0{};
-    c0.fresh = 1;
+    c0.fresh_step = 1;
     // c0 lives on this stack frame: a pageable-memory copy is staged before return
     e = cudaMemcpyAsync(a.ctl, &c0, sizeof(Control), cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return e;
@@ -188,9 +192,18 @@ int upload_args(swb_batch *b) {
     return SWB_OK;
 }
 
+// n batched step launches (k = 0..n-1) and the advance kernel closing them.
+cudaError_t batch_sequence(swb_batch *b, int n, int grid) {
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < n && e == cudaSuccess; ++k)
+        e = swb::launch_batch_step(b->precision, swb::kBatchNT, b->d_args, b->d_tiles, b->ntiles,
+                                   grid, k, b->stream);
+    if (e == cudaSuccess && n > 0) e = swb::launch_batch_advance(b->d_args, b->count, n, b->stream);
+    return e;
+}
+
 int launch_n(swb_batch *b, int n, int grid) {
-    for (int k = 0; k < n; ++k)
-        B_TRY(b, swb::launch_batch_step(b->precision, b->d_args, b->d_tiles, b->ntiles, grid, b->stream));
+    B_TRY(b, batch_sequence(b, n, grid));
     return SWB_OK;
 }
 
@@ -199,7 +212,7 @@ int autotune(swb_batch *b, long long &left) {
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int occ = swb::batch_blocks_per_sm(b->precision);
+    const int occ = swb::batch_blocks_per_sm(b->precision, swb::kBatchNT);
     std::vector<int> cands = {b->ntiles};
     for (int k = 1; k <= occ; ++k) cands.push_back(std::min(b->ntiles, sms * k));
     std::sort(cands.begin(), cands.end());
@@ -288,14 +301,16 @@ int swb_batch_create(const swb_params *params, int count, int precision, swb_bat
     b->slab_bytes = off;
     BC_TRY(cudaMalloc((void **)&b->slab, off));
     BC_TRY(cudaMalloc((void **)&b->staging, (size_t)maxN * 8));
-    std::vector<TileRef> tiles;
+    std::vector<TileRef> tiles, reducers;
     for (int i = 0; i < count; ++i) {
         StepArgs a = swb::lattice_args(params[i], precision, b->slab + offs[i], b->layouts[i]);
         b->args.push_back(a);
         BC_TRY(swb::lattice_init(a, precision, b->layouts[i], nullptr, b->stream));
+        if (swb::needs_partials(a)) reducers.push_back({i, -1, 0});
         for (int ty = 0; ty < a.tiles_y; ++ty)
             for (int tx = 0; tx < a.tiles_x; ++tx) tiles.push_back({i, tx, ty});
     }
+    tiles.insert(tiles.begin(), reducers.begin(), reducers.end());
     b->fields_current.assign(count, 1);
     b->ntiles = (int)tiles.size();
     BC_TRY(cudaMalloc((void **)&b->d_args, sizeof(StepArgs) * count));
@@ -351,9 +366,8 @@ int swb_batch_step(swb_batch *b, int64_t nsteps) {
         if (!b->gvalid) {
             cudaGraph_t g = nullptr;
             B_TRY(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-            cudaError_t le = cudaSuccess;
-            for (int k = 0; k < b->steps_per_graph && le == cudaSuccess; ++k)
-                le = swb::launch_batch_step(b->precision, b->d_args, b->d_tiles, b->ntiles, b->grid, b->stream);
+            cudaError_t le = batch_sequence(b, b->steps_per_graph, b->grid);
+            swb::count_launches(0ULL - (unsigned long long)(b->steps_per_graph + 1));
             cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
             if (le != cudaSuccess) {
                 if (g) cudaGraphDestroy(g);
@@ -367,6 +381,7 @@ int swb_batch_step(swb_batch *b, int64_t nsteps) {
         }
         while (left >= b->steps_per_graph) {
             B_TRY(b, cudaGraphLaunch(b->gexec, b->stream));
+            swb::count_launches(b->steps_per_graph + 1);
             left -= b->steps_per_graph;
         }
     }
@@ -385,8 +400,8 @@ int swb_batch_sync(swb_batch *b) {
 
 int swb_batch_tile(swb_batch *b, int *tile_x, int *tile_y, int *steps_per_graph) {
     if (!b) return swb::bfail(nullptr, SWB_ERR_ARG, "batch is NULL");
-    if (tile_x) *tile_x = b->tuned ? swb::kTX : 0;
-    if (tile_y) *tile_y = b->tuned ? swb::kTY : 0;
+    if (tile_x) *tile_x = b->tuned ? swb::kBatchNT - 4 : 0;
+    if (tile_y) *tile_y = b->tuned ? b->args[0].march_h : 0;
     if (steps_per_graph) *steps_per_graph = b->tuned ? b->steps_per_graph : 0;
     return SWB_OK;
 }

@@ -8,30 +8,38 @@
 
 namespace swb {
 
-// Fused-step tile: TX x TY interior cells per CTA, NTX x NTY threads.
-// The pressure needs h at radius 1, the force p at radius 1, so a tile stages
-// h on (TX+4) x (TY+4) and p on (TX+2) x (TY+2) in shared memory.
-constexpr int kTX = 32;
-constexpr int kTY = 16;
-constexpr int kThreads = 256;
+// Fused step geometry: a CTA of NT threads (64, 128 or 256) owns a strip of
+// NT - 4 columns and H rows (kMinRows..kMaxRows).  Partial-measure buffers
+// are sized for the finest decomposition (NT = 64, H = kMinRows).
+constexpr int kMinRows = 4;
+constexpr int kMaxRows = 512;
+inline long long max_tiles(int Lx, int Ly) {  // per parity slot
+    return (long long)((Lx + 59) / 60) * ((Ly + kMinRows - 1) / kMinRows);
+}
+// CTA width of batched and served lattices (all share one launch).
+constexpr int kBatchNT = 128;
+// Default geometry for a lattice.  *nt on entry: 0 to choose the width too,
+// or a width (64, 128, 256) to keep; *h: rows per strip.
+void default_geometry(int Lx, int Ly, int precision, int *nt, int *h);
 
 // Measure partials per block: mass, wetted, hmax, hmin, area, cos-sum.
 constexpr int kNPart = 6;
 // Capacity of the per-step measure ring of a single state (records).
 constexpr int kRecCap = 65536;
 
-// Device-side control block of one lattice.  The step counter lives on the
-// device so that a captured CUDA graph can be replayed: each launch reads
-// `step`, and the last CTA to finish (ticket) advances it.
+// Device-side control block of one lattice.  A launch sequence of n steps
+// is n step kernels (launch index k = 0..n-1, time_loop iteration
+// t = step_base + k + 1) followed by an advance kernel that reduces the last
+// step's measures and adds n to step_base; a captured CUDA graph replays such
+// a sequence.  No CTA ever waits for another: the measures of iteration t are
+// reduced by an extra CTA of launch t+1 (or by the advance kernel).
 struct Control {
-    long long step;          // iterations completed
-    unsigned int ticket;     // CTAs finished in the current launch
-    int fresh;               // 1: next step takes h, u from the fields
+    long long step_base;     // iterations completed before the current sequence
+    long long fresh_step;    // iteration that takes h, u from the fields (0: none)
     int nan_flag;            // set when a non-finite height is seen
     int pad0;
-    double mass_target;      // FP32/FP16 mass correction: mass to hold
-    double mass_last;        // mass of the height at the start of the last step
-    double corr_last;        // correction added per cell in the last step
+    double mass_target;      // FP16 mass correction: mass to hold
+    double corr[2];          // correction per cell for iteration t in slot t & 1
     long long rec_head;      // records written (monotone)
 };
 
@@ -66,18 +74,30 @@ struct StepArgs {
     int meas_mask;
     double hthresh;
     int mass_corr;
-    double *partials;         // [blocks][kNPart]
+    double *partials;         // [2][max_tiles][kNPart]: slot by iteration parity
     Record *records;          // ring of rec_cap records (may be null if meas_mask == 0)
     int rec_cap;
     Control *ctl;
-    int tiles_x, tiles_y;     // tile grid of this lattice
+    int part_stride;          // partial slots per parity (max_tiles of the lattice)
+    int tiles_x, tiles_y;     // strip grid of this lattice: ceil(Lx/(NT-4)) x ceil(Ly/H)
+    int march_nt, march_h;    // threads per CTA (strip width + 4) and rows per strip
 };
 
-// Entry in the packed tile table of a batch.
+inline void set_geometry(StepArgs &a, int nt, int h) {
+    a.march_nt = nt;
+    a.march_h = h;
+    a.tiles_x = (a.Lx + nt - 5) / (nt - 4);
+    a.tiles_y = (a.Ly + h - 1) / h;
+}
+
+// Entry in the packed tile table of a batch (tx = -1: the lattice's reducer).
 struct TileRef {
     int lattice;
     int tx, ty;
 };
+
+// Whether the step kernels of a lattice produce per-step partial measures.
+__host__ __device__ inline bool needs_partials(const StepArgs &a) { return a.meas_mask != 0 || a.mass_corr != 0; }
 
 // Error text returned by swb_last_error(NULL) on the calling thread.
 void set_global_error(const char *msg);
@@ -86,28 +106,38 @@ void count_launches(unsigned long long n);
 
 // ---- launchers (defined in the .cu files) ----
 // precision: SWB_F64 (swb_step_f64.cu) / SWB_F32, SWB_F16 (swb_step_f32.cu)
-cudaError_t launch_fused_step(int precision, const StepArgs &a, cudaStream_t st);
+// Step kernel number k of a sequence, and the sequence's closing advance
+// kernel (precision independent, defined in swb_step_f64.cu).
+cudaError_t launch_fused_step(int precision, const StepArgs &a, int k, cudaStream_t st);
+cudaError_t launch_advance(const StepArgs &a, int n, cudaStream_t st);
+cudaError_t launch_batch_advance(const StepArgs *d_args, int count, int n, cudaStream_t st);
+// CTAs of step launch k of a single lattice: its strips, plus the reducer.
+inline int step_grid(const StepArgs &a, int k) {
+    return a.tiles_x * a.tiles_y + ((needs_partials(a) && k > 0) ? 1 : 0);
+}
 cudaError_t launch_moments(int precision, const StepArgs &a, cudaStream_t st);
 cudaError_t launch_fout(int precision, const StepArgs &a, double *out, cudaStream_t st);
 cudaError_t launch_pressure_now(int precision, const StepArgs &a, double *out, cudaStream_t st);
-cudaError_t launch_batch_step(int precision, const StepArgs *d_args, const TileRef *d_tiles,
-                              int ntiles, int grid, cudaStream_t st);
-int batch_blocks_per_sm(int precision);
-cudaError_t launch_fused_step_f64(const StepArgs &a, cudaStream_t st);
+cudaError_t launch_batch_step(int precision, int nt, const StepArgs *d_args,
+                              const TileRef *d_tiles, int ntiles, int grid, int k,
+                              cudaStream_t st);
+int batch_blocks_per_sm(int precision, int nt);
+cudaError_t launch_fused_step_f64(const StepArgs &a, int k, cudaStream_t st);
 cudaError_t launch_moments_f64(const StepArgs &a, cudaStream_t st);
 cudaError_t launch_fout_f64(const StepArgs &a, double *out, cudaStream_t st);
 cudaError_t launch_pressure_now_f64(const StepArgs &a, double *out, cudaStream_t st);
-cudaError_t launch_batch_step_f64(const StepArgs *d_args, const TileRef *d_tiles, int ntiles,
-                                  int grid, cudaStream_t st);
-cudaError_t launch_fused_step_f32(int precision, const StepArgs &a, cudaStream_t st);
+cudaError_t launch_batch_step_f64(int nt, const StepArgs *d_args, const TileRef *d_tiles,
+                                  int ntiles, int grid, int k, cudaStream_t st);
+cudaError_t launch_fused_step_f32(int precision, const StepArgs &a, int k, cudaStream_t st);
 cudaError_t launch_moments_f32(int precision, const StepArgs &a, cudaStream_t st);
 cudaError_t launch_fout_f32(int precision, const StepArgs &a, double *out, cudaStream_t st);
 cudaError_t launch_pressure_now_f32(int precision, const StepArgs &a, double *out,
                                     cudaStream_t st);
-cudaError_t launch_batch_step_f32(int precision, const StepArgs *d_args, const TileRef *d_tiles,
-                                  int ntiles, int grid, cudaStream_t st);
-int batch_blocks_per_sm_f64();
-int batch_blocks_per_sm_f32(int precision);
+cudaError_t launch_batch_step_f32(int precision, int nt, const StepArgs *d_args,
+                                  const TileRef *d_tiles, int ntiles, int grid, int k,
+                                  cudaStream_t st);
+int batch_blocks_per_sm_f64(int nt);
+int batch_blocks_per_sm_f32(int precision, int nt);
 
 // plain FP64 per-op kernels (reference operation order)
 struct PlainState {

@@ -32,7 +32,7 @@ struct LatticeLayout {
 
 inline LatticeLayout lattice_layout(const swb_params &p, int precision) {
     const long long N = (long long)p.Lx * p.Ly, pitch = pitch_for(N);
-    const int tiles = ((p.Lx + kTX - 1) / kTX) * ((p.Ly + kTY - 1) / kTY);
+    const long long tiles = max_tiles(p.Lx, p.Ly);
     LatticeLayout L{};
     size_t o = 0;
     const size_t fb = align256(fbuf_bytes_of(precision, pitch));
@@ -42,7 +42,7 @@ inline LatticeLayout lattice_layout(const swb_params &p, int precision) {
     L.h = o; o += fld;
     L.ux = o; o += fld;
     L.uy = o; o += fld;
-    L.partials = o; o += align256((size_t)tiles * kNPart * 8);
+    L.partials = o; o += align256((size_t)2 * tiles * kNPart * 8);
     L.ctl = o; o += align256(sizeof(Control));
     L.total = o;
     return L;
@@ -60,6 +60,7 @@ inline StepArgs lattice_args(const swb_params &p, int precision, char *base, con
     a.uxF = base + L.ux;
     a.uyF = base + L.uy;
     a.partials = (double *)(base + L.partials);
+    a.part_stride = (int)max_tiles(p.Lx, p.Ly);
     a.ctl = (Control *)(base + L.ctl);
     a.gamma = p.gamma;
     a.hmin = p.hmin;
@@ -75,8 +76,9 @@ inline StepArgs lattice_args(const swb_params &p, int precision, char *base, con
     a.theta_mode = THETA_SCALAR;
     a.kap = host_kappa_shared(p.theta, p.n, p.m, p.hmin);
     a.cos_theta = host_cospi_shared(p.theta);
-    a.tiles_x = (p.Lx + kTX - 1) / kTX;
-    a.tiles_y = (p.Ly + kTY - 1) / kTY;
+    int nt = kBatchNT, h;  // one CTA width serves every lattice of a batch
+    default_geometry(p.Lx, p.Ly, precision, &nt, &h);
+    set_geometry(a, nt, h);
     a.hthresh = 0.055;
     a.mass_corr = (precision == SWB_F16) ? 1 : 0;
     a.records = nullptr;

@@ -121,13 +121,15 @@ bool admit_device(swb_server *sv, Req *r) {
 
 bool upload_table(swb_server *sv) {
     std::vector<StepArgs> args;
-    std::vector<TileRef> tiles;
+    std::vector<TileRef> tiles, reducers;
     for (size_t i = 0; i < sv->active.size(); ++i) {
         const StepArgs &a = sv->active[i]->a;
         args.push_back(a);
+        if (swb::needs_partials(a)) reducers.push_back({(int)i, -1, 0});
         for (int ty = 0; ty < a.tiles_y; ++ty)
             for (int tx = 0; tx < a.tiles_x; ++tx) tiles.push_back({(int)i, tx, ty});
     }
+    tiles.insert(tiles.begin(), reducers.begin(), reducers.end());
     if (args.size() > sv->cap_args) {
         cudaFree(sv->d_args);
         sv->cap_args = std::max<size_t>(args.size(), 2 * sv->cap_args);
@@ -147,7 +149,7 @@ bool upload_table(swb_server *sv) {
 
 int count_tiles(swb_server *sv) {
     int n = 0;
-    for (Req *r : sv->active) n += r->a.tiles_x * r->a.tiles_y;
+    for (Req *r : sv->active) n += r->a.tiles_x * r->a.tiles_y + (swb::needs_partials(r->a) ? 1 : 0);
     return n;
 }
 
@@ -155,7 +157,7 @@ void worker_main(swb_server *sv) {
     cudaSetDevice(sv->device);
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, sv->device);
-    const int occ = swb::batch_blocks_per_sm(sv->precision);
+    const int occ = swb::batch_blocks_per_sm(sv->precision, swb::kBatchNT);
     for (;;) {
         std::vector<Req *> admitted;
         bool changed = false;
@@ -221,7 +223,10 @@ void worker_main(swb_server *sv) {
         const double tb = sv->now();
         cudaError_t e = cudaSuccess;
         for (int64_t k = 0; k < tick && e == cudaSuccess; ++k)
-            e = swb::launch_batch_step(sv->precision, sv->d_args, sv->d_tiles, ntiles, grid, sv->stream);
+            e = swb::launch_batch_step(sv->precision, swb::kBatchNT, sv->d_args, sv->d_tiles, ntiles,
+                                       grid, (int)k, sv->stream);
+        if (e == cudaSuccess)
+            e = swb::launch_batch_advance(sv->d_args, (int)sv->active.size(), (int)tick, sv->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(sv->stream);
         double lu = 0.0;
         std::vector<Req *> finished;

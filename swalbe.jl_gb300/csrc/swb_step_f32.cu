@@ -1,6 +1,8 @@
 // swb_step_f32.cu -- FP32-arithmetic kernels: FP32 populations (SWB_F32) and
-// FP32 f0 with FP16 f1..f8 (SWB_F16).  Contraction into FMA is allowed here;
-// parity with the Float64 oracle is checked against stated tolerances.
+// FP32 f0 with FP16 f1..f8 (SWB_F16).  Compiled with --fmad=false so that the
+// single-lattice and batch kernels, which inline the same step code, round
+// identically; parity with the Float64 oracle is checked against stated
+// tolerances.
 #include "swb_step_impl.cuh"
 
 namespace swb {
@@ -24,9 +26,23 @@ int grid_for(long long n, int threads) {
         }                                       \
     } while (0)
 
-cudaError_t launch_fused_step_f32(int precision, const StepArgs &a, cudaStream_t st) {
-    dim3 grid(a.tiles_x, a.tiles_y);
-    DISPATCH_STORE(precision, (fused_step_kernel<S><<<grid, kThreads, 0, st>>>(a)));
+#define DISPATCH_NT(nt, ...)                       \
+    do {                                           \
+        if ((nt) == 64) {                          \
+            constexpr int NT = 64;                 \
+            __VA_ARGS__;                           \
+        } else if ((nt) == 256) {                  \
+            constexpr int NT = 256;                \
+            __VA_ARGS__;                           \
+        } else {                                   \
+            constexpr int NT = 128;                \
+            __VA_ARGS__;                           \
+        }                                          \
+    } while (0)
+
+cudaError_t launch_fused_step_f32(int precision, const StepArgs &a, int k, cudaStream_t st) {
+    const int grid = step_grid(a, k);
+    DISPATCH_STORE(precision, DISPATCH_NT(a.march_nt, (fused_step_kernel<S, NT><<<grid, NT, 0, st>>>(a, k))));
     return cudaGetLastError();
 }
 
@@ -49,18 +65,16 @@ cudaError_t launch_pressure_now_f32(int precision, const StepArgs &a, double *ou
     return cudaGetLastError();
 }
 
-cudaError_t launch_batch_step_f32(int precision, const StepArgs *d_args, const TileRef *d_tiles,
-                                  int ntiles, int grid, cudaStream_t st) {
-    DISPATCH_STORE(precision, (batch_step_kernel<S><<<grid, kThreads, 0, st>>>(d_args, d_tiles, ntiles)));
+cudaError_t launch_batch_step_f32(int precision, int nt, const StepArgs *d_args,
+                                  const TileRef *d_tiles, int ntiles, int grid, int k,
+                                  cudaStream_t st) {
+    DISPATCH_STORE(precision, DISPATCH_NT(nt, (batch_step_kernel<S, NT><<<grid, NT, 0, st>>>(d_args, d_tiles, ntiles, k))));
     return cudaGetLastError();
 }
 
-int batch_blocks_per_sm_f32(int precision) {
+int batch_blocks_per_sm_f32(int precision, int nt) {
     int n = 0;
-    if (precision == SWB_F16)
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_step_kernel<StoreF16>, kThreads, 0);
-    else
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_step_kernel<StoreF32>, kThreads, 0);
+    DISPATCH_STORE(precision, DISPATCH_NT(nt, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_step_kernel<S, NT>, NT, 0)));
     return n < 1 ? 1 : n;
 }
 

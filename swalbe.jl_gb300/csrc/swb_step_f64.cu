@@ -9,9 +9,35 @@
 namespace swb {
 
 // ------------------------------------------------------------ fused, Float64
-cudaError_t launch_fused_step_f64(const StepArgs &a, cudaStream_t st) {
-    dim3 grid(a.tiles_x, a.tiles_y);
-    fused_step_kernel<StoreF64><<<grid, kThreads, 0, st>>>(a);
+#define DISPATCH_NT(nt, ...)                       \
+    do {                                           \
+        if ((nt) == 64) {                          \
+            constexpr int NT = 64;                 \
+            __VA_ARGS__;                           \
+        } else if ((nt) == 256) {                  \
+            constexpr int NT = 256;                \
+            __VA_ARGS__;                           \
+        } else {                                   \
+            constexpr int NT = 128;                \
+            __VA_ARGS__;                           \
+        }                                          \
+    } while (0)
+
+cudaError_t launch_fused_step_f64(const StepArgs &a, int k, cudaStream_t st) {
+    const int grid = step_grid(a, k);
+    DISPATCH_NT(a.march_nt, (fused_step_kernel<StoreF64, NT><<<grid, NT, 0, st>>>(a, k)));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_advance(const StepArgs &a, int n, cudaStream_t st) {
+    count_launches(1);
+    advance_kernel<128><<<1, 128, 0, st>>>(a, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_advance(const StepArgs *d_args, int count, int n, cudaStream_t st) {
+    count_launches(1);
+    batch_advance_kernel<128><<<count, 128, 0, st>>>(d_args, n);
     return cudaGetLastError();
 }
 
@@ -36,15 +62,15 @@ cudaError_t launch_pressure_now_f64(const StepArgs &a, double *out, cudaStream_t
     return cudaGetLastError();
 }
 
-cudaError_t launch_batch_step_f64(const StepArgs *d_args, const TileRef *d_tiles, int ntiles,
-                                  int grid, cudaStream_t st) {
-    batch_step_kernel<StoreF64><<<grid, kThreads, 0, st>>>(d_args, d_tiles, ntiles);
+cudaError_t launch_batch_step_f64(int nt, const StepArgs *d_args, const TileRef *d_tiles,
+                                  int ntiles, int grid, int k, cudaStream_t st) {
+    DISPATCH_NT(nt, (batch_step_kernel<StoreF64, NT><<<grid, NT, 0, st>>>(d_args, d_tiles, ntiles, k)));
     return cudaGetLastError();
 }
 
-int batch_blocks_per_sm_f64() {
+int batch_blocks_per_sm_f64(int nt) {
     int n = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_step_kernel<StoreF64>, kThreads, 0);
+    DISPATCH_NT(nt, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_step_kernel<StoreF64, NT>, NT, 0));
     return n < 1 ? 1 : n;
 }
 

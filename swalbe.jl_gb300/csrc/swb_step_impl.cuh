@@ -363,180 +363,195 @@ __device__ __forceinline__ PartT<R> block_reduce(PartT<R> p, PartT<R> *red) {
     return p;
 }
 
-// ------------------------------------------------------------ the tile step
-template <class S, int TX, int TY>
-struct TileSmem {
+// ------------------------------------------------------------ the marching step
+// A CTA of NT threads owns a strip of W = NT - 4 columns and H rows of one
+// lattice; thread t owns column x0 - 2 + t for the whole strip.  It sweeps the
+// rows in order, keeping in shared memory the heights of rows y-2..y+2 (ring
+// of 5), the film pressure of rows y-1..y+1 and the momenta of the rows whose
+// output is pending (rings of 4).  Per output row y it
+//   1. turns the pulled populations of row y+2 (prefetched into registers one
+//      row earlier) into h, j = Σ c_q f_q and the rounding residue of h;
+//   2. issues the pull of row y+3 (in flight during 3-4);
+//   3. computes p on row y+1 (columns 1..NT-2);
+//   4. computes forces, equilibrium and collision of row y and stores it.
+// Only the x halo (4 of NT columns) and the 4 extra rows of each strip are
+// recomputed; the column index math is done once per thread.
+template <class S, int NT>
+struct MarchSmem {
     using R = typename S::real;
-    R h[TY + 4][TX + 4];
-    R jx[TY][TX];
-    R jy[TY][TX];
-    R hlo[TY][TX];  // FP32 paths: rounding error of the pulled height
-    R p[TY + 2][TX + 2];
-    R kapc[TX + 2];
-    R cosc[TX];
-    PartT<R> red[kThreads / 32];
-    PartT<double> redd[kThreads / 32];
-    int last;
+    R h[5][NT];
+    R p[4][NT];
+    R jx[4][NT];
+    R jy[4][NT];
+    R lo[4][NT];  // FP32 paths: rounding error of the pulled height
+    R kapc[NT];   // moving-wettability mode: kappa per column
+    R cosc[NT];   // moving-wettability mode: cospi(θ) per column
+    PartT<R> red[NT / 32];
+    PartT<double> redd[NT / 32];
 };
 
-// Finishes a launch for one lattice: block partials, ticket, and in the last
-// CTA the lattice-wide reduction (Float64, fixed order: deterministic), the
-// per-step record and the control update.  No CTA ever waits on another.
+// Block partial measures of iteration t into its parity slot.
 template <int NT, class R>
-__device__ void finish_lattice(const StepArgs &a, const PartT<R> &part, int any_nan,
-                               long long step, int fresh, double corr, int nblocks, int blin,
-                               PartT<R> *red, PartT<double> *redd, int *s_last) {
-    const bool need = (a.meas_mask != 0) || a.mass_corr;
-    PartT<R> tot;
-    if (need) tot = block_reduce<NT>(part, red);
+__device__ __forceinline__ void write_partials(const StepArgs &a, const PartT<R> &part,
+                                               long long t, int blin, PartT<R> *red) {
+    const PartT<R> tot = block_reduce<NT>(part, red);
     if (threadIdx.x == 0) {
-        if (any_nan) a.ctl->nan_flag = 1;
-        if (need) {
-            double *pp = a.partials + (size_t)blin * kNPart;
-            pp[0] = (double)tot.mhi + (double)tot.mlo;
-            pp[1] = (double)tot.wet;
-            pp[2] = (double)tot.hmax;
-            pp[3] = (double)tot.hmin;
-            pp[4] = (double)tot.area;
-            pp[5] = (double)tot.cossum;
-        }
-        __threadfence();
-        unsigned int prev = atomicAdd(&a.ctl->ticket, 1u);
-        *s_last = (prev == (unsigned int)(nblocks - 1));
+        double *pp = a.partials + ((size_t)(t & 1) * (size_t)a.part_stride + (size_t)blin) * kNPart;
+        pp[0] = (double)tot.mhi + (double)tot.mlo;
+        pp[1] = (double)tot.wet;
+        pp[2] = (double)tot.hmax;
+        pp[3] = (double)tot.hmin;
+        pp[4] = (double)tot.area;
+        pp[5] = (double)tot.cossum;
     }
-    __syncthreads();
-    if (!*s_last) return;
-    __threadfence();
+}
+
+// Lattice-wide measures of iteration s (its partials are complete: they were
+// written by an earlier launch): Float64, fixed order, so deterministic.
+// Writes the per-step record and, for the FP16 mass correction, the
+// correction of iteration s + 2.  M(s) is the mass of the populations
+// iteration s pulled; the corrections c(s) and c(s+1) were applied after that
+// and are not in it, so
+//   c(s+2) = (M_target - M(s) - N (c(s) + c(s+1))) / N
+// makes M(s+3) = M_target up to three steps of rounding noise.
+template <int NT>
+__device__ void reduce_step(const StepArgs &a, long long s, PartT<double> *redd) {
+    const int nblocks = a.tiles_x * a.tiles_y;
+    const double *base = a.partials + (size_t)(s & 1) * (size_t)a.part_stride * kNPart;
     PartT<double> acc;
     part_init(acc);
-    if (need) {
-        for (int b = threadIdx.x; b < nblocks; b += NT) {
-            const double *pp = a.partials + (size_t)b * kNPart;
-            PartT<double> q;
-            q.mhi = __ldcg(pp + 0);
-            q.mlo = 0.0;
-            q.wet = (int)__ldcg(pp + 1);
-            q.hmax = __ldcg(pp + 2);
-            q.hmin = __ldcg(pp + 3);
-            q.area = __ldcg(pp + 4);
-            q.cossum = __ldcg(pp + 5);
-            part_merge(acc, q);
-        }
-        acc = block_reduce<NT>(acc, redd);
+    for (int b = threadIdx.x; b < nblocks; b += NT) {
+        const double *pp = base + (size_t)b * kNPart;
+        PartT<double> q;
+        q.mhi = __ldcg(pp + 0);
+        q.mlo = 0.0;
+        q.wet = (int)__ldcg(pp + 1);
+        q.hmax = __ldcg(pp + 2);
+        q.hmin = __ldcg(pp + 3);
+        q.area = __ldcg(pp + 4);
+        q.cossum = __ldcg(pp + 5);
+        part_merge(acc, q);
     }
+    acc = block_reduce<NT>(acc, redd);
     if (threadIdx.x == 0) {
-        const long long t = step + 1;
+        Control *c = a.ctl;
         const double mass = acc.mhi + acc.mlo;
         if (a.meas_mask) {
-            Record &r = a.records[(t - 1) % a.rec_cap];
-            r.t = t;
+            Record &r = a.records[(s - 1) % a.rec_cap];
+            r.t = s;
             r.mass = mass;
             r.wetted = (double)acc.wet;
             r.hmax = acc.hmax;
             r.hmin = acc.hmin;
             r.area = acc.area;
             r.cos_sum = a.theta_mode == THETA_SCALAR ? (double)acc.wet * a.cos_theta : acc.cossum;
-            a.ctl->rec_head = a.ctl->rec_head + 1;
+            c->rec_head = c->rec_head + 1;
         }
         if (a.mass_corr) {
-            if (fresh) a.ctl->mass_target = mass;
-            a.ctl->mass_last = mass;
-            a.ctl->corr_last = corr;
+            if (s == c->fresh_step) c->mass_target = mass;
+            const double N = (double)a.Lx * (double)a.Ly;
+            const double in_flight = c->corr[s & 1] + c->corr[(s + 1) & 1];
+            c->corr[s & 1] = (c->mass_target - mass - N * in_flight) / N;
         }
-        a.ctl->fresh = 0;
-        a.ctl->ticket = 0u;
-        __threadfence();
-        a.ctl->step = t;
     }
 }
 
-// One time_loop iteration on tile (bx, by) of the lattice described by `a`.
-template <class S, int TX, int TY, int NT>
-__device__ __forceinline__ void step_tile(const StepArgs &a, int bx, int by,
-                                          TileSmem<S, TX, TY> &sm) {
+// One time_loop iteration on strip (bx, by) of the lattice described by `a`.
+template <class S, int NT>
+__device__ __forceinline__ void march_tile(const StepArgs &a, int bx, int by, int k,
+                                           MarchSmem<S, NT> &sm) {
     using R = typename S::real;
     constexpr bool LIT = S::kLiteral;
-    const int tid = threadIdx.x;
+    constexpr int W = NT - 4;
+    const int t = threadIdx.x;
     const int Lx = a.Lx, Ly = a.Ly;
+    const int H = a.march_h;
     const long long pitch = a.pitch;
-    const long long step = a.ctl->step;
-    const int fresh = a.ctl->fresh;
-    const long long t = step + 1;  // 1-based time_loop iteration
-    const void *src = (step & 1) ? a.fb : a.fa;
-    void *dst = (step & 1) ? a.fa : a.fb;
-    const int x0 = bx * TX, y0 = by * TY;
+    const long long done = a.ctl->step_base + k;  // iterations completed
+    const long long tt = done + 1;                // this time_loop iteration (1-based)
+    const int fresh = tt == a.ctl->fresh_step;
+    const void *src = (done & 1) ? a.fb : a.fa;
+    void *dst = (done & 1) ? a.fa : a.fb;
+    const int x0 = bx * W, y0 = by * H;
+    const int rows = min(H, Ly - y0);
     const R gamma = R(a.gamma), hmin = R(a.hmin), hcrit = R(a.hcrit);
 
-    // FP32/FP16: per-cell share of the mass correction, from the mass of the
-    // previous step's height and the correction applied then.
-    double corr = 0.0;
-    if (!LIT && a.mass_corr && !fresh) {
-        const double N = (double)Lx * (double)Ly;
-        corr = (a.ctl->mass_target - a.ctl->mass_last - N * a.ctl->corr_last) / N;
+    // this thread's column
+    const int gx = wrapc(x0 - 2 + t, Lx);
+    const int gxm = gx == 0 ? Lx - 1 : gx - 1, gxp = gx == Lx - 1 ? 0 : gx + 1;
+    const bool interior = t >= 2 && t < NT - 2 && x0 + t - 2 < Lx;
+    const bool pcol = t >= 1 && t < NT - 1;
+
+    // FP16: per-cell share of the mass correction of this iteration
+    const double corr = (!LIT && a.mass_corr && !fresh) ? a.ctl->corr[tt & 1] : 0.0;
+    // θ(x, t) of the moving-wettability mode depends on x only
+    if (a.theta_mode == THETA_WAVE) {
+        R th = R(a.theta0) + R(a.dtheta) * sinpi_r(R(2) * (R(gx) - R(a.wave_v) * R(tt)) / R(Lx));
+        sm.kapc[t] = kappa_of(th, a.n, a.m, hmin);
+        sm.cosc[t] = cospi_r(th);
     }
 
-    // ---- phase A: heights on the tile + 2 halo (moments of pulled f) ----
-    constexpr int AW = TX + 4, AH = TY + 4;
-    for (int idx = tid; idx < AW * AH; idx += NT) {
-        const int lx = idx % AW, ly = idx / AW;
-        const int gx = wrapc(x0 - 2 + lx, Lx), gy = wrapc(y0 - 2 + ly, Ly);
+    // pulled populations of the next leading row (prefetch; two in flight in the prologue)
+    R fa_[9], fb_[9];
+    auto issue = [&](R(&ft)[9], int yy) {
+        const int gy = wrapc(yy, Ly);
+        if (fresh) {
+            ft[0] = reinterpret_cast<const R *>(a.hF)[gy * Lx + gx];
+        } else {
+            const int gym = gy == 0 ? Ly - 1 : gy - 1, gyp = gy == Ly - 1 ? 0 : gy + 1;
+            pull9<S>(src, pitch, Lx, gx, gy, gxm, gxp, gym, gyp, ft);
+        }
+    };
+    auto consume = [&](const R(&ft)[9], int yy) {
+        const int r = yy - y0 + 2;  // >= 0
         R h, jx = R(0), jy = R(0), lo = R(0);
         if (fresh) {
-            h = reinterpret_cast<const R *>(a.hF)[gy * Lx + gx];
+            h = ft[0];
         } else {
-            const int gxm = gx == 0 ? Lx - 1 : gx - 1, gxp = gx == Lx - 1 ? 0 : gx + 1;
-            const int gym = gy == 0 ? Ly - 1 : gy - 1, gyp = gy == Ly - 1 ? 0 : gy + 1;
-            R ft[9];
-            pull9<S>(src, pitch, Lx, gx, gy, gxm, gxp, gym, gyp, ft);
             moments9<LIT>(ft, h, jx, jy);
             if constexpr (!LIT) lo = moments_lo(ft, h);
         }
-        sm.h[ly][lx] = h;
-        const int ix = lx - 2, iy = ly - 2;
-        if (ix >= 0 && ix < TX && iy >= 0 && iy < TY) {
-            sm.jx[iy][ix] = jx;
-            sm.jy[iy][ix] = jy;
-            sm.hlo[iy][ix] = lo;
-        }
-    }
-    // θ(x, t) of the moving-wettability mode depends on x only: one kappa
-    // per tile column.
-    if (a.theta_mode == THETA_WAVE) {
-        for (int c = tid; c < TX + 2; c += NT) {
-            const int gx = wrapc(x0 - 1 + c, Lx);
-            R th = R(a.theta0) + R(a.dtheta) * sinpi_r(R(2) * (R(gx) - R(a.wave_v) * R(t)) / R(Lx));
-            sm.kapc[c] = kappa_of(th, a.n, a.m, hmin);
-            if (c >= 1 && c <= TX) sm.cosc[c - 1] = cospi_r(th);
-        }
-    }
-    __syncthreads();
-
-    // ---- phase B: film pressure on the tile + 1 halo ----
-    constexpr int BW = TX + 2, BH = TY + 2;
-    for (int idx = tid; idx < BW * BH; idx += NT) {
-        const int lx = idx % BW, ly = idx / BW;
-        const int ax = lx + 1, ay = ly + 1;
+        sm.h[r % 5][t] = h;
+        sm.jx[r & 3][t] = jx;
+        sm.jy[r & 3][t] = jy;
+        sm.lo[r & 3][t] = lo;
+    };
+    auto pressure_row = [&](int yy) {
+        if (!pcol) return;
+        const int r = yy - y0 + 2;  // >= 1
+        const R *hm = sm.h[(r + 4) % 5], *hc = sm.h[r % 5], *hp = sm.h[(r + 1) % 5];
         R kap;
-        if (a.theta_mode == THETA_SCALAR) {
+        if (a.theta_mode == THETA_SCALAR)
             kap = R(a.kap);
-        } else if (a.theta_mode == THETA_FIELD) {
-            const int gx = wrapc(x0 - 1 + lx, Lx), gy = wrapc(y0 - 1 + ly, Ly);
-            kap = reinterpret_cast<const R *>(a.kapF)[gy * Lx + gx];
-        } else {
-            kap = sm.kapc[lx];
-        }
-        sm.p[ly][lx] = pressure_cell<LIT, R>(
-            sm.h[ay][ax], sm.h[ay][ax - 1], sm.h[ay - 1][ax], sm.h[ay][ax + 1], sm.h[ay + 1][ax],
-            sm.h[ay - 1][ax - 1], sm.h[ay - 1][ax + 1], sm.h[ay + 1][ax + 1],
-            sm.h[ay + 1][ax - 1], kap, gamma, hmin, hcrit, a.n, a.m);
-    }
-    __syncthreads();
+        else if (a.theta_mode == THETA_FIELD)
+            kap = reinterpret_cast<const R *>(a.kapF)[wrapc(yy, Ly) * Lx + gx];
+        else
+            kap = sm.kapc[t];
+        // ip = h[i-1,j], jp = h[i,j-1], im = h[i+1,j], jm = h[i,j+1], ...
+        sm.p[r & 3][t] = pressure_cell<LIT, R>(hc[t], hc[t - 1], hm[t], hc[t + 1], hp[t],
+                                               hm[t - 1], hm[t + 1], hp[t + 1], hp[t - 1], kap,
+                                               gamma, hmin, hcrit, a.n, a.m);
+    };
 
-    // ---- phase C: forces, equilibrium, collision on the interior ----
+    // prologue: heights of rows y0-2..y0+1 (two pulls in flight), then the
+    // pull of row y0+2 stays in flight into the loop
+    issue(fa_, y0 - 2);
+    issue(fb_, y0 - 1);
+    consume(fa_, y0 - 2);
+    issue(fa_, y0);
+    consume(fb_, y0 - 1);
+    issue(fb_, y0 + 1);
+    consume(fa_, y0);
+    issue(fa_, y0 + 2);
+    consume(fb_, y0 + 1);
+    __syncthreads();
+    pressure_row(y0 - 1);
+    pressure_row(y0);
+
     R incl_fac = R(0);
     if (a.incl) {
         incl_fac = a.incl_loop_time
-                       ? R(0.5) + R(0.5) * tanh_r(R(t - a.incl_tstart) / R(a.incl_tsmooth))
+                       ? R(0.5) + R(0.5) * tanh_r(R(tt - a.incl_tstart) / R(a.incl_tsmooth))
                        : R(a.incl_fixed);
     }
     const R delta6 = R(6.0 * a.delta), delta3sq = R(3.0 * (a.delta * a.delta)), mu6 = R(6.0 * a.mu);
@@ -545,25 +560,33 @@ __device__ __forceinline__ void step_tile(const StepArgs &a, int bx, int by,
     PartT<R> part;
     part_init(part);
     int any_nan = 0;
-    constexpr int ROWS = NT / TX;
-#pragma unroll 1
-    for (int k = 0; k < TY / ROWS; ++k) {
-        const int lx = tid % TX, ly = tid / TX + k * ROWS;
-        const int gx = x0 + lx, gy = y0 + ly;
-        if (gx >= Lx || gy >= Ly) continue;
+
+    auto row = [&](R(&ft)[9], int j) {
+        const int y = y0 + j;
+        consume(ft, y + 2);
+        if (j + 1 < rows) issue(ft, y + 3);  // one row ahead
+        __syncthreads();
+        pressure_row(y + 1);
+        __syncthreads();
+        if (!interior) return;
+        // ---- output row y, column gx ----
+        const int r = y - y0 + 2;
+        const int gy = wrapc(y, Ly);
         const int cell = gy * Lx + gx;
-        const R h = sm.h[ly + 2][lx + 2];
+        const R *hrow = sm.h[r % 5];
+        const R h = hrow[t];
         R ux, uy;
         if (fresh) {
             ux = reinterpret_cast<const R *>(a.uxF)[cell];
             uy = reinterpret_cast<const R *>(a.uyF)[cell];
         } else {
-            velocity<LIT>(h, sm.jx[ly][lx], sm.jy[ly][lx], ux, uy);
+            velocity<LIT>(h, sm.jx[r & 3][t], sm.jy[r & 3][t], ux, uy);
         }
         // h∇p! (src/forcing.jl:181-184)
+        const R *pm = sm.p[(r + 3) & 3], *pc = sm.p[r & 3], *pp = sm.p[(r + 1) & 3];
         R gpx, gpy;
-        grad9<R>(sm.p[ly + 1][lx], sm.p[ly][lx + 1], sm.p[ly + 1][lx + 2], sm.p[ly + 2][lx + 1],
-                 sm.p[ly][lx], sm.p[ly][lx + 2], sm.p[ly + 2][lx + 2], sm.p[ly + 2][lx], gpx, gpy);
+        grad9<R>(pc[t - 1], pm[t], pc[t + 1], pp[t], pm[t - 1], pm[t + 1], pp[t + 1], pp[t - 1],
+                 gpx, gpy);
         const R hgx = h * gpx, hgy = h * gpy;
         // slippage! (src/forcing.jl:43-44) and the force sum (src/simulate.jl:18-19)
         R sx, sy;
@@ -583,20 +606,19 @@ __device__ __forceinline__ void step_tile(const StepArgs &a, int bx, int by,
             Fy = Fy + (h * R(a.ay)) * incl_fac;
         }
         // collision (src/collide.jl:267-280); ftemp only matters for τ != 1
-        R ft[9];
+        R fq[9];
         R hft = h;
         if (!a.tau_is_one) {
-            const int gxm = gx == 0 ? Lx - 1 : gx - 1, gxp = gx == Lx - 1 ? 0 : gx + 1;
             const int gym = gy == 0 ? Ly - 1 : gy - 1, gyp = gy == Ly - 1 ? 0 : gy + 1;
-            pull9<S>(src, pitch, Lx, gx, gy, gxm, gxp, gym, gyp, ft);
-            if (!LIT) hft = ft[0] + small8(ft);
+            pull9<S>(src, pitch, Lx, gx, gy, gxm, gxp, gym, gyp, fq);
+            if (!LIT) hft = fq[0] + small8(fq);
         }
         if constexpr (LIT) {
             R fe[9];
             feq_literal<R>(h, ux, uy, g, fe);
 #pragma unroll
             for (int q = 0; q < 9; ++q) {
-                R v = a.tau_is_one ? fe[q] : omeg * ft[q] + invtau * fe[q];
+                R v = a.tau_is_one ? fe[q] : omeg * fq[q] + invtau * fe[q];
                 if (q > 0) v = v + source<R>(q, Fx, Fy);
                 S::st(dst, pitch, q, cell, v);
             }
@@ -614,22 +636,22 @@ __device__ __forceinline__ void step_tile(const StepArgs &a, int bx, int by,
             feq_fast(h, ux, uy, g, fe);
 #pragma unroll
             for (int q = 1; q < 9; ++q) {
-                R v = a.tau_is_one ? fe[q] : omeg * ft[q] + invtau * fe[q];
+                R v = a.tau_is_one ? fe[q] : omeg * fq[q] + invtau * fe[q];
                 fo[q] = S::rt(q, v + source<R>(q, Fx, Fy));
             }
-            const R hlo = fresh ? R(0) : sm.hlo[ly][lx];
+            const R hlo = fresh ? R(0) : sm.lo[r & 3][t];
             // Σ_q fpost_q = (1-1/τ) Σ ft + Σ feq/τ = h once h is the pulled mass
             const R mc = (a.tau_is_one || !fresh) ? h : omeg * hft + invtau * h;
             const R ssum = small8(fo);
             R f0 = mc - ssum;
             const R e = (mc - f0) - ssum;
             if constexpr (!S::kHalf) {
-                const R d = R(0.5) * (e + hlo + R(corr));
-                fo[1] = fo[1] + d;
-                fo[3] = fo[3] + d;
+                const R dd = R(0.5) * (e + hlo + R(corr));
+                fo[1] = fo[1] + dd;
+                fo[3] = fo[3] + dd;
             } else {
                 f0 = add_stochastic((float)f0, (float)(e + hlo + R(corr)),
-                                    mix32((unsigned)cell, (unsigned)t));
+                                    mix32((unsigned)cell, (unsigned)tt));
             }
             fo[0] = f0;
 #pragma unroll
@@ -640,53 +662,91 @@ __device__ __forceinline__ void step_tile(const StepArgs &a, int bx, int by,
         if (a.meas_mask || a.mass_corr) {
             mass_add(part, h);
             if constexpr (!LIT) {
-                if (!fresh) part.mlo += sm.hlo[ly][lx];
+                if (!fresh) part.mlo += sm.lo[r & 3][t];
             }
             const bool wet = h > thr;
             part.wet += wet ? 1 : 0;
             part.hmax = fmax(part.hmax, h);
             part.hmin = fmin(part.hmin, h);
             if ((a.meas_mask & SWB_MEAS_AREA) && wet) {
-                const int ax = lx + 2, ay = ly + 2;
+                const R *hm = sm.h[(r + 4) % 5], *hp = sm.h[(r + 1) % 5];
                 R gx2, gy2;
-                grad9<R>(sm.h[ay][ax - 1], sm.h[ay - 1][ax], sm.h[ay][ax + 1], sm.h[ay + 1][ax],
-                         sm.h[ay - 1][ax - 1], sm.h[ay - 1][ax + 1], sm.h[ay + 1][ax + 1],
-                         sm.h[ay + 1][ax - 1], gx2, gy2);
+                grad9<R>(hrow[t - 1], hm[t], hrow[t + 1], hp[t], hm[t - 1], hm[t + 1], hp[t + 1],
+                         hp[t - 1], gx2, gy2);
                 part.area += sqrt(gx2 * gx2 + gy2 * gy2 + R(1));
                 if (a.theta_mode == THETA_FIELD)
                     part.cossum += reinterpret_cast<const R *>(a.cosF)[cell];
                 else if (a.theta_mode == THETA_WAVE)
-                    part.cossum += sm.cosc[lx];
+                    part.cossum += sm.cosc[t];
             }
         }
-    }
+    };
+#pragma unroll 1
+    for (int j = 0; j < rows; ++j) row(fa_, j);
     any_nan = __syncthreads_or(any_nan);
-    const int nblocks = a.tiles_x * a.tiles_y;
-    finish_lattice<NT, R>(a, part, any_nan, step, fresh, corr, nblocks, by * a.tiles_x + bx,
-                          sm.red, sm.redd, &sm.last);
+    if (any_nan && t == 0) a.ctl->nan_flag = 1;
+    if (needs_partials(a)) write_partials<NT, R>(a, part, tt, by * a.tiles_x + bx, sm.red);
 }
 
-// Single lattice: one CTA per tile.
-template <class S>
-__global__ void __launch_bounds__(kThreads) fused_step_kernel(const StepArgs a) {
-    __shared__ TileSmem<S, kTX, kTY> sm;
-    step_tile<S, kTX, kTY, kThreads>(a, blockIdx.x, blockIdx.y, sm);
+// Single lattice: one CTA per strip, plus (when measures are kept and k > 0)
+// a reducer CTA, block 0, for the previous iteration's measures.
+template <class S, int NT>
+__global__ void __launch_bounds__(NT) fused_step_kernel(const StepArgs a, int k) {
+    __shared__ MarchSmem<S, NT> sm;
+    int b = blockIdx.x;
+    if (needs_partials(a) && k > 0) {
+        if (b == 0) {
+            reduce_step<NT>(a, a.ctl->step_base + k, sm.redd);
+            return;
+        }
+        b -= 1;
+    }
+    march_tile<S, NT>(a, b % a.tiles_x, b / a.tiles_x, k, sm);
 }
 
-// Batch: persistent CTAs walk a packed table of tiles of many lattices.
-template <class S>
-__global__ void __launch_bounds__(kThreads) batch_step_kernel(const StepArgs *__restrict__ args,
-                                                              const TileRef *__restrict__ tiles,
-                                                              int ntiles) {
-    __shared__ TileSmem<S, kTX, kTY> sm;
+// Closes a sequence of n step launches: the last iteration's measures, then
+// the step counter.  One CTA.
+template <int NT>
+__global__ void __launch_bounds__(NT) advance_kernel(const StepArgs a, int n) {
+    __shared__ PartT<double> redd[NT / 32];
+    const long long s = a.ctl->step_base + n;
+    if (needs_partials(a) && n > 0) reduce_step<NT>(a, s, redd);
+    __syncthreads();
+    if (threadIdx.x == 0) a.ctl->step_base = s;
+}
+
+// Batch: persistent CTAs walk a packed table of strips of many lattices;
+// entries with tx = -1 reduce their lattice's previous iteration.
+template <class S, int NT>
+__global__ void __launch_bounds__(NT) batch_step_kernel(const StepArgs *__restrict__ args,
+                                                        const TileRef *__restrict__ tiles,
+                                                        int ntiles, int k) {
+    __shared__ MarchSmem<S, NT> sm;
     __shared__ StepArgs sa;
-    for (int k = blockIdx.x; k < ntiles; k += gridDim.x) {
-        const TileRef tr = tiles[k];
+    for (int e = blockIdx.x; e < ntiles; e += gridDim.x) {
+        const TileRef tr = tiles[e];
         if (threadIdx.x == 0) sa = args[tr.lattice];
         __syncthreads();
-        step_tile<S, kTX, kTY, kThreads>(sa, tr.tx, tr.ty, sm);
+        if (tr.tx >= 0)
+            march_tile<S, NT>(sa, tr.tx, tr.ty, k, sm);
+        else if (k > 0)
+            reduce_step<NT>(sa, sa.ctl->step_base + k, sm.redd);
         __syncthreads();
     }
+}
+
+// One CTA per lattice closes a batch sequence of n launches.
+template <int NT>
+__global__ void __launch_bounds__(NT) batch_advance_kernel(const StepArgs *__restrict__ args,
+                                                           int n) {
+    __shared__ PartT<double> redd[NT / 32];
+    __shared__ StepArgs sa;
+    if (threadIdx.x == 0) sa = args[blockIdx.x];
+    __syncthreads();
+    const long long s = sa.ctl->step_base + n;
+    if (needs_partials(sa) && n > 0) reduce_step<NT>(sa, s, redd);
+    __syncthreads();
+    if (threadIdx.x == 0) sa.ctl->step_base = s;
 }
 
 // moments! into the fields (used when the host reads h/u).
@@ -694,7 +754,7 @@ template <class S>
 __global__ void moments_kernel(const StepArgs a) {
     using R = typename S::real;
     const int Lx = a.Lx, Ly = a.Ly;
-    const long long step = a.ctl->step;
+    const long long step = a.ctl->step_base;
     const void *src = (step & 1) ? a.fb : a.fa;
     for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < (long long)Lx * Ly;
          c += (long long)gridDim.x * blockDim.x) {
@@ -717,7 +777,7 @@ __global__ void fout_kernel(const StepArgs a, double *out) {
     using R = typename S::real;
     const int Lx = a.Lx, Ly = a.Ly;
     const long long N = (long long)Lx * Ly;
-    const long long step = a.ctl->step;
+    const long long step = a.ctl->step_base;
     const void *src = (step & 1) ? a.fb : a.fa;
     for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < N;
          c += (long long)gridDim.x * blockDim.x) {
@@ -736,7 +796,7 @@ __global__ void pressure_now_kernel(const StepArgs a, double *out) {
     using R = typename S::real;
     const int Lx = a.Lx, Ly = a.Ly;
     const R *h = reinterpret_cast<const R *>(a.hF);
-    const long long t = a.ctl->step + 1;
+    const long long t = a.ctl->step_base + 1;
     for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < (long long)Lx * Ly;
          c += (long long)gridDim.x * blockDim.x) {
         const int i = (int)(c % Lx), j = (int)(c / Lx);

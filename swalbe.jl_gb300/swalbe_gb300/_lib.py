@@ -96,6 +96,8 @@ def lib() -> C.CDLL:
             "swb_set_inclination": (i, [p, d, d, i, i64, i64, i64]),
             "swb_set_measures": (i, [p, i, d]),
             "swb_set_mass_correction": (i, [p, i]),
+            "swb_set_geometry": (i, [p, i, i]),
+            "swb_get_geometry": (i, [p, C.POINTER(i), C.POINTER(i)]),
             "swb_step": (i, [p, i64]),
             "swb_sync": (i, [p]),
             "swb_steps_done": (i, [p, C.POINTER(i64)]),

@@ -191,6 +191,14 @@ class GB300State:
         self._chk(lib().swb_set_inclination(self._h, float(alpha[0]), float(alpha[1]),
                                             int(loop_time), int(t), int(tstart), int(tsmooth)))
 
+    def set_geometry(self, nt: int = 0, h: int = 0) -> None:
+        self._chk(lib().swb_set_geometry(self._h, int(nt), int(h)))
+
+    def geometry(self):
+        a, b = C.c_int(), C.c_int()
+        self._chk(lib().swb_get_geometry(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
     def set_mass_correction(self, on: bool) -> None:
         self._chk(lib().swb_set_mass_correction(self._h, int(bool(on))))
 

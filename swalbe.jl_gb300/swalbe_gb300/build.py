@@ -21,7 +21,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall"]
 UNITS = {
     "swb_step_f64.cu": ["--fmad=false"],
-    "swb_step_f32.cu": [],
+    # no implicit FMA contraction: every kernel that inlines the step (single,
+    # batch) must round identically for results to be independent of it
+    "swb_step_f32.cu": ["--fmad=false"],
     "swb_api.cu": [],
     "swb_batch.cu": [],
     "swb_server.cu": [],

@@ -204,6 +204,26 @@ def test_config1_droplet_256_bit_exact():
     assert ref.wet[0] < ref.wet[-1]
 
 
+@pytest.mark.parametrize("T", [np.float64, np.float32])
+def test_geometry_does_not_change_results(T):
+    """Strip width and height are a performance choice only."""
+    Lx, Ly, steps = 150, 97, 120
+    s = sysc(Lx, Ly, tau=0.9, delta=2.0)
+    h0 = droplet(Lx, Ly, 30)
+    out = []
+    for nt, hh in ((64, 4), (128, 16), (256, 64), (128, 512)):
+        st = sw.Sys(s, "GB300", T=T)
+        st.set_geometry(nt, hh)
+        st.height = h0
+        st.step(steps)
+        out.append(st.height)
+    for o in out[1:]:
+        assert np.array_equal(o, out[0])
+    if T == np.float64:
+        ref = oracle.time_loop_literal(oparams(s), h0, steps)
+        assert np.array_equal(out[0], ref.height)
+
+
 # ------------------------------------------------------------------ FP32 / FP16
 def rel_l2(a, b):
     return float(np.linalg.norm(a - b) / np.linalg.norm(b))
@@ -276,7 +296,13 @@ def test_batch_matches_single():
             if i == 3:
                 st.set_theta_wave(1 / 5, 1 / 36, 1 / 98)
             st.step(137)
-            assert np.array_equal(b.get_height(i), st.height), (T, i)
+            if T == np.float16:
+                # the FP16 mass correction depends on the FP64 mass sum, whose
+                # order follows the strip decomposition (batch and single state
+                # may choose different strips)
+                assert np.allclose(b.get_height(i), st.height, rtol=1e-5, atol=0), (T, i)
+            else:
+                assert np.array_equal(b.get_height(i), st.height), (T, i)
         if T == np.float64:
             ref = oracle.time_loop_literal(oparams(systems[0]), hs[0], 137)
             assert np.array_equal(b.get_height(0), ref.height)
