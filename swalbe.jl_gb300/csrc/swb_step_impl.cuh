@@ -163,13 +163,19 @@ __device__ __forceinline__ R moments_lo(const R f[9], R h) {
     return small8(f) - (h - f[0]);
 }
 
+// a / b: IEEE in Float64 (the reference's rounding); in FP32 arithmetic the
+// fast reciprocal-based quotient (<= 2 ulp), whose error is far inside the
+// tolerance the FP32 modes are checked against.
+__device__ __forceinline__ double qdiv(double a, double b) { return a / b; }
+__device__ __forceinline__ float qdiv(float a, float b) { return __fdividef(a, b); }
+
 template <bool LIT, class R>
 __device__ __forceinline__ void velocity(R h, R jx, R jy, R &ux, R &uy) {
     if constexpr (LIT) {
         ux = jx / h;
         uy = jy / h;
     } else {
-        R inv = R(1) / h;
+        R inv = qdiv(R(1), h);
         ux = jx * inv;
         uy = jy * inv;
     }
@@ -181,7 +187,11 @@ template <bool LIT, class R>
 __device__ __forceinline__ R pressure_cell(R h, R ip, R jp, R im, R jm, R ipjp, R imjp, R imjm,
                                            R ipjm, R kap, R gamma, R hmin, R hcrit, int n,
                                            int m) {
-    R x = hmin / (h + hcrit);
+    R x;
+    if constexpr (LIT)
+        x = hmin / (h + hcrit);
+    else
+        x = qdiv(hmin, h + hcrit);
     R pn, pm;
     if (!LIT && n == 9 && m == 3) {
         R x3 = x * x * x;
@@ -384,8 +394,6 @@ struct MarchSmem {
     R jx[4][NT];
     R jy[4][NT];
     R lo[4][NT];  // FP32 paths: rounding error of the pulled height
-    R kapc[NT];   // moving-wettability mode: kappa per column
-    R cosc[NT];   // moving-wettability mode: cospi(θ) per column
     PartT<R> red[NT / 32];
     PartT<double> redd[NT / 32];
 };
@@ -418,20 +426,29 @@ template <int NT>
 __device__ void reduce_step(const StepArgs &a, long long s, PartT<double> *redd) {
     const int nblocks = a.tiles_x * a.tiles_y;
     const double *base = a.partials + (size_t)(s & 1) * (size_t)a.part_stride * kNPart;
-    PartT<double> acc;
-    part_init(acc);
+    // plain Float64 sums over the block partials (each already a compensated
+    // sum): ~1e-15 relative for a few thousand blocks.  Unrolled so that many
+    // partials are in flight at once: this CTA runs beside the strips and must
+    // not become the launch's straggler.
+    double m = 0.0, wt = 0.0, ar = 0.0, cs = 0.0, mx = -INFINITY, mn = INFINITY;
+#pragma unroll 4
     for (int b = threadIdx.x; b < nblocks; b += NT) {
         const double *pp = base + (size_t)b * kNPart;
-        PartT<double> q;
-        q.mhi = __ldcg(pp + 0);
-        q.mlo = 0.0;
-        q.wet = (int)__ldcg(pp + 1);
-        q.hmax = __ldcg(pp + 2);
-        q.hmin = __ldcg(pp + 3);
-        q.area = __ldcg(pp + 4);
-        q.cossum = __ldcg(pp + 5);
-        part_merge(acc, q);
+        m += __ldcg(pp + 0);
+        wt += __ldcg(pp + 1);
+        mx = fmax(mx, __ldcg(pp + 2));
+        mn = fmin(mn, __ldcg(pp + 3));
+        ar += __ldcg(pp + 4);
+        cs += __ldcg(pp + 5);
     }
+    PartT<double> acc;
+    acc.mhi = m;
+    acc.mlo = 0.0;
+    acc.wet = (int)wt;
+    acc.hmax = mx;
+    acc.hmin = mn;
+    acc.area = ar;
+    acc.cossum = cs;
     acc = block_reduce<NT>(acc, redd);
     if (threadIdx.x == 0) {
         Control *c = a.ctl;
@@ -456,10 +473,13 @@ __device__ void reduce_step(const StepArgs &a, long long s, PartT<double> *redd)
     }
 }
 
-// One time_loop iteration on strip (bx, by) of the lattice described by `a`.
-template <class S, int NT>
-__device__ __forceinline__ void march_tile(const StepArgs &a, int bx, int by, int k,
-                                           MarchSmem<S, NT> &sm) {
+// One time_loop iteration on strip (bx, by) of the lattice described by `a`,
+// compiled for the iteration's rare cases: FRESH (the first iteration after
+// the fields were set: h, u come from the fields) and TAU1 (τ = 1: the
+// previous populations drop out of the collision).
+template <class S, int NT, bool FRESH, bool TAU1>
+__device__ __forceinline__ void march_run(const StepArgs &a, int bx, int by, long long done,
+                                          MarchSmem<S, NT> &sm) {
     using R = typename S::real;
     constexpr bool LIT = S::kLiteral;
     constexpr int W = NT - 4;
@@ -467,14 +487,18 @@ __device__ __forceinline__ void march_tile(const StepArgs &a, int bx, int by, in
     const int Lx = a.Lx, Ly = a.Ly;
     const int H = a.march_h;
     const long long pitch = a.pitch;
-    const long long done = a.ctl->step_base + k;  // iterations completed
-    const long long tt = done + 1;                // this time_loop iteration (1-based)
-    const int fresh = tt == a.ctl->fresh_step;
+    const long long tt = done + 1;  // this time_loop iteration (1-based)
     const void *src = (done & 1) ? a.fb : a.fa;
     void *dst = (done & 1) ? a.fa : a.fb;
     const int x0 = bx * W, y0 = by * H;
     const int rows = min(H, Ly - y0);
     const R gamma = R(a.gamma), hmin = R(a.hmin), hcrit = R(a.hcrit);
+    // periodic row index; rows run from y0-2 to y0+rows+1, one wrap suffices
+    // unless the lattice is thinner than 3 rows
+    const bool tiny_y = Ly < 3;
+    auto wrow = [&](int yy) {
+        return tiny_y ? wrapc(yy, Ly) : (yy < 0 ? yy + Ly : (yy >= Ly ? yy - Ly : yy));
+    };
 
     // this thread's column
     const int gx = wrapc(x0 - 2 + t, Lx);
@@ -483,19 +507,22 @@ __device__ __forceinline__ void march_tile(const StepArgs &a, int bx, int by, in
     const bool pcol = t >= 1 && t < NT - 1;
 
     // FP16: per-cell share of the mass correction of this iteration
-    const double corr = (!LIT && a.mass_corr && !fresh) ? a.ctl->corr[tt & 1] : 0.0;
-    // θ(x, t) of the moving-wettability mode depends on x only
-    if (a.theta_mode == THETA_WAVE) {
-        R th = R(a.theta0) + R(a.dtheta) * sinpi_r(R(2) * (R(gx) - R(a.wave_v) * R(tt)) / R(Lx));
-        sm.kapc[t] = kappa_of(th, a.n, a.m, hmin);
-        sm.cosc[t] = cospi_r(th);
+    const double corr = (!LIT && !FRESH && a.mass_corr) ? a.ctl->corr[tt & 1] : 0.0;
+    // kappa and cospi(θ) of this column: constant (scalar θ) or θ(x, t) of
+    // the moving-wettability mode, which depends on x only
+    const int mode = a.theta_mode;
+    R kap_col = R(a.kap), cos_col = R(a.cos_theta);
+    if (mode == THETA_WAVE) {
+        const R th = R(a.theta0) + R(a.dtheta) * sinpi_r(R(2) * (R(gx) - R(a.wave_v) * R(tt)) / R(Lx));
+        kap_col = kappa_of(th, a.n, a.m, hmin);
+        cos_col = cospi_r(th);
     }
 
     // pulled populations of the next leading row (prefetch; two in flight in the prologue)
     R fa_[9], fb_[9];
     auto issue = [&](R(&ft)[9], int yy) {
-        const int gy = wrapc(yy, Ly);
-        if (fresh) {
+        const int gy = wrow(yy);
+        if constexpr (FRESH) {
             ft[0] = reinterpret_cast<const R *>(a.hF)[gy * Lx + gx];
         } else {
             const int gym = gy == 0 ? Ly - 1 : gy - 1, gyp = gy == Ly - 1 ? 0 : gy + 1;
@@ -504,29 +531,24 @@ __device__ __forceinline__ void march_tile(const StepArgs &a, int bx, int by, in
     };
     auto consume = [&](const R(&ft)[9], int yy) {
         const int r = yy - y0 + 2;  // >= 0
-        R h, jx = R(0), jy = R(0), lo = R(0);
-        if (fresh) {
-            h = ft[0];
+        if constexpr (FRESH) {
+            sm.h[r % 5][t] = ft[0];
         } else {
+            R h, jx, jy;
             moments9<LIT>(ft, h, jx, jy);
-            if constexpr (!LIT) lo = moments_lo(ft, h);
+            sm.h[r % 5][t] = h;
+            sm.jx[r & 3][t] = jx;
+            sm.jy[r & 3][t] = jy;
+            if constexpr (!LIT) sm.lo[r & 3][t] = moments_lo(ft, h);
         }
-        sm.h[r % 5][t] = h;
-        sm.jx[r & 3][t] = jx;
-        sm.jy[r & 3][t] = jy;
-        sm.lo[r & 3][t] = lo;
     };
     auto pressure_row = [&](int yy) {
         if (!pcol) return;
         const int r = yy - y0 + 2;  // >= 1
         const R *hm = sm.h[(r + 4) % 5], *hc = sm.h[r % 5], *hp = sm.h[(r + 1) % 5];
-        R kap;
-        if (a.theta_mode == THETA_SCALAR)
-            kap = R(a.kap);
-        else if (a.theta_mode == THETA_FIELD)
-            kap = reinterpret_cast<const R *>(a.kapF)[wrapc(yy, Ly) * Lx + gx];
-        else
-            kap = sm.kapc[t];
+        const R kap = mode == THETA_FIELD
+                          ? reinterpret_cast<const R *>(a.kapF)[wrow(yy) * Lx + gx]
+                          : kap_col;
         // ip = h[i-1,j], jp = h[i,j-1], im = h[i+1,j], jm = h[i,j+1], ...
         sm.p[r & 3][t] = pressure_cell<LIT, R>(hc[t], hc[t - 1], hm[t], hc[t + 1], hp[t],
                                                hm[t - 1], hm[t + 1], hp[t + 1], hp[t - 1], kap,
@@ -557,26 +579,28 @@ __device__ __forceinline__ void march_tile(const StepArgs &a, int bx, int by, in
     const R delta6 = R(6.0 * a.delta), delta3sq = R(3.0 * (a.delta * a.delta)), mu6 = R(6.0 * a.mu);
     const R omeg = R(a.omeg), invtau = R(a.invtau), g = R(a.g);
     const R thr = R(a.hthresh);
+    const bool measure = a.meas_mask || a.mass_corr;
     PartT<R> part;
     part_init(part);
     int any_nan = 0;
 
-    auto row = [&](R(&ft)[9], int j) {
+#pragma unroll 1
+    for (int j = 0; j < rows; ++j) {
         const int y = y0 + j;
-        consume(ft, y + 2);
-        if (j + 1 < rows) issue(ft, y + 3);  // one row ahead
+        consume(fa_, y + 2);
+        if (j + 1 < rows) issue(fa_, y + 3);  // one row ahead
         __syncthreads();
         pressure_row(y + 1);
         __syncthreads();
-        if (!interior) return;
+        if (!interior) continue;
         // ---- output row y, column gx ----
         const int r = y - y0 + 2;
-        const int gy = wrapc(y, Ly);
+        const int gy = wrow(y);
         const int cell = gy * Lx + gx;
         const R *hrow = sm.h[r % 5];
         const R h = hrow[t];
         R ux, uy;
-        if (fresh) {
+        if constexpr (FRESH) {
             ux = reinterpret_cast<const R *>(a.uxF)[cell];
             uy = reinterpret_cast<const R *>(a.uyF)[cell];
         } else {
@@ -595,8 +619,7 @@ __device__ __forceinline__ void march_tile(const StepArgs &a, int bx, int by, in
             sx = (mu6 * h * ux) / den;
             sy = (mu6 * h * uy) / den;
         } else {
-            const R inv = R(1) / ((R(2) * h + delta6) * h + delta3sq);
-            const R c = mu6 * h * inv;
+            const R c = qdiv(mu6 * h, (R(2) * h + delta6) * h + delta3sq);
             sx = c * ux;
             sy = c * uy;
         }
@@ -608,17 +631,21 @@ __device__ __forceinline__ void march_tile(const StepArgs &a, int bx, int by, in
         // collision (src/collide.jl:267-280); ftemp only matters for τ != 1
         R fq[9];
         R hft = h;
-        if (!a.tau_is_one) {
+        if constexpr (!TAU1) {
             const int gym = gy == 0 ? Ly - 1 : gy - 1, gyp = gy == Ly - 1 ? 0 : gy + 1;
             pull9<S>(src, pitch, Lx, gx, gy, gxm, gxp, gym, gyp, fq);
-            if (!LIT) hft = fq[0] + small8(fq);
+            if constexpr (!LIT) hft = fq[0] + small8(fq);
         }
         if constexpr (LIT) {
             R fe[9];
             feq_literal<R>(h, ux, uy, g, fe);
 #pragma unroll
             for (int q = 0; q < 9; ++q) {
-                R v = a.tau_is_one ? fe[q] : omeg * fq[q] + invtau * fe[q];
+                R v;
+                if constexpr (TAU1)
+                    v = fe[q];
+                else
+                    v = omeg * fq[q] + invtau * fe[q];
                 if (q > 0) v = v + source<R>(q, Fx, Fy);
                 S::st(dst, pitch, q, cell, v);
             }
@@ -636,12 +663,16 @@ __device__ __forceinline__ void march_tile(const StepArgs &a, int bx, int by, in
             feq_fast(h, ux, uy, g, fe);
 #pragma unroll
             for (int q = 1; q < 9; ++q) {
-                R v = a.tau_is_one ? fe[q] : omeg * fq[q] + invtau * fe[q];
+                R v;
+                if constexpr (TAU1)
+                    v = fe[q];
+                else
+                    v = omeg * fq[q] + invtau * fe[q];
                 fo[q] = S::rt(q, v + source<R>(q, Fx, Fy));
             }
-            const R hlo = fresh ? R(0) : sm.lo[r & 3][t];
+            const R hlo = FRESH ? R(0) : sm.lo[r & 3][t];
             // Σ_q fpost_q = (1-1/τ) Σ ft + Σ feq/τ = h once h is the pulled mass
-            const R mc = (a.tau_is_one || !fresh) ? h : omeg * hft + invtau * h;
+            const R mc = (TAU1 || !FRESH) ? h : omeg * hft + invtau * h;
             const R ssum = small8(fo);
             R f0 = mc - ssum;
             const R e = (mc - f0) - ssum;
@@ -659,11 +690,9 @@ __device__ __forceinline__ void march_tile(const StepArgs &a, int bx, int by, in
         }
         // measures of the height at the start of this iteration
         if (!isfinite(h)) any_nan = 1;
-        if (a.meas_mask || a.mass_corr) {
+        if (measure) {
             mass_add(part, h);
-            if constexpr (!LIT) {
-                if (!fresh) part.mlo += sm.lo[r & 3][t];
-            }
+            if constexpr (!LIT && !FRESH) part.mlo += sm.lo[r & 3][t];
             const bool wet = h > thr;
             part.wet += wet ? 1 : 0;
             part.hmax = fmax(part.hmax, h);
@@ -674,18 +703,34 @@ __device__ __forceinline__ void march_tile(const StepArgs &a, int bx, int by, in
                 grad9<R>(hrow[t - 1], hm[t], hrow[t + 1], hp[t], hm[t - 1], hm[t + 1], hp[t + 1],
                          hp[t - 1], gx2, gy2);
                 part.area += sqrt(gx2 * gx2 + gy2 * gy2 + R(1));
-                if (a.theta_mode == THETA_FIELD)
+                if (mode == THETA_FIELD)
                     part.cossum += reinterpret_cast<const R *>(a.cosF)[cell];
-                else if (a.theta_mode == THETA_WAVE)
-                    part.cossum += sm.cosc[t];
+                else if (mode == THETA_WAVE)
+                    part.cossum += cos_col;
             }
         }
-    };
-#pragma unroll 1
-    for (int j = 0; j < rows; ++j) row(fa_, j);
+    }
     any_nan = __syncthreads_or(any_nan);
     if (any_nan && t == 0) a.ctl->nan_flag = 1;
-    if (needs_partials(a)) write_partials<NT, R>(a, part, tt, by * a.tiles_x + bx, sm.red);
+    if (measure) write_partials<NT, R>(a, part, tt, by * a.tiles_x + bx, sm.red);
+}
+
+template <class S, int NT>
+__device__ __forceinline__ void march_tile(const StepArgs &a, int bx, int by, int k,
+                                           MarchSmem<S, NT> &sm) {
+    const long long done = a.ctl->step_base + k;  // iterations completed
+    const bool fresh = done + 1 == a.ctl->fresh_step;
+    if (fresh) {
+        if (a.tau_is_one)
+            march_run<S, NT, true, true>(a, bx, by, done, sm);
+        else
+            march_run<S, NT, true, false>(a, bx, by, done, sm);
+    } else {
+        if (a.tau_is_one)
+            march_run<S, NT, false, true>(a, bx, by, done, sm);
+        else
+            march_run<S, NT, false, false>(a, bx, by, done, sm);
+    }
 }
 
 // Single lattice: one CTA per strip, plus (when measures are kept and k > 0)
