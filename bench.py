@@ -51,6 +51,12 @@ def parse():
     ap.add_argument("--precision", default="f32", choices=["f32", "f16", "f64"])
     ap.add_argument("--chunk", type=int, default=CHUNK)
     ap.add_argument("--no-extras", action="store_true", help="skip the 2048² and FP64 side runs")
+    ap.add_argument("--profile-case", choices=["rt512", "film2048"],
+                    help="run a few steps of one case, untimed (for ncu captures)")
+    ap.add_argument("--geometry", default="", help="strip geometry NT,H for --profile-case")
+    ap.add_argument("--case-steps", type=int, default=12)
+    ap.add_argument("--workload", choices=["ensemble", "serving"],
+                    help="print the ensemble (config 4) or serving (config 5) line only")
     return ap.parse_args()
 
 
@@ -315,8 +321,10 @@ def run_ours(args):
     traffic = load_traffic(key)
 
     extras = {}
-    if not args.no_extras:
+    if not args.no_extras and world == 1:
         extras = side_runs(sw, L, np, torch, hbm)
+        extras["ensemble"] = ensemble_run(sw, np)
+        extras["serving"] = serving_run(sw, np)
 
     line = {
         "metric": "MLUPS", "value": value, "unit": "MLUPS", "n_gpus": world,
@@ -397,8 +405,165 @@ def side_runs(sw, L, np, torch, hbm):
     return out
 
 
+def ensemble_run(sw, np, count=512, steps=200, plain_sample=8):
+    """Config 4: `count` two-cap coalescence lattices (128², 256², 512²,
+    1024x256) advanced together in FP32 by the batch kernel, against the
+    plain one-at-a-time paths on a sample of the same instances."""
+    from swalbe_gb300 import configs
+    members, full_steps = configs.ensemble(count)
+    systems = [m.sysc for m in members]
+    cells = sum(s.Lx * s.Ly for s in systems)
+    b = sw.Batch(systems, T=np.float32)
+    for i, m in enumerate(members):
+        b.set_height(i, m.h0)
+    b.step(40)  # includes the autotuning probes
+    b.sync()
+    t0 = time.perf_counter()
+    b.step(steps)
+    b.sync()  # raises if any lattice went non-finite
+    dt = time.perf_counter() - t0
+    batch_mlups = cells * steps / dt / 1e6
+    tile = b.tile()
+    b.close()
+    del b
+    # one at a time: the plain Float64 per-op path and the fused FP32 step
+    rng = np.random.default_rng(0)
+    sample = [members[i] for i in rng.choice(len(members), plain_sample, replace=False)]
+    out = {}
+    for label, dev, T, nst in (("plain_f64_one_at_a_time", "GB300-plain", np.float64, 30),
+                               ("fused_f32_one_at_a_time", "GB300", np.float32, 200)):
+        lu, tt = 0.0, 0.0
+        for m in sample:
+            st = sw.Sys(m.sysc, dev, T=T)
+            st.height = m.h0
+            st.step(5)
+            st.sync()
+            t1 = time.perf_counter()
+            st.step(nst)
+            st.sync()
+            tt += time.perf_counter() - t1
+            lu += m.sysc.Lx * m.sysc.Ly * nst
+            del st
+        out[label] = {"MLUPS": lu / tt / 1e6, "sample": f"{plain_sample} instances x {nst} steps"}
+    return {
+        "instances": count, "cells": cells, "time_steps_per_sim": full_steps,
+        "batch_f32": {"MLUPS": batch_mlups, "sims_per_s": count * steps / (dt * full_steps),
+                      "timed_steps": steps, "strip": {"width": tile[0], "rows": tile[1]}},
+        **out,
+        "speedup_vs_plain": batch_mlups / out["plain_f64_one_at_a_time"]["MLUPS"],
+        "speedup_vs_fused_one_at_a_time": batch_mlups / out["fused_f32_one_at_a_time"]["MLUPS"],
+    }
+
+
+def serving_run(sw, np, duration=12.0, rate=200.0, budget=24 << 30, steps_per_tick=200,
+                queue_limit=64):
+    """Config 5: Poisson arrivals of thin-film solves (sides 64..2048, 1k-100k
+    steps, moving wettability, g in [-1e-3, 0]) into the server for
+    `duration` seconds; offered load far exceeds the GPU, so the queue is
+    bounded and the excess rejected at submission."""
+    from swalbe_gb300 import configs
+    reqs = configs.serving_stream(rate=rate, duration=duration, seed=5)
+    sv = sw.Server(budget, T=np.float32, steps_per_tick=steps_per_tick)
+    sv.set_queue_limit(queue_limit)
+    t0 = time.perf_counter()
+    pending, done, rejected, i = {}, [], 0, 0
+    offered_lu = 0.0
+    while True:
+        now = time.perf_counter() - t0
+        while i < len(reqs) and reqs[i].t_arrival <= now:
+            r = reqs[i]
+            i += 1
+            offered_lu += r.sysc.Lx * r.sysc.Ly * r.nsteps
+            if sv.stats().queued >= queue_limit:
+                rejected += 1
+                continue
+            rid = sv.submit(r.sysc, r.height(), r.nsteps, theta0=r.theta0, dtheta=r.dtheta, v=r.v)
+            if rid is None:
+                rejected += 1
+            else:
+                pending[rid] = r
+        for rid in list(pending):
+            ok, _, info = sv.poll(rid)
+            if ok:
+                done.append(info.t_done - info.t_submit)
+                del pending[rid]
+        if now > duration:
+            break
+        time.sleep(0.002)
+    st = sv.stats()
+    wall = time.perf_counter() - t0
+    lat = sorted(done)
+    pct = (lambda q: lat[min(len(lat) - 1, int(q * len(lat)))] if lat else None)
+    res = {
+        "duration_s": wall, "offered_req_per_s": rate, "arrivals": i,
+        "offered_MLUPS": offered_lu / duration / 1e6,
+        "served_MLUPS": st.lattice_updates / wall / 1e6,
+        "completed": len(done), "admitted": int(st.admitted), "rejected_queue_full": rejected,
+        "resident_at_end": int(st.running), "queued_at_end": int(st.queued),
+        "latency_s": {"p50": pct(0.50), "p99": pct(0.99), "max": lat[-1] if lat else None},
+        "hbm_budget_GB": budget / 1e9, "steps_per_tick": steps_per_tick,
+    }
+    sv.close()
+    return res
+
+
+def run_workload(args):
+    import numpy as np
+
+    import swalbe_gb300 as sw
+    sw.build()
+    if args.workload == "ensemble":
+        r = ensemble_run(sw, np)
+        line = {"metric": "MLUPS", "value": r["batch_f32"]["MLUPS"], "unit": "MLUPS",
+                "workload": "ensemble", **r}
+    else:
+        r = serving_run(sw, np)
+        line = {"metric": "MLUPS", "value": r["served_MLUPS"], "unit": "MLUPS",
+                "workload": "serving", **r}
+    print(json.dumps(line), flush=True)
+
+
+def profile_case(args):
+    """A few launches of one workload, untimed: the committed command that the
+    ncu summaries under profiles/ were captured from."""
+    import numpy as np
+
+    import swalbe_gb300 as sw
+    from swalbe_gb300 import _lib as L
+    from swalbe_gb300 import configs
+    sw.build()
+    T = {"f32": np.float32, "f16": np.float16, "f64": np.float64}[args.precision]
+    if args.profile_case == "rt512":
+        sysc, h0, _ = configs.rayleigh_taylor_512()
+        meas = L.MEAS_MASS | L.MEAS_MAXMIN
+    else:
+        n = 2048
+        sysc = sw.SysConst(n, n, sw.Taumucs())
+        h0 = np.asfortranarray(1.0 + np.random.default_rng(3).uniform(-0.1, 0.1, (n, n)))
+        meas = 0
+    st = sw.Sys(sysc, "GB300", T=T)
+    if meas:
+        st.set_measures(meas)
+    if args.geometry:
+        nt, hh = (int(v) for v in args.geometry.split(","))
+        st.set_geometry(nt, hh)
+    else:
+        st.set_geometry(0, 0)
+    st.height = h0
+    st.step(args.case_steps)
+    st.sync()
+    print(json.dumps({"case": args.profile_case, "precision": args.precision,
+                      "geometry": st.geometry(), "steps": args.case_steps}))
+
+
 def main():
     args = parse()
+    if args.profile_case:
+        profile_case(args)
+        return
+    if args.workload:
+        run_workload(args)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -41,6 +41,7 @@ extern "C" {
 #define SWB_ERR_UNSUPPORTED (-5) /* operation not available in this precision mode */
 #define SWB_ERR_CANCELLED (-6)   /* request cancelled                              */
 #define SWB_ERR_NOT_FOUND (-7)   /* unknown request id                             */
+#define SWB_ERR_BUSY (-8)        /* request queue full                             */
 
 /* ---- precision modes ---- */
 #define SWB_F64 0     /* fused step, Float64 arithmetic in the reference's operation order */
@@ -226,6 +227,8 @@ int swb_batch_set_height(swb_batch *b, int idx, const double *host);
 int swb_batch_get_height(swb_batch *b, int idx, double *host);
 int swb_batch_set_theta_wave(swb_batch *b, int idx, double theta0, double dtheta, double v);
 int swb_batch_step(swb_batch *b, int64_t nsteps);
+/* Waits for the batch; SWB_ERR_NAN (lattice index in swb_last_error) if a
+ * lattice saw a non-finite height. */
 int swb_batch_sync(swb_batch *b);
 /* Tile shape chosen by the autotuner (0 until the first step). */
 int swb_batch_tile(swb_batch *b, int *tile_x, int *tile_y, int *steps_per_graph);
@@ -256,6 +259,10 @@ typedef struct swb_server_stats {
  * steps_per_tick: time steps run per scheduling tick. */
 int swb_server_create(size_t hbm_budget, int precision, int steps_per_tick, swb_server **out);
 int swb_server_destroy(swb_server *sv);
+/* At most `max_queued` requests wait for admission (each holds its initial
+ * film in host memory); further submissions return SWB_ERR_BUSY and count
+ * as rejected.  Default 1024. */
+int swb_server_set_queue_limit(swb_server *sv, int64_t max_queued);
 /* Queues a solve: params (Lx, Ly, γ, θ, g, ...), initial height (copied),
  * moving wettability (dtheta = 0 for none) and the step count. */
 int swb_server_submit(swb_server *sv, const swb_params *p, const double *h0, double theta0,

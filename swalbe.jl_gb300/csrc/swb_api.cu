@@ -554,6 +554,7 @@ const char *swb_status_string(int st) {
         case SWB_ERR_UNSUPPORTED: return "unsupported in this mode";
         case SWB_ERR_CANCELLED: return "cancelled";
         case SWB_ERR_NOT_FOUND: return "not found";
+        case SWB_ERR_BUSY: return "busy";
         default: return "unknown status";
     }
 }

@@ -41,6 +41,11 @@ __global__ void d2f(const double *s, float *d, long long n) {
          i += (long long)gridDim.x * blockDim.x)
         d[i] = (float)s[i];
 }
+__global__ void gather_nan(const StepArgs *args, int count, int *flags) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x)
+        flags[i] = args[i].ctl->nan_flag;
+}
+
 __global__ void set_fresh_k(Control *c) {
     c->fresh_step = c->step_base + 1;
     c->corr[0] = 0.0;
@@ -147,6 +152,7 @@ struct swb_batch {
     double *staging = nullptr;
     StepArgs *d_args = nullptr;
     TileRef *d_tiles = nullptr;
+    int *d_flags = nullptr;
     int ntiles = 0;
     cudaStream_t stream = nullptr;
     cudaGraphExec_t gexec = nullptr;
@@ -168,6 +174,7 @@ struct swb_batch {
         cudaFree(staging);
         cudaFree(d_args);
         cudaFree(d_tiles);
+        cudaFree(d_flags);
         if (stream) cudaStreamDestroy(stream);
     }
 };
@@ -314,6 +321,7 @@ int swb_batch_create(const swb_params *params, int count, int precision, swb_bat
     b->fields_current.assign(count, 1);
     b->ntiles = (int)tiles.size();
     BC_TRY(cudaMalloc((void **)&b->d_args, sizeof(StepArgs) * count));
+    BC_TRY(cudaMalloc((void **)&b->d_flags, sizeof(int) * count));
     BC_TRY(cudaMalloc((void **)&b->d_tiles, sizeof(TileRef) * tiles.size()));
     BC_TRY(cudaMemcpy(b->d_tiles, tiles.data(), sizeof(TileRef) * tiles.size(), cudaMemcpyHostToDevice));
 #undef BC_TRY
@@ -395,6 +403,18 @@ int swb_batch_step(swb_batch *b, int64_t nsteps) {
 int swb_batch_sync(swb_batch *b) {
     if (!b) return swb::bfail(nullptr, SWB_ERR_ARG, "batch is NULL");
     B_TRY(b, cudaStreamSynchronize(b->stream));
+    if (b->args_dirty) return SWB_OK;  // no step since the arguments changed
+    swb::count_launches(1);
+    swb::gather_nan<<<(b->count + 255) / 256, 256, 0, b->stream>>>(b->d_args, b->count, b->d_flags);
+    B_TRY(b, cudaGetLastError());
+    std::vector<int> flags(b->count);
+    B_TRY(b, cudaMemcpyAsync(flags.data(), b->d_flags, sizeof(int) * b->count,
+                             cudaMemcpyDeviceToHost, b->stream));
+    B_TRY(b, cudaStreamSynchronize(b->stream));
+    for (int i = 0; i < b->count; ++i)
+        if (flags[i])
+            return swb::bfail(&b->err, SWB_ERR_NAN,
+                              "non-finite height in lattice " + std::to_string(i));
     return SWB_OK;
 }
 

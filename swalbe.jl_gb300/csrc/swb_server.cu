@@ -56,6 +56,7 @@ struct swb_server {
     size_t budget = 0, in_use = 0;
     int precision = SWB_F32;
     int steps_per_tick = 100;
+    int64_t max_queued = 1024;
     int device = 0;
     std::mutex mu;
     std::condition_variable cv;
@@ -331,6 +332,14 @@ int swb_server_submit(swb_server *sv, const swb_params *p, const double *h0, dou
         p->n <= p->m || p->m < 1 || !(p->hmin > 0))
         return sfail(SWB_ERR_ARG, "invalid params");
     if (p->kbt != 0.0) return sfail(SWB_ERR_UNSUPPORTED, "kbt != 0 is not supported");
+    {
+        std::lock_guard<std::mutex> g(sv->mu);
+        if ((int64_t)sv->queue.size() >= sv->max_queued) {
+            sv->st.submitted++;
+            sv->st.rejected++;
+            return sfail(SWB_ERR_BUSY, "request queue full");
+        }
+    }
     auto r = std::make_unique<Req>();
     r->p = *p;
     r->h0.assign(h0, h0 + (size_t)p->Lx * p->Ly);
@@ -356,6 +365,13 @@ int swb_server_submit(swb_server *sv, const swb_params *p, const double *h0, dou
         sv->reqs[r->id] = std::move(r);
     }
     sv->cv.notify_all();
+    return SWB_OK;
+}
+
+int swb_server_set_queue_limit(swb_server *sv, int64_t max_queued) {
+    if (!sv || max_queued < 1) return sfail(SWB_ERR_ARG, "bad arguments");
+    std::lock_guard<std::mutex> g(sv->mu);
+    sv->max_queued = max_queued;
     return SWB_OK;
 }
 

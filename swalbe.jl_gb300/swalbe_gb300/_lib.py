@@ -22,6 +22,7 @@ SWB_ERR_NAN = -4
 SWB_ERR_UNSUPPORTED = -5
 SWB_ERR_CANCELLED = -6
 SWB_ERR_NOT_FOUND = -7
+SWB_ERR_BUSY = -8
 
 SWB_F64, SWB_F32, SWB_F16, SWB_PLAIN64 = 0, 1, 2, 3
 
@@ -123,6 +124,7 @@ def lib() -> C.CDLL:
             "swb_server_create": (i, [C.c_size_t, i, i, C.POINTER(p)]),
             "swb_server_destroy": (i, [p]),
             "swb_server_submit": (i, [p, PP, p, d, d, d, i64, C.POINTER(i64)]),
+            "swb_server_set_queue_limit": (i, [p, i64]),
             "swb_server_poll": (i, [p, i64, p, C.POINTER(RequestInfo)]),
             "swb_server_cancel": (i, [p, i64]),
             "swb_server_stats_get": (i, [p, C.POINTER(ServerStats)]),

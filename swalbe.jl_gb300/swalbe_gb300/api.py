@@ -530,13 +530,20 @@ class Server:
 
     __del__ = close
 
-    def submit(self, sysc: SysConst, h0, nsteps: int, theta0=None, dtheta=0.0, v=0.0) -> int:
+    def set_queue_limit(self, n: int) -> None:
+        check(lib().swb_server_set_queue_limit(self._h, int(n)))
+
+    def submit(self, sysc: SysConst, h0, nsteps: int, theta0=None, dtheta=0.0, v=0.0):
+        """Request id, or None when the queue is full (counted as rejected)."""
         p = sysc.c_params()
         a = _f64(h0, (sysc.Lx, sysc.Ly))
         th0 = sysc.param.theta if theta0 is None else theta0
         rid = C.c_int64()
-        check(lib().swb_server_submit(self._h, C.byref(p), a.ctypes.data, float(th0), float(dtheta),
-                                      float(v), int(nsteps), C.byref(rid)))
+        st = lib().swb_server_submit(self._h, C.byref(p), a.ctypes.data, float(th0), float(dtheta),
+                                     float(v), int(nsteps), C.byref(rid))
+        if st == L.SWB_ERR_BUSY:
+            return None
+        check(st)
         return rid.value
 
     def poll(self, rid: int, shape=None):

@@ -15,6 +15,9 @@ import numpy as np
 
 from .api import SysConst, Taumucs, cospi, singledroplet, two_caps
 
+# Tallest cap of the ensemble instances (lattice units).
+CAP_HMAX = 20.0
+
 
 def droplet_relax_256():
     """Config 1: 256², Float64, τ=1, γ=0.01, δ=1, θ=1/9, n=9, m=3, hmin=0.1,
@@ -53,8 +56,10 @@ class EnsembleMember:
 
 def ensemble(count: int = 512, seed: int = 4, steps: int = 20000) -> Tuple[List[EnsembleMember], int]:
     """Config 4: `count` coalescence instances; sizes from {128², 256², 512²,
-    1024x256}; two caps of radii U[0.15, 0.40]·Ly separated by an edge gap of
-    U{2..10} cells; θ ~ U[1/18, 1/4] for the caps and the substrate; FP32."""
+    1024x256}; two caps of sphere radii U[0.15, 0.40]·Ly (scaled down where
+    both would not fit side by side, or where the taller cap would exceed
+    CAP_HMAX) separated by an edge gap of U{2..10} cells; θ ~ U[1/18, 1/4]
+    for the caps and the substrate; FP32."""
     rng = np.random.default_rng(seed)
     sizes = [(128, 128), (256, 256), (512, 512), (1024, 256)]
     out = []
@@ -63,12 +68,34 @@ def ensemble(count: int = 512, seed: int = 4, steps: int = 20000) -> Tuple[List[
         th = float(rng.uniform(1 / 18, 1 / 4))
         r1, r2 = rng.uniform(0.15, 0.40, 2) * Ly
         gap = int(rng.integers(2, 11))
-        # contact radii of the caps: R sin(πθ); centre them along x
-        a1, a2 = r1 * math.sin(math.pi * th), r2 * math.sin(math.pi * th)
-        cx = Lx / 2
-        c1 = (cx - gap / 2 - a1, Ly / 2)
-        c2 = (cx + gap / 2 + a2, Ly / 2)
-        h0 = two_caps(Lx, Ly, r1, r2, th, th, c1, c2)
+        # contact radii of the caps: R sin(πθ); centre them along x.  On
+        # square lattices two caps of sphere radius 0.4·Ly at 45° are wider
+        # than the lattice and would overlap across the periodic boundary
+        # (the reference algorithm diverges on that input), so both radii are
+        # scaled down until the two contact circles and the gap fit with an
+        # 8-cell margin.
+        sn = math.sin(math.pi * th)
+        fit = (Lx - gap - 8) / (2 * (r1 + r2) * sn)
+        if fit < 1:
+            r1, r2 = r1 * fit, r2 * fit
+        # Film heights above ~30 lattice units are linearly unstable under
+        # the reference scheme at γ = 0.01: capillary waves grow and Float64
+        # diverges within a few hundred steps (a flat film of height 35 does
+        # by step 2000, a 512² pair of caps 52 high by step 500).  Caps of
+        # sphere radius 0.4·Ly at θ = π/4 would reach ~60, so the radii are
+        # scaled down until the taller cap is at most CAP_HMAX high, the cap
+        # height of the 256² droplet case.
+        tall = max(r1, r2) * (1 - math.cos(math.pi * th))
+        if tall > CAP_HMAX:
+            r1, r2 = r1 * CAP_HMAX / tall, r2 * CAP_HMAX / tall
+        a1, a2 = r1 * sn, r2 * sn
+        left = (Lx - (2 * a1 + gap + 2 * a2)) / 2  # the pair is centred in x
+        c1 = (left + a1, Ly / 2)
+        c2 = (left + 2 * a1 + gap + a2, Ly / 2)
+        # the precursor floor max(0.05, ·) as in config 1: combining caps with
+        # the reference's rule (clamp only negatives) leaves rim cells of
+        # ~1e-6 height, where u = j/h diverges within a few steps
+        h0 = np.asfortranarray(np.maximum(two_caps(Lx, Ly, r1, r2, th, th, c1, c2), 0.05))
         out.append(EnsembleMember(SysConst(Lx, Ly, Taumucs(Tmax=steps, theta=th)), h0))
     return out, steps
 

@@ -75,3 +75,26 @@ def test_sliding_droplet(orc, golden):
     ix, iy = np.unravel_index(np.argmax(r.height), r.height.shape)
     assert ix + 1 != 75 and iy + 1 == 75
     assert np.all(r.velx < 0.1) and np.all(r.vely < 0.1)
+
+
+@pytest.mark.parametrize("H,stable", [(20.0, True), (40.0, False)])
+def test_tall_flat_film_stability_limit(orc, H, stable):
+    """The scheme's capillary waves are stable on a flat film of height 20 at
+    γ = 0.01 and grow without bound at height 40 (Float64, the reference
+    algorithm).  The batched-ensemble generator caps its droplets below this
+    limit."""
+    rng = np.random.default_rng(1)
+    h0 = H * (1 + 1e-3 * rng.uniform(-1, 1, (48, 48)))
+    r = orc.FusedState(orc.params(48, 48, theta=1 / 4), h0).run(1000)
+    finite = bool(np.isfinite(r.height).all())
+    if stable:
+        assert finite and r.height.max() - r.height.min() < 2 * H * 1e-3
+    else:
+        assert not finite or r.height.max() - r.height.min() > 1.0
+
+
+def test_ensemble_caps_below_stability_limit():
+    from swalbe_gb300 import configs
+    members, _ = configs.ensemble(512)
+    assert max(float(m.h0.max()) for m in members) <= configs.CAP_HMAX + 1e-9
+    assert min(float(m.h0.min()) for m in members) >= 0.05
