@@ -155,8 +155,10 @@ int swb_set_theta_wave(swb_state *s, double theta0, double dtheta, double v);
 int swb_set_inclination(swb_state *s, double ax, double ay, int loop_time, int64_t t,
                         int64_t tstart, int64_t tsmooth);
 
-/* Strip geometry of the fused step: CTAs of nt threads (64, 128, 256) own
- * strips of nt-4 columns and h rows (4..512).  By default SWB_F64 / SWB_F32
+/* Geometry of the fused step: CTAs of nt threads (64, 128, 256) own strips
+ * of nt-4 columns and h rows (4..512) that they march row by row; or, with
+ * nt = 32 (SWB_F32 / SWB_F16 only; h is ignored), CTAs of 256 threads own
+ * 2D tiles of 32 x 16 cells whose loads are all issued at once.  By default SWB_F64 / SWB_F32
  * states autotune it on their first swb_step of >= 256 steps (timing a few
  * geometries on those real steps; remembered per lattice size), and SWB_F16
  * states use a size rule.  Setting it (or (0, 0): the size rule) turns the
@@ -164,6 +166,24 @@ int swb_set_inclination(swb_state *s, double ax, double ay, int loop_time, int64
  * the FP64 mass sum that drives the SWB_F16 mass correction. */
 int swb_set_geometry(swb_state *s, int nt, int h);
 int swb_get_geometry(swb_state *s, int *nt, int *h);
+
+/* Launch form of swb_step (no counterpart in the reference, whose time loop
+ * runs each op as its own broadcast, src/simulate.jl:15-22).
+ *   SWB_STEP_PER_ITERATION  one kernel per iteration, replayed from CUDA
+ *                           graphs of 64 iterations;
+ *   SWB_STEP_MULTI          SWB_F32 / SWB_F16 only: one cooperative launch
+ *                           runs up to 1024 iterations, CTAs meeting at a
+ *                           grid barrier between iterations (strip width 64
+ *                           or 128);
+ *   SWB_STEP_AUTO           (default) the autotuner times both forms with
+ *                           the geometry; without it, PER_ITERATION.
+ * Both forms give identical results for the same geometry.
+ * swb_get_step_mode reports the form in effect (PER_ITERATION or MULTI). */
+#define SWB_STEP_AUTO 0
+#define SWB_STEP_PER_ITERATION 1
+#define SWB_STEP_MULTI 2
+int swb_set_step_mode(swb_state *s, int mode);
+int swb_get_step_mode(swb_state *s, int *mode);
 
 /* SWB_F32 / SWB_F16: hold the total mass at its value when the fields were
  * last set, by an FP64-measured correction spread over the cells (default:

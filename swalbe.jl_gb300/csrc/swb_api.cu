@@ -203,9 +203,14 @@ int batch_blocks_per_sm(int precision, int nt) {
 
 // Default strip geometry by lattice size (from sweeps on GB300): narrow
 // strips (64 threads) and as many rows per strip as still leave ~1000 CTAs;
-// FP16 small lattices prefer 128-thread strips.
+// FP16 small lattices prefer 128-thread strips.  (*nt == kTileGeom keeps
+// the 2D tiles.)
 void default_geometry(int Lx, int Ly, int precision, int *nt, int *h) {
     int n = *nt;
+    if (n == kTileGeom) {
+        *h = kTileY;
+        return;
+    }
     if (!n) n = (precision == SWB_F16 && (long long)Lx * Ly <= 512LL * 512) ? 128 : 64;
     const long long strips = (Lx + n - 5) / (n - 4);
     const long long want = precision == SWB_F64 ? 600 : 1000;
@@ -253,6 +258,11 @@ struct swb_state {
     // strip geometry: autotuned on the first long run unless set explicitly
     bool tuned = false;
     bool autotune = true;
+    // launch form: SWB_STEP_AUTO (tuner / size rule) or a fixed one; persist
+    // is the form in effect (multi-step cooperative kernel vs one launch per
+    // iteration replayed from CUDA graphs)
+    int mode = SWB_STEP_AUTO;
+    bool persist = false;
     // graph cache
     cudaGraphExec_t gexec = nullptr;
     int gsteps = 0;
@@ -357,12 +367,21 @@ int set_fresh(swb_state *s) {
 }
 
 int check_nan(swb_state *s) {
-    int flag = 0;
     if (s->plain()) return SWB_OK;
-    CUDA_TRY(&s->err, cudaMemcpyAsync(&flag, &s->a.ctl->nan_flag, sizeof(int),
-                                      cudaMemcpyDeviceToHost, s->stream));
+    Control c{};
+    CUDA_TRY(&s->err, cudaMemcpyAsync(&c, s->a.ctl, sizeof(Control), cudaMemcpyDeviceToHost,
+                                      s->stream));
     CUDA_TRY(&s->err, cudaStreamSynchronize(s->stream));
-    if (flag) return fail(&s->err, SWB_ERR_NAN, "non-finite height detected during a step");
+    if (c.bar_err) {
+        // a grid-barrier wait gave up: the iterations of that launch are not
+        // valid.  Re-arm the barrier so that the state can be re-initialised.
+        CUDA_TRY(&s->err, cudaMemsetAsync(s->a.bar, 0, swb::kBarWords * sizeof(unsigned int),
+                                          s->stream));
+        CUDA_TRY(&s->err, cudaMemsetAsync(&s->a.ctl->bar_err, 0, sizeof(int), s->stream));
+        CUDA_TRY(&s->err, cudaStreamSynchronize(s->stream));
+        return fail(&s->err, SWB_ERR_CUDA, "multi-step kernel: grid barrier wait timed out");
+    }
+    if (c.nan_flag) return fail(&s->err, SWB_ERR_NAN, "non-finite height detected during a step");
     return SWB_OK;
 }
 
@@ -400,17 +419,61 @@ constexpr int kGraphSteps = 64;
 
 // Geometries chosen by the autotuner, per (Lx, Ly, precision), process-wide.
 std::mutex g_tune_mu;
-std::vector<std::array<int, 5>> g_tuned;  // Lx, Ly, precision, nt, h
+std::vector<std::array<int, 7>> g_tuned;  // Lx, Ly, precision, mode, nt, h, persist
 
-bool tuned_lookup(int Lx, int Ly, int prec, int *nt, int *h) {
+bool tuned_lookup(int Lx, int Ly, int prec, int mode, int *nt, int *h, bool *persist) {
     std::lock_guard<std::mutex> g(g_tune_mu);
     for (auto &e : g_tuned)
-        if (e[0] == Lx && e[1] == Ly && e[2] == prec) {
-            *nt = e[3];
-            *h = e[4];
+        if (e[0] == Lx && e[1] == Ly && e[2] == prec && e[3] == mode) {
+            *nt = e[4];
+            *h = e[5];
+            *persist = e[6] != 0;
             return true;
         }
     return false;
+}
+
+// Iterations per launch of the multi-step kernel (keeps launches short).
+constexpr int kRunChunk = 1024;
+
+// CTAs of the multi-step kernel for the state's geometry: one per strip plus
+// the reducer, capped at what the GPU holds at once (0: not possible).
+int run_grid(swb_state *s) {
+    const int per_sm = swb::fused_run_blocks_per_sm(s->precision, s->a.march_nt);
+    if (per_sm <= 0) return 0;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long want =
+        (long long)s->a.tiles_x * s->a.tiles_y + (swb::needs_partials(s->a) ? 1 : 0);
+    const long long cap = (long long)per_sm * sms;
+    return (int)(want < cap ? want : cap);
+}
+
+bool run_possible(const swb_state *s) {
+    return (s->precision == SWB_F32 || s->precision == SWB_F16) &&
+           (s->a.march_nt == 64 || s->a.march_nt == 128 || s->a.march_nt == swb::kTileGeom);
+}
+
+// n iterations as multi-step launches of at most kRunChunk iterations.
+cudaError_t run_sequence(swb_state *s, long long n) {
+    const int grid = run_grid(s);
+    if (grid <= 0) return cudaErrorInvalidConfiguration;
+    while (n > 0) {
+        const int c = (int)(n < kRunChunk ? n : kRunChunk);
+        cudaError_t e = swb::launch_fused_run(s->precision, s->a, c, grid, s->stream);
+        if (e != cudaSuccess) return e;
+        swb::count_launches(1);
+        n -= c;
+    }
+    return cudaSuccess;
+}
+
+// Launch form without the tuner: one launch per iteration unless the
+// multi-step kernel was asked for (on GB300 it measured 5-25 % slower than
+// graph-replayed launches at 512^2..2048^2; the tuner times both).
+bool persist_default(const swb_state *s) {
+    return s->mode == SWB_STEP_MULTI && run_possible(s);
 }
 
 // n step launches (k = 0..n-1) and the advance kernel that closes them.
@@ -430,32 +493,49 @@ constexpr int kTuneProbe = 8;
 
 int autotune_geometry(swb_state *s, long long &left) {
     int nt = 0, h = 0;
-    if (tuned_lookup(s->p.Lx, s->p.Ly, s->precision, &nt, &h)) {
+    bool pers = false;
+    if (tuned_lookup(s->p.Lx, s->p.Ly, s->precision, s->mode, &nt, &h, &pers)) {
         swb::set_geometry(s->a, nt, h);
+        s->persist = pers;
         s->invalidate_graph();
         s->tuned = true;
         return SWB_OK;
     }
-    const int cands[][2] = {{64, 4}, {64, 8}, {64, 16}, {64, 32}, {128, 4}, {128, 16}, {256, 16}};
+    // {nt, h, multi-step}
+    const int K = swb::kTileGeom;
+    const int all[][3] = {{64, 4, 0},  {64, 8, 0},  {64, 16, 0}, {64, 32, 0}, {128, 4, 0},
+                          {128, 16, 0}, {256, 16, 0}, {K, 16, 0},  {64, 8, 1},  {64, 16, 1},
+                          {128, 8, 1},  {K, 16, 1}};
+    std::vector<std::array<int, 3>> cands;
+    const bool multi_ok = s->precision == SWB_F32 || s->precision == SWB_F16;
+    for (auto &c : all) {
+        if (c[0] == K && !multi_ok) continue;
+        if (c[2] && (!multi_ok || s->mode == SWB_STEP_PER_ITERATION)) continue;
+        if (!c[2] && s->mode == SWB_STEP_MULTI) continue;
+        cands.push_back({c[0], c[1], c[2]});
+    }
     cudaEvent_t e0, e1;
     CUDA_TRY(&s->err, cudaEventCreate(&e0));
     CUDA_TRY(&s->err, cudaEventCreate(&e1));
     float best = 1e30f;
     int bnt = s->a.march_nt, bh = s->a.march_h;
+    bool bpers = s->persist;
     int rc = SWB_OK;
     bool first = true;
     for (auto &c : cands) {
         if (c[1] > s->p.Ly && c[1] != swb::kMinRows) continue;
         swb::set_geometry(s->a, c[0], c[1]);
+        s->persist = c[2] != 0;
+        if (s->persist && run_grid(s) <= 0) continue;
         if (first) {  // warm-up with the first candidate
-            cudaError_t e = launch_sequence(s, kTuneProbe);
+            cudaError_t e = s->persist ? run_sequence(s, kTuneProbe) : launch_sequence(s, kTuneProbe);
             if (e != cudaSuccess) { rc = fail(&s->err, SWB_ERR_CUDA, cudaGetErrorString(e)); break; }
             left -= kTuneProbe;
             s->steps += kTuneProbe;
             first = false;
         }
         cudaEventRecord(e0, s->stream);
-        cudaError_t e = launch_sequence(s, kTuneProbe);
+        cudaError_t e = s->persist ? run_sequence(s, kTuneProbe) : launch_sequence(s, kTuneProbe);
         cudaEventRecord(e1, s->stream);
         if (e == cudaSuccess) e = cudaEventSynchronize(e1);
         if (e != cudaSuccess) { rc = fail(&s->err, SWB_ERR_CUDA, cudaGetErrorString(e)); break; }
@@ -467,16 +547,18 @@ int autotune_geometry(swb_state *s, long long &left) {
             best = ms;
             bnt = c[0];
             bh = c[1];
+            bpers = s->persist;
         }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     swb::set_geometry(s->a, bnt, bh);
+    s->persist = bpers;
     s->invalidate_graph();
     s->tuned = true;
     if (rc == SWB_OK) {
         std::lock_guard<std::mutex> g(g_tune_mu);
-        g_tuned.push_back({s->p.Lx, s->p.Ly, s->precision, bnt, bh});
+        g_tuned.push_back({s->p.Lx, s->p.Ly, s->precision, s->mode, bnt, bh, bpers ? 1 : 0});
     }
     return rc;
 }
@@ -488,6 +570,10 @@ int fused_steps(swb_state *s, long long nsteps) {
         (s->precision == SWB_F64 || s->precision == SWB_F32)) {
         int rc = autotune_geometry(s, left);
         if (rc) return rc;
+    }
+    if (s->persist) {
+        if (left > 0) CUDA_TRY(&s->err, run_sequence(s, left));
+        left = 0;
     }
     if (left >= kGraphSteps) {
         if (!s->gvalid) {
@@ -570,7 +656,8 @@ int swb_state_bytes(const swb_params *p, int precision, size_t *bytes) {
         b = align256((size_t)27 * N * 8) + 11 * align256((size_t)N * 8);
     } else if (precision == SWB_F64 || precision == SWB_F32 || precision == SWB_F16) {
         b = 2 * align256(fbuf_bytes(precision, pitch)) + 3 * align256((size_t)N * real_bytes(precision)) +
-            align256((size_t)2 * tiles * swb::kNPart * 8) + align256(sizeof(Control));
+            align256((size_t)2 * tiles * swb::kNPart * 8) + align256(sizeof(Control)) +
+            align256(swb::kBarWords * sizeof(unsigned int));
     } else {
         return fail(nullptr, SWB_ERR_ARG, "unknown precision");
     }
@@ -652,6 +739,8 @@ int swb_create(const swb_params *p, int precision, swb_state **out) {
         a.part_stride = (int)swb::max_tiles(p->Lx, p->Ly);
         CREATE_TRY(s->alloc((void **)&a.partials, (size_t)2 * a.part_stride * swb::kNPart * 8));
         CREATE_TRY(s->alloc((void **)&a.ctl, sizeof(Control)));
+        CREATE_TRY(s->alloc((void **)&a.bar, swb::kBarWords * sizeof(unsigned int)));
+        CREATE_TRY(cudaMemsetAsync(a.bar, 0, swb::kBarWords * sizeof(unsigned int), s->stream));
         Control c0{};
         c0.fresh_step = 1;
         CREATE_TRY(cudaMemcpyAsync(a.ctl, &c0, sizeof(Control), cudaMemcpyHostToDevice, s->stream));
@@ -663,6 +752,7 @@ int swb_create(const swb_params *p, int precision, swb_state **out) {
     CREATE_TRY(cudaMemsetAsync(s->mticket, 0, sizeof(unsigned int), s->stream));
     s->a.records = s->rec;
     s->a.rec_cap = swb::kRecCap;
+    s->persist = persist_default(s);
     CREATE_TRY(cudaStreamSynchronize(s->stream));
 #undef CREATE_TRY
     *out = s;
@@ -870,9 +960,16 @@ int swb_set_geometry(swb_state *s, int nt, int h) {
     if (s->plain()) return SWB_OK;
     if (nt == 0 && h == 0) {
         swb::default_geometry(s->p.Lx, s->p.Ly, s->precision, &nt, &h);  // nt == 0: choose
+    } else if (nt == swb::kTileGeom) {
+        if (s->precision == SWB_F64)
+            return fail(&s->err, SWB_ERR_UNSUPPORTED, "2D tiles: FP32 and FP16 storage only");
+        h = swb::kTileY;
     } else if ((nt != 64 && nt != 128 && nt != 256) || h < swb::kMinRows || h > swb::kMaxRows) {
-        return fail(&s->err, SWB_ERR_ARG, "geometry: nt must be 64, 128 or 256 and 4 <= h <= 512");
+        return fail(&s->err, SWB_ERR_ARG,
+                    "geometry: nt must be 64, 128 or 256 and 4 <= h <= 512, or nt = 32 (2D tiles)");
     }
+    if (s->mode == SWB_STEP_MULTI && nt == 256)
+        return fail(&s->err, SWB_ERR_UNSUPPORTED, "multi-step kernel: nt must be 64 or 128");
     s->autotune = false;  // an explicit geometry (or the default) is kept
     s->tuned = true;
     if (s->a.march_nt != nt || s->a.march_h != h) {
@@ -880,6 +977,36 @@ int swb_set_geometry(swb_state *s, int nt, int h) {
         swb::set_geometry(s->a, nt, h);
         s->invalidate_graph();
     }
+    s->persist = persist_default(s);
+    return SWB_OK;
+}
+
+int swb_set_step_mode(swb_state *s, int mode) {
+    if (!s) return fail(nullptr, SWB_ERR_ARG, "state is NULL");
+    if (mode != SWB_STEP_AUTO && mode != SWB_STEP_PER_ITERATION && mode != SWB_STEP_MULTI)
+        return fail(&s->err, SWB_ERR_ARG, "unknown step mode");
+    if (s->plain())
+        return mode == SWB_STEP_MULTI
+                   ? fail(&s->err, SWB_ERR_UNSUPPORTED, "plain path: one kernel per op")
+                   : SWB_OK;
+    if (mode == SWB_STEP_MULTI && s->precision != SWB_F32 && s->precision != SWB_F16)
+        return fail(&s->err, SWB_ERR_UNSUPPORTED, "multi-step kernel: FP32 and FP16 storage only");
+    CUDA_TRY(&s->err, cudaStreamSynchronize(s->stream));
+    s->mode = mode;
+    if (mode == SWB_STEP_MULTI && s->a.march_nt == 256) {
+        int nt = 128, h = 0;
+        swb::default_geometry(s->p.Lx, s->p.Ly, s->precision, &nt, &h);
+        swb::set_geometry(s->a, nt, h);
+    }
+    if (s->autotune) s->tuned = false;  // re-tune within the new form
+    s->persist = persist_default(s);
+    s->invalidate_graph();
+    return SWB_OK;
+}
+
+int swb_get_step_mode(swb_state *s, int *mode) {
+    if (!s || !mode) return fail(s ? &s->err : nullptr, SWB_ERR_ARG, "NULL argument");
+    *mode = (!s->plain() && s->persist) ? SWB_STEP_MULTI : SWB_STEP_PER_ITERATION;
     return SWB_OK;
 }
 

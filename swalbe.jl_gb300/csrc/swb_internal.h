@@ -13,8 +13,10 @@ namespace swb {
 // are sized for the finest decomposition (NT = 64, H = kMinRows).
 constexpr int kMinRows = 4;
 constexpr int kMaxRows = 512;
-inline long long max_tiles(int Lx, int Ly) {  // per parity slot
-    return (long long)((Lx + 59) / 60) * ((Ly + kMinRows - 1) / kMinRows);
+inline long long max_tiles(int Lx, int Ly) {  // per parity slot: strips or 2D tiles
+    const long long strips = (long long)((Lx + 59) / 60) * ((Ly + kMinRows - 1) / kMinRows);
+    const long long tiles = (long long)((Lx + 31) / 32) * ((Ly + 15) / 16);
+    return strips > tiles ? strips : tiles;
 }
 // CTA width of batched and served lattices (all share one launch).
 constexpr int kBatchNT = 128;
@@ -41,6 +43,8 @@ struct Control {
     double mass_target;      // FP16 mass correction: mass to hold
     double corr[2];          // correction per cell for iteration t in slot t & 1
     long long rec_head;      // records written (monotone)
+    int bar_err;             // a grid-barrier wait of the multi-step kernel gave up
+    int pad1;
 };
 
 struct Record {              // one time_loop iteration
@@ -80,15 +84,29 @@ struct StepArgs {
     Control *ctl;
     int part_stride;          // partial slots per parity (max_tiles of the lattice)
     int tiles_x, tiles_y;     // strip grid of this lattice: ceil(Lx/(NT-4)) x ceil(Ly/H)
-    int march_nt, march_h;    // threads per CTA (strip width + 4) and rows per strip
+    int march_nt, march_h;    // threads per CTA (strip width + 4) and rows per strip,
+                              // or kTileGeom and kT2Y rows: 2D tiles of 32 x 16 cells
+    unsigned int *bar;        // grid-barrier words of the multi-step kernel (kBarWords)
 };
+
+// Geometry value of the 2D-tile form: CTAs of 256 threads own 32 x 16 cells.
+constexpr int kTileGeom = 32;
+constexpr int kTileX = 32, kTileY = 16, kTileThreads = 256;
 
 inline void set_geometry(StepArgs &a, int nt, int h) {
     a.march_nt = nt;
+    if (nt == kTileGeom) {
+        a.march_h = kTileY;
+        a.tiles_x = (a.Lx + kTileX - 1) / kTileX;
+        a.tiles_y = (a.Ly + kTileY - 1) / kTileY;
+        return;
+    }
     a.march_h = h;
     a.tiles_x = (a.Lx + nt - 5) / (nt - 4);
     a.tiles_y = (a.Ly + h - 1) / h;
 }
+// Threads per CTA of a geometry.
+inline int geometry_threads(int nt) { return nt == kTileGeom ? kTileThreads : nt; }
 
 // Entry in the packed tile table of a batch (tx = -1: the lattice's reducer).
 struct TileRef {
@@ -115,6 +133,18 @@ cudaError_t launch_batch_advance(const StepArgs *d_args, int count, int n, cudaS
 inline int step_grid(const StepArgs &a, int k) {
     return a.tiles_x * a.tiles_y + ((needs_partials(a) && k > 0) ? 1 : 0);
 }
+// Multi-step kernel: n iterations of a single F32/F16 lattice in one
+// cooperative launch of `grid` CTAs (all co-resident), a grid barrier
+// between iterations; closes the sequence itself (no advance kernel).
+cudaError_t launch_fused_run(int precision, const StepArgs &a, int n, int grid, cudaStream_t st);
+// CTAs of width nt one SM holds for the multi-step kernel (0: unsupported).
+int fused_run_blocks_per_sm(int precision, int nt);
+// Grid barrier of the multi-step kernel: a top counter, kBarGroups group
+// counters and kBarGroups generation words, each on its own 128-byte line.
+constexpr unsigned long long kBarrierTimeoutNs = 2000000000ULL;  // one wait
+constexpr unsigned int kBarGroups = 32;
+constexpr unsigned int kBarStride = 32;  // words
+constexpr unsigned int kBarWords = kBarStride * (1 + 2 * kBarGroups);
 cudaError_t launch_moments(int precision, const StepArgs &a, cudaStream_t st);
 cudaError_t launch_fout(int precision, const StepArgs &a, double *out, cudaStream_t st);
 cudaError_t launch_pressure_now(int precision, const StepArgs &a, double *out, cudaStream_t st);

@@ -42,7 +42,11 @@ int grid_for(long long n, int threads) {
 
 cudaError_t launch_fused_step_f32(int precision, const StepArgs &a, int k, cudaStream_t st) {
     const int grid = step_grid(a, k);
-    DISPATCH_STORE(precision, DISPATCH_NT(a.march_nt, (fused_step_kernel<S, NT><<<grid, NT, 0, st>>>(a, k))));
+    if (a.march_nt == kTileGeom) {
+        DISPATCH_STORE(precision, (fused_tile_kernel<S><<<grid, kT2NT, 0, st>>>(a, k)));
+    } else {
+        DISPATCH_STORE(precision, DISPATCH_NT(a.march_nt, (fused_step_kernel<S, NT><<<grid, NT, 0, st>>>(a, k))));
+    }
     return cudaGetLastError();
 }
 

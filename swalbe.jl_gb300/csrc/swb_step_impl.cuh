@@ -25,17 +25,33 @@
 #pragma once
 #include <cuda_fp16.h>
 
+#include <type_traits>
+
 #include "swb_internal.h"
 
 namespace swb {
 
 // ------------------------------------------------------------ storage
-struct StoreF64 {
+// Load policies.  LdNC reads through the non-coherent path (__ldg), valid
+// while the populations are read-only for the whole launch: kernels that do
+// one time step.  LdCG reads at L2 (__ldcg), which other CTAs' writes reach
+// before a grid barrier releases: kernels that do several time steps.
+struct LdNC {
+    template <class T>
+    __device__ __forceinline__ static T ld(const T *p) { return __ldg(p); }
+};
+struct LdCG {
+    template <class T>
+    __device__ __forceinline__ static T ld(const T *p) { return __ldcg(p); }
+};
+
+template <class L>
+struct StoreF64T {
     using real = double;
     static constexpr bool kLiteral = true;
     static constexpr bool kHalf = false;
     __device__ __forceinline__ static double ld(const void *b, long long pitch, int q, int i) {
-        return __ldg(reinterpret_cast<const double *>(b) + q * pitch + i);
+        return L::ld(reinterpret_cast<const double *>(b) + q * pitch + i);
     }
     __device__ __forceinline__ static void st(void *b, long long pitch, int q, int i, double v) {
         reinterpret_cast<double *>(b)[q * pitch + i] = v;
@@ -43,12 +59,13 @@ struct StoreF64 {
     __device__ __forceinline__ static double rt(int, double v) { return v; }
 };
 
-struct StoreF32 {
+template <class L>
+struct StoreF32T {
     using real = float;
     static constexpr bool kLiteral = false;
     static constexpr bool kHalf = false;
     __device__ __forceinline__ static float ld(const void *b, long long pitch, int q, int i) {
-        return __ldg(reinterpret_cast<const float *>(b) + q * pitch + i);
+        return L::ld(reinterpret_cast<const float *>(b) + q * pitch + i);
     }
     __device__ __forceinline__ static void st(void *b, long long pitch, int q, int i, float v) {
         reinterpret_cast<float *>(b)[q * pitch + i] = v;
@@ -58,7 +75,8 @@ struct StoreF32 {
 
 // f0 as an FP32 plane, f1..f8 as FP16 planes holding 2^10 f_q (the scale
 // keeps populations of order 1e-5..1e-2 in the normal FP16 range).
-struct StoreF16 {
+template <class L>
+struct StoreF16T {
     using real = float;
     static constexpr bool kLiteral = false;
     static constexpr bool kHalf = true;
@@ -68,8 +86,8 @@ struct StoreF16 {
         return reinterpret_cast<const __half *>(reinterpret_cast<const float *>(b) + pitch);
     }
     __device__ __forceinline__ static float ld(const void *b, long long pitch, int q, int i) {
-        if (q == 0) return __ldg(reinterpret_cast<const float *>(b) + i);
-        return __half2float(__ldg(hp(b, pitch) + (q - 1) * pitch + i)) * kInv;
+        if (q == 0) return L::ld(reinterpret_cast<const float *>(b) + i);
+        return __half2float(L::ld(hp(b, pitch) + (q - 1) * pitch + i)) * kInv;
     }
     __device__ __forceinline__ static void st(void *b, long long pitch, int q, int i, float v) {
         if (q == 0) {
@@ -83,6 +101,10 @@ struct StoreF16 {
         return q == 0 ? v : __half2float(__float2half_rn(v * kScale)) * kInv;
     }
 };
+
+using StoreF64 = StoreF64T<LdNC>;
+using StoreF32 = StoreF32T<LdNC>;
+using StoreF16 = StoreF16T<LdNC>;
 
 // ------------------------------------------------------------ helpers
 __device__ __forceinline__ int wrapc(int x, int L) {
@@ -462,14 +484,139 @@ __device__ void reduce_step(const StepArgs &a, long long s, PartT<double> *redd)
             r.hmin = acc.hmin;
             r.area = acc.area;
             r.cos_sum = a.theta_mode == THETA_SCALAR ? (double)acc.wet * a.cos_theta : acc.cossum;
-            c->rec_head = c->rec_head + 1;
+            c->rec_head = __ldcg(&c->rec_head) + 1;
         }
         if (a.mass_corr) {
-            if (s == c->fresh_step) c->mass_target = mass;
+            if (s == __ldcg(&c->fresh_step)) c->mass_target = mass;
             const double N = (double)a.Lx * (double)a.Ly;
-            const double in_flight = c->corr[s & 1] + c->corr[(s + 1) & 1];
-            c->corr[s & 1] = (c->mass_target - mass - N * in_flight) / N;
+            const double in_flight = __ldcg(&c->corr[s & 1]) + __ldcg(&c->corr[(s + 1) & 1]);
+            c->corr[s & 1] = (__ldcg(&c->mass_target) - mass - N * in_flight) / N;
         }
+    }
+}
+
+// Per-tile constants of the force and collision stage.
+template <class R>
+struct CellConst {
+    R delta6, delta3sq, mu6, omeg, invtau, g, incl_fac;
+    double corr;  // FP16 mass correction per cell of this iteration
+};
+
+template <class R>
+__device__ __forceinline__ CellConst<R> cell_consts(const StepArgs &a, long long tt, double corr) {
+    CellConst<R> c;
+    c.incl_fac = R(0);
+    if (a.incl) {
+        c.incl_fac = a.incl_loop_time
+                         ? R(0.5) + R(0.5) * tanh_r(R(tt - a.incl_tstart) / R(a.incl_tsmooth))
+                         : R(a.incl_fixed);
+    }
+    c.delta6 = R(6.0 * a.delta);
+    c.delta3sq = R(3.0 * (a.delta * a.delta));
+    c.mu6 = R(6.0 * a.mu);
+    c.omeg = R(a.omeg);
+    c.invtau = R(a.invtau);
+    c.g = R(a.g);
+    c.corr = corr;
+    return c;
+}
+
+// Forces, equilibrium and collision of one cell and the store of its nine
+// post-collision populations: slippage! (src/forcing.jl:43-44), the force sum
+// (src/simulate.jl:18-19), inclination! (src/forcing.jl:364-365),
+// equilibrium! and BGKandStream! (src/collide.jl:267-280).  (gpx, gpy) is
+// ∇p at the cell (h∇p!, src/forcing.jl:181-184); *hlo_p the rounding
+// residue of the pulled height (FP32 arithmetic; not read for a fresh step).
+template <class S, bool FRESH, bool TAU1>
+__device__ __forceinline__ void collide_cell(const StepArgs &a,
+                                             const CellConst<typename S::real> &cc,
+                                             const void *src, void *dst, int gx, int gy, int gxm,
+                                             int gxp, int cell, long long tt,
+                                             typename S::real h, typename S::real ux,
+                                             typename S::real uy, typename S::real gpx,
+                                             typename S::real gpy,
+                                             const typename S::real *hlo_p) {
+    using R = typename S::real;
+    constexpr bool LIT = S::kLiteral;
+    const long long pitch = a.pitch;
+    const int Lx = a.Lx, Ly = a.Ly;
+    const R hgx = h * gpx, hgy = h * gpy;
+    // slippage! (src/forcing.jl:43-44) and the force sum (src/simulate.jl:18-19)
+    R sx, sy;
+    if constexpr (LIT) {
+        const R den = R(2) * (h * h) + cc.delta6 * h + cc.delta3sq;
+        sx = (cc.mu6 * h * ux) / den;
+        sy = (cc.mu6 * h * uy) / den;
+    } else {
+        const R c = qdiv(cc.mu6 * h, (R(2) * h + cc.delta6) * h + cc.delta3sq);
+        sx = c * ux;
+        sy = c * uy;
+    }
+    R Fx = -hgx - sx, Fy = -hgy - sy;
+    if (a.incl) {  // inclination! (src/forcing.jl:364-365)
+        Fx = Fx + (h * R(a.ax)) * cc.incl_fac;
+        Fy = Fy + (h * R(a.ay)) * cc.incl_fac;
+    }
+    // collision (src/collide.jl:267-280); ftemp only matters for τ != 1
+    R fq[9];
+    R hft = h;
+    if constexpr (!TAU1) {
+        const int gym = gy == 0 ? Ly - 1 : gy - 1, gyp = gy == Ly - 1 ? 0 : gy + 1;
+        pull9<S>(src, pitch, Lx, gx, gy, gxm, gxp, gym, gyp, fq);
+        if constexpr (!LIT) hft = fq[0] + small8(fq);
+    }
+    if constexpr (LIT) {
+        R fe[9];
+        feq_literal<R>(h, ux, uy, cc.g, fe);
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            R v;
+            if constexpr (TAU1)
+                v = fe[q];
+            else
+                v = cc.omeg * fq[q] + cc.invtau * fe[q];
+            if (q > 0) v = v + source<R>(q, Fx, Fy);
+            S::st(dst, pitch, q, cell, v);
+        }
+    } else {
+        // FP32 arithmetic.  f0 closes the mass balance with the values as
+        // stored: f0 = M - Σ_{q>0} f_q, where M (the pulled mass, hi + lo)
+        // is what the cell must hold.  e, the exact rounding error of f0
+        // (Fast2Sum), the lo part of M and the FP64-measured correction
+        // are then put back: FP32 populations fold them into f1 and f3
+        // equally (momentum unchanged), resolved to ~ulp(f1); FP16
+        // populations add them to f0 by stochastic rounding, so that the
+        // per-cell storage error is unbiased (round-to-nearest would drop
+        // the sub-ulp term every step and drift).
+        R fe[9], fo[9];
+        feq_fast(h, ux, uy, cc.g, fe);
+#pragma unroll
+        for (int q = 1; q < 9; ++q) {
+            R v;
+            if constexpr (TAU1)
+                v = fe[q];
+            else
+                v = cc.omeg * fq[q] + cc.invtau * fe[q];
+            fo[q] = S::rt(q, v + source<R>(q, Fx, Fy));
+        }
+        R hlo = R(0);
+        if constexpr (!FRESH) hlo = *hlo_p;
+        // Σ_q fpost_q = (1-1/τ) Σ ft + Σ feq/τ = h once h is the pulled mass
+        const R mc = (TAU1 || !FRESH) ? h : cc.omeg * hft + cc.invtau * h;
+        const R ssum = small8(fo);
+        R f0 = mc - ssum;
+        const R e = (mc - f0) - ssum;
+        if constexpr (!S::kHalf) {
+            const R dd = R(0.5) * (e + hlo + R(cc.corr));
+            fo[1] = fo[1] + dd;
+            fo[3] = fo[3] + dd;
+        } else {
+            f0 = add_stochastic((float)f0, (float)(e + hlo + R(cc.corr)),
+                                mix32((unsigned)cell, (unsigned)tt));
+        }
+        fo[0] = f0;
+#pragma unroll
+        for (int q = 0; q < 9; ++q) S::st(dst, pitch, q, cell, fo[q]);
     }
 }
 
@@ -507,7 +654,7 @@ __device__ __forceinline__ void march_run(const StepArgs &a, int bx, int by, lon
     const bool pcol = t >= 1 && t < NT - 1;
 
     // FP16: per-cell share of the mass correction of this iteration
-    const double corr = (!LIT && !FRESH && a.mass_corr) ? a.ctl->corr[tt & 1] : 0.0;
+    const double corr = (!LIT && !FRESH && a.mass_corr) ? __ldcg(&a.ctl->corr[tt & 1]) : 0.0;
     // kappa and cospi(θ) of this column: constant (scalar θ) or θ(x, t) of
     // the moving-wettability mode, which depends on x only
     const int mode = a.theta_mode;
@@ -570,14 +717,7 @@ __device__ __forceinline__ void march_run(const StepArgs &a, int bx, int by, lon
     pressure_row(y0 - 1);
     pressure_row(y0);
 
-    R incl_fac = R(0);
-    if (a.incl) {
-        incl_fac = a.incl_loop_time
-                       ? R(0.5) + R(0.5) * tanh_r(R(tt - a.incl_tstart) / R(a.incl_tsmooth))
-                       : R(a.incl_fixed);
-    }
-    const R delta6 = R(6.0 * a.delta), delta3sq = R(3.0 * (a.delta * a.delta)), mu6 = R(6.0 * a.mu);
-    const R omeg = R(a.omeg), invtau = R(a.invtau), g = R(a.g);
+    const CellConst<R> cc = cell_consts<R>(a, tt, corr);
     const R thr = R(a.hthresh);
     const bool measure = a.meas_mask || a.mass_corr;
     PartT<R> part;
@@ -611,83 +751,8 @@ __device__ __forceinline__ void march_run(const StepArgs &a, int bx, int by, lon
         R gpx, gpy;
         grad9<R>(pc[t - 1], pm[t], pc[t + 1], pp[t], pm[t - 1], pm[t + 1], pp[t + 1], pp[t - 1],
                  gpx, gpy);
-        const R hgx = h * gpx, hgy = h * gpy;
-        // slippage! (src/forcing.jl:43-44) and the force sum (src/simulate.jl:18-19)
-        R sx, sy;
-        if constexpr (LIT) {
-            const R den = R(2) * (h * h) + delta6 * h + delta3sq;
-            sx = (mu6 * h * ux) / den;
-            sy = (mu6 * h * uy) / den;
-        } else {
-            const R c = qdiv(mu6 * h, (R(2) * h + delta6) * h + delta3sq);
-            sx = c * ux;
-            sy = c * uy;
-        }
-        R Fx = -hgx - sx, Fy = -hgy - sy;
-        if (a.incl) {  // inclination! (src/forcing.jl:364-365)
-            Fx = Fx + (h * R(a.ax)) * incl_fac;
-            Fy = Fy + (h * R(a.ay)) * incl_fac;
-        }
-        // collision (src/collide.jl:267-280); ftemp only matters for τ != 1
-        R fq[9];
-        R hft = h;
-        if constexpr (!TAU1) {
-            const int gym = gy == 0 ? Ly - 1 : gy - 1, gyp = gy == Ly - 1 ? 0 : gy + 1;
-            pull9<S>(src, pitch, Lx, gx, gy, gxm, gxp, gym, gyp, fq);
-            if constexpr (!LIT) hft = fq[0] + small8(fq);
-        }
-        if constexpr (LIT) {
-            R fe[9];
-            feq_literal<R>(h, ux, uy, g, fe);
-#pragma unroll
-            for (int q = 0; q < 9; ++q) {
-                R v;
-                if constexpr (TAU1)
-                    v = fe[q];
-                else
-                    v = omeg * fq[q] + invtau * fe[q];
-                if (q > 0) v = v + source<R>(q, Fx, Fy);
-                S::st(dst, pitch, q, cell, v);
-            }
-        } else {
-            // FP32 arithmetic.  f0 closes the mass balance with the values as
-            // stored: f0 = M - Σ_{q>0} f_q, where M (the pulled mass, hi + lo)
-            // is what the cell must hold.  e, the exact rounding error of f0
-            // (Fast2Sum), the lo part of M and the FP64-measured correction
-            // are then put back: FP32 populations fold them into f1 and f3
-            // equally (momentum unchanged), resolved to ~ulp(f1); FP16
-            // populations add them to f0 by stochastic rounding, so that the
-            // per-cell storage error is unbiased (round-to-nearest would drop
-            // the sub-ulp term every step and drift).
-            R fe[9], fo[9];
-            feq_fast(h, ux, uy, g, fe);
-#pragma unroll
-            for (int q = 1; q < 9; ++q) {
-                R v;
-                if constexpr (TAU1)
-                    v = fe[q];
-                else
-                    v = omeg * fq[q] + invtau * fe[q];
-                fo[q] = S::rt(q, v + source<R>(q, Fx, Fy));
-            }
-            const R hlo = FRESH ? R(0) : sm.lo[r & 3][t];
-            // Σ_q fpost_q = (1-1/τ) Σ ft + Σ feq/τ = h once h is the pulled mass
-            const R mc = (TAU1 || !FRESH) ? h : omeg * hft + invtau * h;
-            const R ssum = small8(fo);
-            R f0 = mc - ssum;
-            const R e = (mc - f0) - ssum;
-            if constexpr (!S::kHalf) {
-                const R dd = R(0.5) * (e + hlo + R(corr));
-                fo[1] = fo[1] + dd;
-                fo[3] = fo[3] + dd;
-            } else {
-                f0 = add_stochastic((float)f0, (float)(e + hlo + R(corr)),
-                                    mix32((unsigned)cell, (unsigned)tt));
-            }
-            fo[0] = f0;
-#pragma unroll
-            for (int q = 0; q < 9; ++q) S::st(dst, pitch, q, cell, fo[q]);
-        }
+        collide_cell<S, FRESH, TAU1>(a, cc, src, dst, gx, gy, gxm, gxp, cell, tt, h, ux, uy, gpx,
+                                     gpy, &sm.lo[r & 3][t]);
         // measures of the height at the start of this iteration
         if (!isfinite(h)) any_nan = 1;
         if (measure) {
@@ -715,11 +780,11 @@ __device__ __forceinline__ void march_run(const StepArgs &a, int bx, int by, lon
     if (measure) write_partials<NT, R>(a, part, tt, by * a.tiles_x + bx, sm.red);
 }
 
+// Iteration done + 1 of strip (bx, by), dispatched on its rare cases.
 template <class S, int NT>
-__device__ __forceinline__ void march_tile(const StepArgs &a, int bx, int by, int k,
+__device__ __forceinline__ void march_tile(const StepArgs &a, int bx, int by, long long done,
                                            MarchSmem<S, NT> &sm) {
-    const long long done = a.ctl->step_base + k;  // iterations completed
-    const bool fresh = done + 1 == a.ctl->fresh_step;
+    const bool fresh = done + 1 == __ldcg(&a.ctl->fresh_step);
     if (fresh) {
         if (a.tau_is_one)
             march_run<S, NT, true, true>(a, bx, by, done, sm);
@@ -730,6 +795,303 @@ __device__ __forceinline__ void march_tile(const StepArgs &a, int bx, int by, in
             march_run<S, NT, false, true>(a, bx, by, done, sm);
         else
             march_run<S, NT, false, false>(a, bx, by, done, sm);
+    }
+}
+
+// ------------------------------------------------------------ 2D tiles
+// For lattices whose populations stay in L2, the strip march above is bound
+// by one L2 round trip per row.  A 2D tile instead pulls all its cells at
+// once: a CTA of kT2NT threads owns kT2X x kT2Y output cells and
+//   A. pulls the (kT2X+4) x (kT2Y+4) cells around them (three per thread,
+//      27 loads in flight) and keeps h, and j and the rounding residue of
+//      the output cells, in shared memory;
+//   B. computes p on the (kT2X+2) x (kT2Y+2) cells around the outputs;
+//   C. computes forces and collision of the outputs (collide_cell, the same
+//      code as the strips: FP32 results are identical).
+// Halo pulls are 1.4x the outputs; they are served by L2.
+constexpr int kT2X = 32, kT2Y = 16, kT2NT = 256;
+constexpr int kT2HX = kT2X + 4, kT2HY = kT2Y + 4;  // heights
+constexpr int kT2PX = kT2X + 2, kT2PY = kT2Y + 2;  // pressures
+constexpr int kT2Out = kT2X * kT2Y;
+static_assert(kT2HX * kT2HY <= 3 * kT2NT, "three pulls per thread");
+static_assert(kT2PX * kT2PY <= 3 * kT2NT, "three pressures per thread");
+static_assert(kT2Out == 2 * kT2NT, "two outputs per thread");
+
+template <class S>
+struct TileSmem {
+    using R = typename S::real;
+    R h[kT2HY * kT2HX];
+    R p[kT2PY * kT2PX];
+    R jx[kT2Out];
+    R jy[kT2Out];
+    R lo[kT2Out];
+    PartT<R> red[kT2NT / 32];
+    PartT<double> redd[kT2NT / 32];
+};
+
+template <class S, bool FRESH, bool TAU1>
+__device__ __forceinline__ void tile2d_run(const StepArgs &a, int bx, int by, long long done,
+                                           TileSmem<S> &sm) {
+    using R = typename S::real;
+    static_assert(!S::kLiteral, "2D tiles: FP32 arithmetic only");
+    const int t = threadIdx.x;
+    const int Lx = a.Lx, Ly = a.Ly;
+    const long long pitch = a.pitch;
+    const long long tt = done + 1;
+    const void *src = (done & 1) ? a.fb : a.fa;
+    void *dst = (done & 1) ? a.fa : a.fb;
+    const int x0 = bx * kT2X, y0 = by * kT2Y;
+    const R gamma = R(a.gamma), hmin = R(a.hmin), hcrit = R(a.hcrit);
+    const int mode = a.theta_mode;
+    const double corr = (!FRESH && a.mass_corr) ? __ldcg(&a.ctl->corr[tt & 1]) : 0.0;
+
+    // A. pulls and moments
+    R ft[3][9];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int i = t + k * kT2NT;
+        if (i < kT2HX * kT2HY) {
+            const int gx = wrapc(x0 - 2 + i % kT2HX, Lx), gy = wrapc(y0 - 2 + i / kT2HX, Ly);
+            if constexpr (FRESH) {
+                ft[k][0] = reinterpret_cast<const R *>(a.hF)[gy * Lx + gx];
+            } else {
+                const int gxm = gx == 0 ? Lx - 1 : gx - 1, gxp = gx == Lx - 1 ? 0 : gx + 1;
+                const int gym = gy == 0 ? Ly - 1 : gy - 1, gyp = gy == Ly - 1 ? 0 : gy + 1;
+                pull9<S>(src, pitch, Lx, gx, gy, gxm, gxp, gym, gyp, ft[k]);
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int i = t + k * kT2NT;
+        if (i < kT2HX * kT2HY) {
+            const int lx = i % kT2HX, ly = i / kT2HX;
+            if constexpr (FRESH) {
+                sm.h[i] = ft[k][0];
+            } else {
+                R h, jx, jy;
+                moments9<false>(ft[k], h, jx, jy);
+                sm.h[i] = h;
+                if (lx >= 2 && lx < kT2X + 2 && ly >= 2 && ly < kT2Y + 2) {
+                    const int o = (ly - 2) * kT2X + (lx - 2);
+                    sm.jx[o] = jx;
+                    sm.jy[o] = jy;
+                    sm.lo[o] = moments_lo(ft[k], h);
+                }
+            }
+        }
+    }
+    __syncthreads();
+
+    // B. film pressure around the outputs
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int i = t + k * kT2NT;
+        if (i < kT2PX * kT2PY) {
+            const int px = i % kT2PX, py = i / kT2PX;
+            const R *hm = sm.h + py * kT2HX + px + 1;  // row above, column of the cell
+            const R *hc = hm + kT2HX, *hp = hc + kT2HX;
+            R kap = R(a.kap);
+            if (mode != THETA_SCALAR) {
+                const int gx = wrapc(x0 - 1 + px, Lx);
+                if (mode == THETA_FIELD) {
+                    const int gy = wrapc(y0 - 1 + py, Ly);
+                    kap = reinterpret_cast<const R *>(a.kapF)[gy * Lx + gx];
+                } else {
+                    const R th = R(a.theta0) + R(a.dtheta) * sinpi_r(R(2) * (R(gx) - R(a.wave_v) * R(tt)) / R(Lx));
+                    kap = kappa_of(th, a.n, a.m, hmin);
+                }
+            }
+            // ip = h[i-1,j], jp = h[i,j-1], im = h[i+1,j], jm = h[i,j+1], ...
+            sm.p[i] = pressure_cell<false, R>(hc[0], hc[-1], hm[0], hc[1], hp[0], hm[-1], hm[1],
+                                              hp[1], hp[-1], kap, gamma, hmin, hcrit, a.n, a.m);
+        }
+    }
+    __syncthreads();
+
+    // C. forces, collision, stores and measures of the outputs
+    const CellConst<R> cc = cell_consts<R>(a, tt, corr);
+    const R thr = R(a.hthresh);
+    const bool measure = a.meas_mask || a.mass_corr;
+    PartT<R> part;
+    part_init(part);
+    int any_nan = 0;
+#pragma unroll 1
+    for (int k = 0; k < 2; ++k) {
+        const int o = t + k * kT2NT;
+        const int ox = o % kT2X, oy = o / kT2X;
+        const int gx = x0 + ox, gy = y0 + oy;
+        if (gx >= Lx || gy >= Ly) continue;
+        const int cell = gy * Lx + gx;
+        const int gxm = gx == 0 ? Lx - 1 : gx - 1, gxp = gx == Lx - 1 ? 0 : gx + 1;
+        const R *hc = sm.h + (oy + 2) * kT2HX + ox + 2;
+        const R h = hc[0];
+        R ux, uy;
+        if constexpr (FRESH) {
+            ux = reinterpret_cast<const R *>(a.uxF)[cell];
+            uy = reinterpret_cast<const R *>(a.uyF)[cell];
+        } else {
+            velocity<false>(h, sm.jx[o], sm.jy[o], ux, uy);
+        }
+        const R *pc = sm.p + (oy + 1) * kT2PX + ox + 1, *pm = pc - kT2PX, *pp = pc + kT2PX;
+        R gpx, gpy;
+        grad9<R>(pc[-1], pm[0], pc[1], pp[0], pm[-1], pm[1], pp[1], pp[-1], gpx, gpy);
+        collide_cell<S, FRESH, TAU1>(a, cc, src, dst, gx, gy, gxm, gxp, cell, tt, h, ux, uy, gpx,
+                                     gpy, &sm.lo[o]);
+        if (!isfinite(h)) any_nan = 1;
+        if (measure) {
+            mass_add(part, h);
+            if constexpr (!FRESH) part.mlo += sm.lo[o];
+            const bool wet = h > thr;
+            part.wet += wet ? 1 : 0;
+            part.hmax = fmax(part.hmax, h);
+            part.hmin = fmin(part.hmin, h);
+            if ((a.meas_mask & SWB_MEAS_AREA) && wet) {
+                const R *hm = hc - kT2HX, *hp = hc + kT2HX;
+                R gx2, gy2;
+                grad9<R>(hc[-1], hm[0], hc[1], hp[0], hm[-1], hm[1], hp[1], hp[-1], gx2, gy2);
+                part.area += sqrt(gx2 * gx2 + gy2 * gy2 + R(1));
+                if (mode == THETA_FIELD) {
+                    part.cossum += reinterpret_cast<const R *>(a.cosF)[cell];
+                } else if (mode == THETA_WAVE) {
+                    const R th = R(a.theta0) + R(a.dtheta) * sinpi_r(R(2) * (R(gx) - R(a.wave_v) * R(tt)) / R(Lx));
+                    part.cossum += cospi_r(th);
+                }
+            }
+        }
+    }
+    any_nan = __syncthreads_or(any_nan);
+    if (any_nan && t == 0) a.ctl->nan_flag = 1;
+    if (measure) write_partials<kT2NT, R>(a, part, tt, by * a.tiles_x + bx, sm.red);
+}
+
+template <class S>
+__device__ __forceinline__ void tile2d_tile(const StepArgs &a, int bx, int by, long long done,
+                                            TileSmem<S> &sm) {
+    const bool fresh = done + 1 == __ldcg(&a.ctl->fresh_step);
+    if (fresh) {
+        if (a.tau_is_one)
+            tile2d_run<S, true, true>(a, bx, by, done, sm);
+        else
+            tile2d_run<S, true, false>(a, bx, by, done, sm);
+    } else {
+        if (a.tau_is_one)
+            tile2d_run<S, false, true>(a, bx, by, done, sm);
+        else
+            tile2d_run<S, false, false>(a, bx, by, done, sm);
+    }
+}
+
+// One iteration, one CTA per 2D tile plus the reducer (block 0).
+template <class S>
+__global__ void __launch_bounds__(kT2NT, 4) fused_tile_kernel(const StepArgs a, int k) {
+    __shared__ TileSmem<S> sm;
+    int b = blockIdx.x;
+    if (needs_partials(a) && k > 0) {
+        if (b == 0) {
+            reduce_step<kT2NT>(a, a.ctl->step_base + k, sm.redd);
+            return;
+        }
+        b -= 1;
+    }
+    tile2d_tile<S>(a, b % a.tiles_x, b / a.tiles_x, a.ctl->step_base + k, sm);
+}
+
+// ------------------------------------------------------------ multi-step
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Barrier across all CTAs of a cooperative launch (all co-resident), in two
+// levels so that no counter takes more than ~G/kBarGroups arrivals: CTA b
+// arrives on the counter of group b % kBarGroups; the last of a group
+// re-arms that counter and arrives on the top counter; the last group
+// re-arms the top counter and bumps every group's generation word, which the
+// group's CTAs poll (each word on its own 128-byte line).  Arrivals are
+// released by a device-scope fence.  Every wait is bounded by
+// kBarrierTimeoutNs and a spin cap; on expiry the CTA raises *err, and all
+// CTAs waiting now or later give up.  Returns false when the launch must stop.
+__device__ __forceinline__ bool grid_barrier(unsigned int *bar, int *err, unsigned int G) {
+    __syncthreads();
+    int ok = 1;
+    if (threadIdx.x == 0) {
+        const unsigned int grp = blockIdx.x % kBarGroups;
+        const unsigned int ngroups = G < kBarGroups ? G : kBarGroups;
+        const unsigned int gsize = (G - 1 - grp) / kBarGroups + 1;
+        unsigned int *sub = bar + kBarStride * (1 + grp);
+        volatile unsigned int *gen = bar + kBarStride * (1 + kBarGroups + grp);
+        volatile int *verr = err;
+        const unsigned int g0 = *gen;
+        __threadfence();
+        bool released = false;
+        if (atomicAdd(sub, 1u) == gsize - 1) {
+            atomicExch(sub, 0u);
+            __threadfence();
+            if (atomicAdd(bar, 1u) == ngroups - 1) {
+                atomicExch(bar, 0u);
+                __threadfence();
+                for (unsigned int k = 0; k < ngroups; ++k)
+                    atomicAdd(bar + kBarStride * (1 + kBarGroups + k), 1u);
+                released = true;
+            }
+        }
+        if (!released) {
+            const unsigned long long t0 = globaltimer_ns();
+            unsigned int spins = 0;
+            while (*gen == g0) {
+                if (*verr) {
+                    ok = 0;
+                    break;
+                }
+                if ((++spins & 255u) == 0u &&
+                    (globaltimer_ns() - t0 > kBarrierTimeoutNs || spins > (1u << 28))) {
+                    atomicExch(err, 1);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(32);
+            }
+        }
+        __threadfence();
+    }
+    return __syncthreads_and(ok) != 0;
+}
+
+// n time_loop iterations of one lattice in one cooperative launch.  CTA b
+// walks tiles b, b + G, ... of each iteration (strips of NT threads, or 2D
+// tiles when T2D); CTA G - 1 also reduces the previous iteration's measures
+// (with G = tiles + 1 it does nothing else), and after the last barrier the
+// last iteration's, and advances step_base.  S uses L2 loads (LdCG):
+// populations written by other CTAs one iteration earlier are read after a
+// grid barrier.
+template <class S, int NT, bool T2D>
+__global__ void __launch_bounds__(NT, T2D ? 2 : 1) fused_run_kernel(const StepArgs a, int n) {
+    using Smem = typename std::conditional<T2D, TileSmem<S>, MarchSmem<S, NT>>::type;
+    __shared__ Smem sm;
+    const int G = gridDim.x, b = blockIdx.x;
+    const int ntiles = a.tiles_x * a.tiles_y;
+    const bool red = needs_partials(a);
+    const long long base = __ldcg(&a.ctl->step_base);
+    for (int k = 0; k < n; ++k) {
+        if (red && k > 0 && b == G - 1) {
+            reduce_step<NT>(a, base + k, sm.redd);
+            __syncthreads();
+        }
+        for (int e = b; e < ntiles; e += G) {
+            if constexpr (T2D)
+                tile2d_tile<S>(a, e % a.tiles_x, e / a.tiles_x, base + k, sm);
+            else
+                march_tile<S, NT>(a, e % a.tiles_x, e / a.tiles_x, base + k, sm);
+            __syncthreads();
+        }
+        if (!grid_barrier(a.bar, &a.ctl->bar_err, (unsigned int)G)) return;
+    }
+    if (b == G - 1) {
+        if (red && n > 0) reduce_step<NT>(a, base + n, sm.redd);
+        __syncthreads();
+        if (threadIdx.x == 0) a.ctl->step_base = base + n;
     }
 }
 
@@ -746,7 +1108,7 @@ __global__ void __launch_bounds__(NT) fused_step_kernel(const StepArgs a, int k)
         }
         b -= 1;
     }
-    march_tile<S, NT>(a, b % a.tiles_x, b / a.tiles_x, k, sm);
+    march_tile<S, NT>(a, b % a.tiles_x, b / a.tiles_x, a.ctl->step_base + k, sm);
 }
 
 // Closes a sequence of n step launches: the last iteration's measures, then
@@ -773,7 +1135,7 @@ __global__ void __launch_bounds__(NT) batch_step_kernel(const StepArgs *__restri
         if (threadIdx.x == 0) sa = args[tr.lattice];
         __syncthreads();
         if (tr.tx >= 0)
-            march_tile<S, NT>(sa, tr.tx, tr.ty, k, sm);
+            march_tile<S, NT>(sa, tr.tx, tr.ty, sa.ctl->step_base + k, sm);
         else if (k > 0)
             reduce_step<NT>(sa, sa.ctl->step_base + k, sm.redd);
         __syncthreads();

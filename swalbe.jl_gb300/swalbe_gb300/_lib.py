@@ -30,6 +30,7 @@ FIELD = {"height": 0, "velx": 1, "vely": 2, "pressure": 3, "fout": 4, "feq": 5, 
          "slipx": 8, "slipy": 9, "h∇px": 10, "h∇py": 11, "vsq": 12}
 
 MEAS_MASS, MEAS_WETTED, MEAS_MAXMIN, MEAS_AREA, MEAS_ALL = 1, 2, 4, 8, 15
+STEP_AUTO, STEP_PER_ITERATION, STEP_MULTI = 0, 1, 2
 
 
 class Params(C.Structure):
@@ -99,6 +100,8 @@ def lib() -> C.CDLL:
             "swb_set_mass_correction": (i, [p, i]),
             "swb_set_geometry": (i, [p, i, i]),
             "swb_get_geometry": (i, [p, C.POINTER(i), C.POINTER(i)]),
+            "swb_set_step_mode": (i, [p, i]),
+            "swb_get_step_mode": (i, [p, C.POINTER(i)]),
             "swb_step": (i, [p, i64]),
             "swb_sync": (i, [p]),
             "swb_steps_done": (i, [p, C.POINTER(i64)]),

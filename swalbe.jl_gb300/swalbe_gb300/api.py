@@ -199,6 +199,17 @@ class GB300State:
         self._chk(lib().swb_get_geometry(self._h, C.byref(a), C.byref(b)))
         return a.value, b.value
 
+    def set_step_mode(self, mode) -> None:
+        """"auto", "per_iteration" (one launch per iteration, CUDA graphs) or
+        "multi" (one cooperative launch per 1024 iterations; FP32/FP16)."""
+        m = {"auto": 0, "per_iteration": 1, "multi": 2}.get(mode, mode)
+        self._chk(lib().swb_set_step_mode(self._h, int(m)))
+
+    def step_mode(self) -> str:
+        a = C.c_int()
+        self._chk(lib().swb_get_step_mode(self._h, C.byref(a)))
+        return {1: "per_iteration", 2: "multi"}[a.value]
+
     def set_mass_correction(self, on: bool) -> None:
         self._chk(lib().swb_set_mass_correction(self._h, int(bool(on))))
 

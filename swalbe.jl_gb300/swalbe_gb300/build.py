@@ -24,6 +24,7 @@ UNITS = {
     # no implicit FMA contraction: every kernel that inlines the step (single,
     # batch) must round identically for results to be independent of it
     "swb_step_f32.cu": ["--fmad=false"],
+    "swb_run_f32.cu": ["--fmad=false"],
     "swb_api.cu": [],
     "swb_batch.cu": [],
     "swb_server.cu": [],
