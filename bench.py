@@ -54,6 +54,8 @@ def parse():
     ap.add_argument("--profile-case", choices=["rt512", "film2048"],
                     help="run a few steps of one case, untimed (for ncu captures)")
     ap.add_argument("--geometry", default="", help="strip geometry NT,H for --profile-case")
+    ap.add_argument("--step-mode", default="per_iteration", choices=["per_iteration", "multi"],
+                    help="launch form for --profile-case")
     ap.add_argument("--case-steps", type=int, default=12)
     ap.add_argument("--workload", choices=["ensemble", "serving"],
                     help="print the ensemble (config 4) or serving (config 5) line only")
@@ -128,6 +130,16 @@ class ClockSampler:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
                 "samples": len(sm)}
+
+
+def kernel_name(prec, geo, form):
+    """The dominant kernel of a run with this geometry and launch form."""
+    store = {"f32": "StoreF32", "f16": "StoreF16", "f64": "StoreF64"}[prec]
+    if form == "multi":
+        return f"fused_run_kernel<{store}, {256 if geo[0] == 32 else geo[0]}, {geo[0] == 32}>"
+    if geo[0] == 32:
+        return f"fused_tile_kernel<{store}> (2D tiles 32x16)"
+    return f"fused_step_kernel<{store}, {geo[0]}> (strips of {geo[0] - 4}x{geo[1]})"
 
 
 def load_traffic(kernel_key: str):
@@ -262,14 +274,17 @@ def run_ours(args):
         torch.distributed.barrier()
     torch.cuda.synchronize()
     t_wall = time.perf_counter()
+    torch.cuda.nvtx.range_push("timed")  # the launch-list capture filters on this range
     step_ms, launch_ms = timed_chunks(st, sw, torch, stream, d_h0, d_zero, flush, args.steps,
                                       chunk, N)
+    torch.cuda.nvtx.range_pop()
     torch.cuda.synchronize()
     wall = time.perf_counter() - t_wall
     if world > 1:
         torch.distributed.barrier()
     launches = sw.launch_count() - n0
     clk = clocks.stop()
+    geo, form = st.geometry(), st.step_mode()
 
     dev_s = sum(step_ms) / 1e3
     if world > 1:
@@ -341,6 +356,8 @@ def run_ours(args):
             "l2": "flushed between timed steps (256 MiB write); the 512x512 state (19 MB) is "
                   "L2-resident within a step",
             "parallelism": "replicas" if world > 1 else "single GPU",
+            "geometry": {"nt": geo[0], "rows": geo[1], "form": form,
+                         "chosen_by": "autotuner (timed on the first 2000-step chunk)"},
         },
         "e2e": {"value": e2e_value, "unit": "MLUPS",
                 "h2d_bytes_per_step": 3 * N * rb,
@@ -348,7 +365,7 @@ def run_ours(args):
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": traffic,
-                     "kernel": f"fused_step_kernel<{args.precision}>, 512x512, "
+                     "kernel": f"{kernel_name(args.precision, geo, form)}, 512x512, "
                                f"{B_ALG[args.precision]} B/LU algorithmic",
                      "launch_us": t_launch * 1e6, "peak_kind": f"{peak_kind} (hbm_gbs burst)"},
         "clocks": clk,
@@ -455,18 +472,22 @@ def ensemble_run(sw, np, count=512, steps=200, plain_sample=8):
     }
 
 
-def serving_run(sw, np, duration=12.0, rate=200.0, budget=24 << 30, steps_per_tick=200,
-                queue_limit=64):
-    """Config 5: Poisson arrivals of thin-film solves (sides 64..2048, 1k-100k
+def serving_run(sw, np, duration=12.0, rate=200.0, budget=24 << 30, steps_per_tick=100,
+                queue_limit=256, policy="sjf", max_cells=16 << 20):
+    """Poisson arrivals (200/s) of thin-film solves (sides 64..2048, 1k-100k
     steps, moving wettability, g in [-1e-3, 0]) into the server for
-    `duration` seconds; offered load far exceeds the GPU, so the queue is
-    bounded and the excess rejected at submission."""
+    `duration` seconds.  The offered load is ~300x what one GPU serves, so
+    the queue is bounded; shortest-job-first admission with a bound on the
+    resident cells keeps lock-step ticks short (~60 ms), and a full queue
+    sheds its largest job."""
     from swalbe_gb300 import configs
     reqs = configs.serving_stream(rate=rate, duration=duration, seed=5)
     sv = sw.Server(budget, T=np.float32, steps_per_tick=steps_per_tick)
     sv.set_queue_limit(queue_limit)
+    sv.set_policy(policy, max_cells)
     t0 = time.perf_counter()
     pending, done, rejected, i = {}, [], 0, 0
+    sizes, failed = [], {}
     offered_lu = 0.0
     while True:
         now = time.perf_counter() - t0
@@ -474,9 +495,6 @@ def serving_run(sw, np, duration=12.0, rate=200.0, budget=24 << 30, steps_per_ti
             r = reqs[i]
             i += 1
             offered_lu += r.sysc.Lx * r.sysc.Ly * r.nsteps
-            if sv.stats().queued >= queue_limit:
-                rejected += 1
-                continue
             rid = sv.submit(r.sysc, r.height(), r.nsteps, theta0=r.theta0, dtheta=r.dtheta, v=r.v)
             if rid is None:
                 rejected += 1
@@ -486,6 +504,10 @@ def serving_run(sw, np, duration=12.0, rate=200.0, budget=24 << 30, steps_per_ti
             ok, _, info = sv.poll(rid)
             if ok:
                 done.append(info.t_done - info.t_submit)
+                sizes.append(pending[rid].sysc.Lx * pending[rid].sysc.Ly * pending[rid].nsteps)
+                del pending[rid]
+            elif info.status < 0:  # shed from a full queue, or failed
+                failed[info.status] = failed.get(info.status, 0) + 1
                 del pending[rid]
         if now > duration:
             break
@@ -502,6 +524,11 @@ def serving_run(sw, np, duration=12.0, rate=200.0, budget=24 << 30, steps_per_ti
         "resident_at_end": int(st.running), "queued_at_end": int(st.queued),
         "latency_s": {"p50": pct(0.50), "p99": pct(0.99), "max": lat[-1] if lat else None},
         "hbm_budget_GB": budget / 1e9, "steps_per_tick": steps_per_tick,
+        "policy": policy, "max_resident_cells": max_cells, "queue_limit": queue_limit,
+        "shed_or_rejected_total": int(st.rejected),
+        "ended_with_status": {str(k): v for k, v in failed.items()},
+        "completed_work_LU": {"median": float(np.median(sizes)) if sizes else None,
+                              "max": float(max(sizes)) if sizes else None},
     }
     sv.close()
     return res
@@ -549,11 +576,13 @@ def profile_case(args):
         st.set_geometry(nt, hh)
     else:
         st.set_geometry(0, 0)
+    st.set_step_mode(args.step_mode)
     st.height = h0
     st.step(args.case_steps)
     st.sync()
     print(json.dumps({"case": args.profile_case, "precision": args.precision,
-                      "geometry": st.geometry(), "steps": args.case_steps}))
+                      "geometry": st.geometry(), "form": st.step_mode(),
+                      "steps": args.case_steps}))
 
 
 def main():

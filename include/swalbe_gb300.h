@@ -159,7 +159,7 @@ int swb_set_inclination(swb_state *s, double ax, double ay, int loop_time, int64
  * of nt-4 columns and h rows (4..512) that they march row by row; or, with
  * nt = 32 (SWB_F32 / SWB_F16 only; h is ignored), CTAs of 256 threads own
  * 2D tiles of 32 x 16 cells whose loads are all issued at once.  By default SWB_F64 / SWB_F32
- * states autotune it on their first swb_step of >= 256 steps (timing a few
+ * states autotune it on their first swb_step of >= 512 steps (timing a few
  * geometries on those real steps; remembered per lattice size), and SWB_F16
  * states use a size rule.  Setting it (or (0, 0): the size rule) turns the
  * autotuner off.  Results do not depend on it, except through the order of
@@ -175,8 +175,10 @@ int swb_get_geometry(swb_state *s, int *nt, int *h);
  *                           runs up to 1024 iterations, CTAs meeting at a
  *                           grid barrier between iterations (strip width 64
  *                           or 128);
- *   SWB_STEP_AUTO           (default) the autotuner times both forms with
- *                           the geometry; without it, PER_ITERATION.
+ *   SWB_STEP_AUTO           (default) PER_ITERATION; the autotuner picks the
+ *                           geometry.  (MULTI measured 5-25 % slower on
+ *                           GB300; with SWB_STEP_MULTI the tuner picks the
+ *                           geometry among the multi-step candidates.)
  * Both forms give identical results for the same geometry.
  * swb_get_step_mode reports the form in effect (PER_ITERATION or MULTI). */
 #define SWB_STEP_AUTO 0
@@ -220,6 +222,13 @@ int swb_measure_now(swb_state *s, double hthresh, swb_measure *out);
 int swb_measure_field_noalloc(const double *d_height, int Lx, int Ly, double hthresh,
                               const double *d_cos_theta, double cos_theta, void *stream,
                               swb_measure *out);
+
+/* Number of droplets in a host height field: connected components of the
+ * cells with h > hthresh, 8-connected, periodic in x and y.  Host code, no
+ * GPU.  No counterpart in the reference (its measures stop at wetted!,
+ * src/measures.jl:13-17); used to compare spinodal dewetting across
+ * precisions. */
+int swb_count_droplets(const double *h, int Lx, int Ly, double hthresh, int64_t *count);
 
 /* ---------------------------------------------------------------------- */
 /* Per-op API, SWB_PLAIN64 only: one kernel per reference op on the full   */
@@ -283,6 +292,19 @@ int swb_server_destroy(swb_server *sv);
  * film in host memory); further submissions return SWB_ERR_BUSY and count
  * as rejected.  Default 1024. */
 int swb_server_set_queue_limit(swb_server *sv, int64_t max_queued);
+/* Scheduling.  Resident requests advance in lock step, so a request's
+ * latency is its step count times one step of the whole resident set.
+ *   SWB_SCHED_FIFO  admit in arrival order (default);
+ *   SWB_SCHED_SJF   admit the queued request with the least work
+ *                   (Lx*Ly*nsteps) first; a full queue then sheds its
+ *                   largest request (status SWB_ERR_BUSY) for a smaller
+ *                   newcomer.  Large requests can wait indefinitely under
+ *                   sustained overload.
+ * max_resident_cells > 0 also bounds the summed Lx*Ly of resident requests
+ * (a request larger than the bound still runs when it would be alone). */
+#define SWB_SCHED_FIFO 0
+#define SWB_SCHED_SJF 1
+int swb_server_set_policy(swb_server *sv, int policy, int64_t max_resident_cells);
 /* Queues a solve: params (Lx, Ly, γ, θ, g, ...), initial height (copied),
  * moving wettability (dtheta = 0 for none) and the step count. */
 int swb_server_submit(swb_server *sv, const swb_params *p, const double *h0, double theta0,

@@ -86,7 +86,7 @@ long long pitch_of(long long N) { return (N + 63) / 64 * 64; }
 int check_params(const swb_params *p, std::string *slot) {
     if (!p) return fail(slot, SWB_ERR_ARG, "params is NULL");
     if (p->Lx < 1 || p->Ly < 1) return fail(slot, SWB_ERR_ARG, "Lx and Ly must be >= 1");
-    if ((long long)p->Lx * p->Ly * 9 >= (1LL << 31))
+    if (9LL * (((long long)p->Lx * p->Ly + 63) / 64 * 64) >= (1LL << 31))
         return fail(slot, SWB_ERR_ARG, "lattice too large: Lx*Ly*9 must be < 2^31");
     if (!(p->tau > 0.0)) return fail(slot, SWB_ERR_ARG, "tau must be > 0");
     if (p->n <= p->m || p->m < 1) return fail(slot, SWB_ERR_ARG, "need n > m >= 1");
@@ -485,11 +485,57 @@ cudaError_t launch_sequence(swb_state *s, int n) {
     return e;
 }
 
-// Autotuner: times a few strip geometries on real steps (each probe is a
-// complete launch sequence, so nothing is wasted) and keeps the fastest.
-// Only for SWB_F64 / SWB_F32, whose results do not depend on the geometry.
-constexpr int kTuneMinSteps = 256;
-constexpr int kTuneProbe = 8;
+// Autotuner: times a few geometries and launch forms on real steps (each
+// probe is a complete launch sequence, so nothing is wasted) and keeps the
+// fastest.  Every candidate first runs a short untimed sequence, which also
+// loads its kernel (modules load lazily, on first launch).  Only for
+// SWB_F64 / SWB_F32, whose results do not depend on the geometry.
+constexpr int kTuneMinSteps = 512;
+constexpr int kTuneProbe = 16;
+
+// One candidate's probe: a per-iteration sequence is captured into a graph
+// (as it runs outside the tuner), a multi-step one is a single launch.
+// Returns the GPU time of the second of two runs (the first loads the
+// kernel) in ms, or a negative value on error.
+float tune_probe(swb_state *s, cudaEvent_t e0, cudaEvent_t e1) {
+    cudaGraphExec_t gx = nullptr;
+    if (!s->persist) {
+        cudaGraph_t g = nullptr;
+        if (cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+            return -1.f;
+        cudaError_t le = launch_sequence(s, kTuneProbe);
+        swb::count_launches(0ULL - (unsigned long long)(kTuneProbe + 1));  // captured, not run
+        cudaError_t ce = cudaStreamEndCapture(s->stream, &g);
+        if (le != cudaSuccess || ce != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            return -1.f;
+        }
+        cudaError_t ie = cudaGraphInstantiate(&gx, g, 0);
+        cudaGraphDestroy(g);
+        if (ie != cudaSuccess) return -1.f;
+    }
+    float ms = -1.f;
+    for (int rep = 0; rep < 2; ++rep) {
+        cudaEventRecord(e0, s->stream);
+        cudaError_t e;
+        if (gx) {
+            e = cudaGraphLaunch(gx, s->stream);
+            swb::count_launches(kTuneProbe + 1);
+        } else {
+            e = run_sequence(s, kTuneProbe);
+        }
+        cudaEventRecord(e1, s->stream);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        if (e != cudaSuccess) {
+            ms = -1.f;
+            break;
+        }
+        s->steps += kTuneProbe;
+        cudaEventElapsedTime(&ms, e0, e1);
+    }
+    if (gx) cudaGraphExecDestroy(gx);
+    return ms;
+}
 
 int autotune_geometry(swb_state *s, long long &left) {
     int nt = 0, h = 0;
@@ -510,7 +556,9 @@ int autotune_geometry(swb_state *s, long long &left) {
     const bool multi_ok = s->precision == SWB_F32 || s->precision == SWB_F16;
     for (auto &c : all) {
         if (c[0] == K && !multi_ok) continue;
-        if (c[2] && (!multi_ok || s->mode == SWB_STEP_PER_ITERATION)) continue;
+        // the multi-step form only when asked for: it never won on GB300
+        // (sweeps at 512^2..2048^2), and a 16-iteration probe can misjudge it
+        if (c[2] && (!multi_ok || s->mode != SWB_STEP_MULTI)) continue;
         if (!c[2] && s->mode == SWB_STEP_MULTI) continue;
         cands.push_back({c[0], c[1], c[2]});
     }
@@ -521,28 +569,18 @@ int autotune_geometry(swb_state *s, long long &left) {
     int bnt = s->a.march_nt, bh = s->a.march_h;
     bool bpers = s->persist;
     int rc = SWB_OK;
-    bool first = true;
     for (auto &c : cands) {
         if (c[1] > s->p.Ly && c[1] != swb::kMinRows) continue;
+        if (left < 2 * kTuneProbe) break;
         swb::set_geometry(s->a, c[0], c[1]);
         s->persist = c[2] != 0;
         if (s->persist && run_grid(s) <= 0) continue;
-        if (first) {  // warm-up with the first candidate
-            cudaError_t e = s->persist ? run_sequence(s, kTuneProbe) : launch_sequence(s, kTuneProbe);
-            if (e != cudaSuccess) { rc = fail(&s->err, SWB_ERR_CUDA, cudaGetErrorString(e)); break; }
-            left -= kTuneProbe;
-            s->steps += kTuneProbe;
-            first = false;
+        const float ms = tune_probe(s, e0, e1);
+        if (ms < 0.f) {
+            rc = fail(&s->err, SWB_ERR_CUDA, "autotuner probe failed");
+            break;
         }
-        cudaEventRecord(e0, s->stream);
-        cudaError_t e = s->persist ? run_sequence(s, kTuneProbe) : launch_sequence(s, kTuneProbe);
-        cudaEventRecord(e1, s->stream);
-        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
-        if (e != cudaSuccess) { rc = fail(&s->err, SWB_ERR_CUDA, cudaGetErrorString(e)); break; }
-        left -= kTuneProbe;
-        s->steps += kTuneProbe;
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, e0, e1);
+        left -= 2 * kTuneProbe;
         if (ms < best) {
             best = ms;
             bnt = c[0];

@@ -270,7 +270,7 @@ int swb_batch_create(const swb_params *params, int count, int precision, swb_bat
         return swb::bfail(nullptr, SWB_ERR_ARG, "batch precision must be SWB_F64, SWB_F32 or SWB_F16");
     for (int i = 0; i < count; ++i) {
         const swb_params &p = params[i];
-        if (p.Lx < 1 || p.Ly < 1 || (long long)p.Lx * p.Ly * 9 >= (1LL << 31) || !(p.tau > 0) ||
+        if (p.Lx < 1 || p.Ly < 1 || 9LL * (((long long)p.Lx * p.Ly + 63) / 64 * 64) >= (1LL << 31) || !(p.tau > 0) ||
             p.n <= p.m || p.m < 1 || !(p.hmin > 0))
             return swb::bfail(nullptr, SWB_ERR_ARG, "invalid params for lattice " + std::to_string(i));
         if (p.kbt != 0.0) return swb::bfail(nullptr, SWB_ERR_UNSUPPORTED, "kbt != 0 is not supported");

@@ -8,6 +8,13 @@
 // per step over the packed tile table of all resident lattices.  Each
 // lattice's arithmetic is independent of which others share the launch, so
 // a result is bit-identical alone and in the mix.
+//
+// Resident requests advance in lock step, so a request's latency is its
+// step count times the time of one step of the whole resident set.  The
+// scheduler therefore bounds the resident set (HBM budget, and optionally a
+// cell count) and orders the queue either first-come-first-served or
+// shortest-job-first by work (cells x steps); under SJF a full queue sheds
+// its largest job rather than refusing a smaller newcomer.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -35,6 +42,7 @@ struct Req {
     int64_t nsteps = 0, done = 0;
     int status = 0;  // 0 queued, 1 running, 2 done, <0 error
     double t_submit = 0, t_admit = 0, t_done = 0;
+    double work() const { return (double)p.Lx * p.Ly * (double)nsteps; }
     std::vector<double> result;
     char *dev = nullptr;
     LatticeLayout L{};
@@ -57,6 +65,9 @@ struct swb_server {
     int precision = SWB_F32;
     int steps_per_tick = 100;
     int64_t max_queued = 1024;
+    int policy = SWB_SCHED_FIFO;
+    int64_t max_cells = 0;       // resident cells (0: HBM budget only)
+    int64_t resident_cells = 0;
     int device = 0;
     std::mutex mu;
     std::condition_variable cv;
@@ -174,24 +185,44 @@ void worker_main(swb_server *sv) {
                     cudaFreeAsync((*it)->dev, sv->stream);
                     (*it)->dev = nullptr;
                     sv->in_use -= (*it)->bytes;
+                    sv->resident_cells -= (int64_t)(*it)->p.Lx * (*it)->p.Ly;
                     it = sv->active.erase(it);
                     changed = true;
                 } else {
                     ++it;
                 }
             }
-            // FIFO admission by HBM footprint
-            while (!sv->queue.empty()) {
-                Req *r = sv->reqs[sv->queue.front()].get();
+            // admission: FIFO or shortest job first, while the HBM budget and
+            // the resident-cell bound hold (one request may always run alone)
+            for (;;) {
+                auto pick = sv->queue.end();
+                for (auto it = sv->queue.begin(); it != sv->queue.end(); ++it) {
+                    Req *q = sv->reqs[*it].get();
+                    if (q->cancel) {
+                        pick = it;
+                        break;
+                    }
+                    if (sv->policy == SWB_SCHED_FIFO) {
+                        pick = it;
+                        break;
+                    }
+                    if (pick == sv->queue.end() || q->work() < sv->reqs[*pick]->work()) pick = it;
+                }
+                if (pick == sv->queue.end()) break;
+                Req *r = sv->reqs[*pick].get();
                 if (r->cancel) {
                     r->status = SWB_ERR_CANCELLED;
                     r->t_done = sv->now();
-                    sv->queue.pop_front();
+                    sv->queue.erase(pick);
                     continue;
                 }
+                const int64_t cells = (int64_t)r->p.Lx * r->p.Ly;
                 if (sv->in_use + r->bytes > sv->budget) break;
-                sv->queue.pop_front();
+                const bool alone = sv->active.empty() && admitted.empty();
+                if (sv->max_cells > 0 && sv->resident_cells + cells > sv->max_cells && !alone) break;
+                sv->queue.erase(pick);
                 sv->in_use += r->bytes;
+                sv->resident_cells += cells;
                 r->status = 1;
                 r->t_admit = sv->now();
                 admitted.push_back(r);
@@ -208,6 +239,7 @@ void worker_main(swb_server *sv) {
                 r->status = SWB_ERR_OOM;
                 r->t_done = sv->now();
                 sv->in_use -= r->bytes;
+                sv->resident_cells -= (int64_t)r->p.Lx * r->p.Ly;
                 sv->st.rejected++;
             }
         }
@@ -248,6 +280,7 @@ void worker_main(swb_server *sv) {
             r->status = (e == cudaSuccess && de == cudaSuccess) ? 2 : SWB_ERR_CUDA;
             r->t_done = sv->now();
             sv->in_use -= r->bytes;
+            sv->resident_cells -= (int64_t)r->p.Lx * r->p.Ly;
             sv->st.completed++;
             r->h0.clear();
             r->h0.shrink_to_fit();
@@ -328,16 +361,32 @@ int swb_server_destroy(swb_server *sv) {
 int swb_server_submit(swb_server *sv, const swb_params *p, const double *h0, double theta0,
                       double dtheta, double v, int64_t nsteps, int64_t *id) {
     if (!sv || !p || !h0 || !id || nsteps < 1) return sfail(SWB_ERR_ARG, "bad arguments");
-    if (p->Lx < 1 || p->Ly < 1 || (long long)p->Lx * p->Ly * 9 >= (1LL << 31) || !(p->tau > 0) ||
+    if (p->Lx < 1 || p->Ly < 1 || 9LL * (((long long)p->Lx * p->Ly + 63) / 64 * 64) >= (1LL << 31) || !(p->tau > 0) ||
         p->n <= p->m || p->m < 1 || !(p->hmin > 0))
         return sfail(SWB_ERR_ARG, "invalid params");
     if (p->kbt != 0.0) return sfail(SWB_ERR_UNSUPPORTED, "kbt != 0 is not supported");
+    const double work = (double)p->Lx * p->Ly * (double)nsteps;
     {
         std::lock_guard<std::mutex> g(sv->mu);
         if ((int64_t)sv->queue.size() >= sv->max_queued) {
-            sv->st.submitted++;
+            // SJF sheds the largest queued job if the newcomer is smaller
+            auto big = sv->queue.end();
+            if (sv->policy == SWB_SCHED_SJF)
+                for (auto it = sv->queue.begin(); it != sv->queue.end(); ++it)
+                    if (big == sv->queue.end() || sv->reqs[*it]->work() > sv->reqs[*big]->work())
+                        big = it;
+            if (big == sv->queue.end() || sv->reqs[*big]->work() <= work) {
+                sv->st.submitted++;
+                sv->st.rejected++;
+                return sfail(SWB_ERR_BUSY, "request queue full");
+            }
+            Req *victim = sv->reqs[*big].get();
+            victim->status = SWB_ERR_BUSY;
+            victim->t_done = sv->now();
+            victim->h0.clear();
+            victim->h0.shrink_to_fit();
             sv->st.rejected++;
-            return sfail(SWB_ERR_BUSY, "request queue full");
+            sv->queue.erase(big);
         }
     }
     auto r = std::make_unique<Req>();
@@ -372,6 +421,18 @@ int swb_server_set_queue_limit(swb_server *sv, int64_t max_queued) {
     if (!sv || max_queued < 1) return sfail(SWB_ERR_ARG, "bad arguments");
     std::lock_guard<std::mutex> g(sv->mu);
     sv->max_queued = max_queued;
+    return SWB_OK;
+}
+
+int swb_server_set_policy(swb_server *sv, int policy, int64_t max_resident_cells) {
+    if (!sv || (policy != SWB_SCHED_FIFO && policy != SWB_SCHED_SJF) || max_resident_cells < 0)
+        return sfail(SWB_ERR_ARG, "bad arguments");
+    {
+        std::lock_guard<std::mutex> g(sv->mu);
+        sv->policy = policy;
+        sv->max_cells = max_resident_cells;
+    }
+    sv->cv.notify_all();
     return SWB_OK;
 }
 

@@ -50,10 +50,10 @@ struct StoreF64T {
     using real = double;
     static constexpr bool kLiteral = true;
     static constexpr bool kHalf = false;
-    __device__ __forceinline__ static double ld(const void *b, long long pitch, int q, int i) {
+    __device__ __forceinline__ static double ld(const void *b, int pitch, int q, int i) {
         return L::ld(reinterpret_cast<const double *>(b) + q * pitch + i);
     }
-    __device__ __forceinline__ static void st(void *b, long long pitch, int q, int i, double v) {
+    __device__ __forceinline__ static void st(void *b, int pitch, int q, int i, double v) {
         reinterpret_cast<double *>(b)[q * pitch + i] = v;
     }
     __device__ __forceinline__ static double rt(int, double v) { return v; }
@@ -64,10 +64,10 @@ struct StoreF32T {
     using real = float;
     static constexpr bool kLiteral = false;
     static constexpr bool kHalf = false;
-    __device__ __forceinline__ static float ld(const void *b, long long pitch, int q, int i) {
+    __device__ __forceinline__ static float ld(const void *b, int pitch, int q, int i) {
         return L::ld(reinterpret_cast<const float *>(b) + q * pitch + i);
     }
-    __device__ __forceinline__ static void st(void *b, long long pitch, int q, int i, float v) {
+    __device__ __forceinline__ static void st(void *b, int pitch, int q, int i, float v) {
         reinterpret_cast<float *>(b)[q * pitch + i] = v;
     }
     __device__ __forceinline__ static float rt(int, float v) { return v; }
@@ -82,14 +82,14 @@ struct StoreF16T {
     static constexpr bool kHalf = true;
     static constexpr float kScale = 1024.0f;
     static constexpr float kInv = 1.0f / 1024.0f;
-    __device__ __forceinline__ static const __half *hp(const void *b, long long pitch) {
+    __device__ __forceinline__ static const __half *hp(const void *b, int pitch) {
         return reinterpret_cast<const __half *>(reinterpret_cast<const float *>(b) + pitch);
     }
-    __device__ __forceinline__ static float ld(const void *b, long long pitch, int q, int i) {
+    __device__ __forceinline__ static float ld(const void *b, int pitch, int q, int i) {
         if (q == 0) return L::ld(reinterpret_cast<const float *>(b) + i);
         return __half2float(L::ld(hp(b, pitch) + (q - 1) * pitch + i)) * kInv;
     }
-    __device__ __forceinline__ static void st(void *b, long long pitch, int q, int i, float v) {
+    __device__ __forceinline__ static void st(void *b, int pitch, int q, int i, float v) {
         if (q == 0) {
             reinterpret_cast<float *>(b)[i] = v;
         } else {
@@ -140,7 +140,7 @@ __device__ __forceinline__ R kappa_of(R theta, int n, int m, R hmin) {
 // Pull the nine populations of cell (gx, gy) from the post-collision buffer:
 // f_q(x) = fpost_q(x - c_q), c_q as in src/collide.jl:283-291.
 template <class S>
-__device__ __forceinline__ void pull9(const void *src, long long pitch, int Lx, int gx, int gy,
+__device__ __forceinline__ void pull9(const void *src, int pitch, int Lx, int gx, int gy,
                                       int gxm, int gxp, int gym, int gyp,
                                       typename S::real ft[9]) {
     const int rc = gy * Lx, rm = gym * Lx, rp = gyp * Lx;
@@ -223,18 +223,30 @@ __device__ __forceinline__ R pressure_cell(R h, R ip, R jp, R im, R jm, R ipjp, 
         pn = pow_loop(x, n);
         pm = pow_loop(x, m);
     }
-    R p = -gamma * (kap * (pn - pm));
-    R lap = R(2.0 / 3.0) * (((jp + ip) + im) + jm) + R(1.0 / 6.0) * (((ipjp + imjp) + imjm) + ipjm) -
-            R(10.0 / 3.0) * h;
-    return p - gamma * lap;
+    if constexpr (LIT) {
+        R p = -gamma * (kap * (pn - pm));
+        R lap = R(2.0 / 3.0) * (((jp + ip) + im) + jm) +
+                R(1.0 / 6.0) * (((ipjp + imjp) + imjm) + ipjm) - R(10.0 / 3.0) * h;
+        return p - gamma * lap;
+    } else {  // -γ (κ (x^n - x^m) + ∇²h), with fused multiply-adds
+        const R lap = __fmaf_rn(R(2.0 / 3.0), ((jp + ip) + im) + jm,
+                                __fmaf_rn(R(1.0 / 6.0), ((ipjp + imjp) + imjm) + ipjm,
+                                          R(-10.0 / 3.0) * h));
+        return -gamma * __fmaf_rn(kap, pn - pm, lap);
+    }
 }
 
 // Gradient stencil of h∇p! / ∇f_simple! (src/forcing.jl:181-184).
 template <class R>
 __device__ __forceinline__ void grad9(R ip, R jp, R im, R jm, R ipjp, R imjp, R imjm, R ipjm,
                                       R &gx, R &gy) {
-    gx = R(-1.0 / 3.0) * (ip - im) - R(1.0 / 12.0) * (((ipjp - imjp) - imjm) + ipjm);
-    gy = R(-1.0 / 3.0) * (jp - jm) - R(1.0 / 12.0) * (((ipjp + imjp) - imjm) - ipjm);
+    if constexpr (std::is_same<R, float>::value) {
+        gx = __fmaf_rn(-1.0f / 3.0f, ip - im, (-1.0f / 12.0f) * (((ipjp - imjp) - imjm) + ipjm));
+        gy = __fmaf_rn(-1.0f / 3.0f, jp - jm, (-1.0f / 12.0f) * (((ipjp + imjp) - imjm) - ipjm));
+    } else {
+        gx = R(-1.0 / 3.0) * (ip - im) - R(1.0 / 12.0) * (((ipjp - imjp) - imjm) + ipjm);
+        gy = R(-1.0 / 3.0) * (jp - jm) - R(1.0 / 12.0) * (((ipjp + imjp) - imjm) - ipjm);
+    }
 }
 
 // equilibrium! for one cell, literal (src/equilibrium.jl:67-114).
@@ -251,25 +263,6 @@ __device__ __forceinline__ void feq_literal(R h, R ux, R uy, R g, R fe[9]) {
     fe[6] = w5 * h * (g0 * h + R(3) * (uy - ux) + R(4.5) * ((uy - ux) * (uy - ux)) - R(1.5) * vsq);
     fe[7] = w5 * h * (g0 * h - R(3) * (ux + uy) + R(4.5) * ((ux + uy) * (ux + uy)) - R(1.5) * vsq);
     fe[8] = w5 * h * (g0 * h + R(3) * (ux - uy) + R(4.5) * ((ux - uy) * (ux - uy)) - R(1.5) * vsq);
-}
-
-// equilibrium for q = 1..8, FP32 (same polynomial, shared subexpressions).
-__device__ __forceinline__ void feq_fast(float h, float ux, float uy, float g, float fe[9]) {
-    const float vsq = ux * ux + uy * uy;
-    const float base = 1.5f * g * h - 1.5f * vsq;
-    const float w1h = h * (1.0f / 9.0f), w5h = h * (1.0f / 36.0f);
-    const float a = ux + uy, b = uy - ux;
-    const float ux2 = 4.5f * ux * ux, uy2 = 4.5f * uy * uy;
-    const float a2 = 4.5f * a * a, b2 = 4.5f * b * b;
-    fe[1] = w1h * (base + ux2 + 3.0f * ux);
-    fe[3] = w1h * (base + ux2 - 3.0f * ux);
-    fe[2] = w1h * (base + uy2 + 3.0f * uy);
-    fe[4] = w1h * (base + uy2 - 3.0f * uy);
-    fe[5] = w5h * (base + a2 + 3.0f * a);
-    fe[7] = w5h * (base + a2 - 3.0f * a);
-    fe[6] = w5h * (base + b2 + 3.0f * b);
-    fe[8] = w5h * (base + b2 - 3.0f * b);
-    fe[0] = 0.0f;  // f0 is closed by mass conservation in the fast path
 }
 
 // Force source of BGKandStream! (src/collide.jl:272-280).
@@ -411,7 +404,7 @@ __device__ __forceinline__ PartT<R> block_reduce(PartT<R> p, PartT<R> *red) {
 template <class S, int NT>
 struct MarchSmem {
     using R = typename S::real;
-    R h[5][NT];
+    R h[8][NT];  // ring of 5 live rows; 8 slots so that the index is a mask
     R p[4][NT];
     R jx[4][NT];
     R jy[4][NT];
@@ -538,24 +531,29 @@ __device__ __forceinline__ void collide_cell(const StepArgs &a,
                                              const typename S::real *hlo_p) {
     using R = typename S::real;
     constexpr bool LIT = S::kLiteral;
-    const long long pitch = a.pitch;
+    const int pitch = (int)a.pitch;  // 9 * pitch < 2^31 (checked at creation)
     const int Lx = a.Lx, Ly = a.Ly;
-    const R hgx = h * gpx, hgy = h * gpy;
     // slippage! (src/forcing.jl:43-44) and the force sum (src/simulate.jl:18-19)
-    R sx, sy;
+    R Fx, Fy;
     if constexpr (LIT) {
+        const R hgx = h * gpx, hgy = h * gpy;
         const R den = R(2) * (h * h) + cc.delta6 * h + cc.delta3sq;
-        sx = (cc.mu6 * h * ux) / den;
-        sy = (cc.mu6 * h * uy) / den;
+        const R sx = (cc.mu6 * h * ux) / den;
+        const R sy = (cc.mu6 * h * uy) / den;
+        Fx = -hgx - sx;
+        Fy = -hgy - sy;
+        if (a.incl) {  // inclination! (src/forcing.jl:364-365)
+            Fx = Fx + (h * R(a.ax)) * cc.incl_fac;
+            Fy = Fy + (h * R(a.ay)) * cc.incl_fac;
+        }
     } else {
-        const R c = qdiv(cc.mu6 * h, (R(2) * h + cc.delta6) * h + cc.delta3sq);
-        sx = c * ux;
-        sy = c * uy;
-    }
-    R Fx = -hgx - sx, Fy = -hgy - sy;
-    if (a.incl) {  // inclination! (src/forcing.jl:364-365)
-        Fx = Fx + (h * R(a.ax)) * cc.incl_fac;
-        Fy = Fy + (h * R(a.ay)) * cc.incl_fac;
+        const R c = qdiv(cc.mu6 * h, __fmaf_rn(__fmaf_rn(R(2), h, cc.delta6), h, cc.delta3sq));
+        Fx = __fmaf_rn(-h, gpx, -(c * ux));
+        Fy = __fmaf_rn(-h, gpy, -(c * uy));
+        if (a.incl) {
+            Fx = __fmaf_rn(h * R(a.ax), cc.incl_fac, Fx);
+            Fy = __fmaf_rn(h * R(a.ay), cc.incl_fac, Fy);
+        }
     }
     // collision (src/collide.jl:267-280); ftemp only matters for τ != 1
     R fq[9];
@@ -588,16 +586,31 @@ __device__ __forceinline__ void collide_cell(const StepArgs &a,
         // populations add them to f0 by stochastic rounding, so that the
         // per-cell storage error is unbiased (round-to-nearest would drop
         // the sub-ulp term every step and drift).
-        R fe[9], fo[9];
-        feq_fast(h, ux, uy, cc.g, fe);
+        // Opposite populations (q+, q-) share their equilibrium's even part
+        // A and odd part B (feq = A ± B, src/equilibrium.jl:67-114) and their
+        // force source ±S (src/collide.jl:272-280).
+        R fo[9];
+        const R vsq = __fmaf_rn(ux, ux, uy * uy);
+        const R base = __fmaf_rn(R(1.5) * cc.g, h, R(-1.5) * vsq);
+        const R w1h = h * R(1.0 / 9.0), w5h = h * R(1.0 / 36.0);
+        const R da = ux + uy, db = uy - ux;
+        const R cu[4] = {ux, uy, da, db};
+        const R wq[4] = {w1h, w1h, w5h, w5h};
+        const R sq[4] = {R(1.0 / 3.0) * Fx, R(1.0 / 3.0) * Fy, R(1.0 / 24.0) * (Fx + Fy),
+                         R(1.0 / 24.0) * (Fy - Fx)};
+        constexpr int qp[4] = {1, 2, 5, 6}, qm[4] = {3, 4, 7, 8};
 #pragma unroll
-        for (int q = 1; q < 9; ++q) {
-            R v;
-            if constexpr (TAU1)
-                v = fe[q];
-            else
-                v = cc.omeg * fq[q] + cc.invtau * fe[q];
-            fo[q] = S::rt(q, v + source<R>(q, Fx, Fy));
+        for (int k = 0; k < 4; ++k) {
+            const R A = wq[k] * __fmaf_rn(R(4.5) * cu[k], cu[k], base);
+            if constexpr (TAU1) {
+                const R BS = __fmaf_rn(R(3) * wq[k], cu[k], sq[k]);
+                fo[qp[k]] = S::rt(qp[k], A + BS);
+                fo[qm[k]] = S::rt(qm[k], A - BS);
+            } else {
+                const R B = (R(3) * wq[k]) * cu[k];
+                fo[qp[k]] = S::rt(qp[k], __fmaf_rn(cc.omeg, fq[qp[k]], cc.invtau * (A + B)) + sq[k]);
+                fo[qm[k]] = S::rt(qm[k], __fmaf_rn(cc.omeg, fq[qm[k]], cc.invtau * (A - B)) - sq[k]);
+            }
         }
         R hlo = R(0);
         if constexpr (!FRESH) hlo = *hlo_p;
@@ -633,7 +646,7 @@ __device__ __forceinline__ void march_run(const StepArgs &a, int bx, int by, lon
     const int t = threadIdx.x;
     const int Lx = a.Lx, Ly = a.Ly;
     const int H = a.march_h;
-    const long long pitch = a.pitch;
+    const int pitch = (int)a.pitch;  // 9 * pitch < 2^31 (checked at creation)
     const long long tt = done + 1;  // this time_loop iteration (1-based)
     const void *src = (done & 1) ? a.fb : a.fa;
     void *dst = (done & 1) ? a.fa : a.fb;
@@ -679,11 +692,11 @@ __device__ __forceinline__ void march_run(const StepArgs &a, int bx, int by, lon
     auto consume = [&](const R(&ft)[9], int yy) {
         const int r = yy - y0 + 2;  // >= 0
         if constexpr (FRESH) {
-            sm.h[r % 5][t] = ft[0];
+            sm.h[r & 7][t] = ft[0];
         } else {
             R h, jx, jy;
             moments9<LIT>(ft, h, jx, jy);
-            sm.h[r % 5][t] = h;
+            sm.h[r & 7][t] = h;
             sm.jx[r & 3][t] = jx;
             sm.jy[r & 3][t] = jy;
             if constexpr (!LIT) sm.lo[r & 3][t] = moments_lo(ft, h);
@@ -692,7 +705,7 @@ __device__ __forceinline__ void march_run(const StepArgs &a, int bx, int by, lon
     auto pressure_row = [&](int yy) {
         if (!pcol) return;
         const int r = yy - y0 + 2;  // >= 1
-        const R *hm = sm.h[(r + 4) % 5], *hc = sm.h[r % 5], *hp = sm.h[(r + 1) % 5];
+        const R *hm = sm.h[(r + 7) & 7], *hc = sm.h[r & 7], *hp = sm.h[(r + 1) & 7];
         const R kap = mode == THETA_FIELD
                           ? reinterpret_cast<const R *>(a.kapF)[wrow(yy) * Lx + gx]
                           : kap_col;
@@ -737,7 +750,7 @@ __device__ __forceinline__ void march_run(const StepArgs &a, int bx, int by, lon
         const int r = y - y0 + 2;
         const int gy = wrow(y);
         const int cell = gy * Lx + gx;
-        const R *hrow = sm.h[r % 5];
+        const R *hrow = sm.h[r & 7];
         const R h = hrow[t];
         R ux, uy;
         if constexpr (FRESH) {
@@ -763,7 +776,7 @@ __device__ __forceinline__ void march_run(const StepArgs &a, int bx, int by, lon
             part.hmax = fmax(part.hmax, h);
             part.hmin = fmin(part.hmin, h);
             if ((a.meas_mask & SWB_MEAS_AREA) && wet) {
-                const R *hm = sm.h[(r + 4) % 5], *hp = sm.h[(r + 1) % 5];
+                const R *hm = sm.h[(r + 7) & 7], *hp = sm.h[(r + 1) & 7];
                 R gx2, gy2;
                 grad9<R>(hrow[t - 1], hm[t], hrow[t + 1], hp[t], hm[t - 1], hm[t + 1], hp[t + 1],
                          hp[t - 1], gx2, gy2);
@@ -836,7 +849,7 @@ __device__ __forceinline__ void tile2d_run(const StepArgs &a, int bx, int by, lo
     static_assert(!S::kLiteral, "2D tiles: FP32 arithmetic only");
     const int t = threadIdx.x;
     const int Lx = a.Lx, Ly = a.Ly;
-    const long long pitch = a.pitch;
+    const int pitch = (int)a.pitch;  // 9 * pitch < 2^31 (checked at creation)
     const long long tt = done + 1;
     const void *src = (done & 1) ? a.fb : a.fa;
     void *dst = (done & 1) ? a.fa : a.fb;
@@ -1169,7 +1182,7 @@ __global__ void moments_kernel(const StepArgs a) {
         const int gxm = gx == 0 ? Lx - 1 : gx - 1, gxp = gx == Lx - 1 ? 0 : gx + 1;
         const int gym = gy == 0 ? Ly - 1 : gy - 1, gyp = gy == Ly - 1 ? 0 : gy + 1;
         R ft[9], h, jx, jy, ux, uy;
-        pull9<S>(src, a.pitch, Lx, gx, gy, gxm, gxp, gym, gyp, ft);
+        pull9<S>(src, (int)a.pitch, Lx, gx, gy, gxm, gxp, gym, gyp, ft);
         moments9<S::kLiteral>(ft, h, jx, jy);
         velocity<S::kLiteral>(h, jx, jy, ux, uy);
         reinterpret_cast<R *>(a.hF)[c] = h;
@@ -1192,7 +1205,7 @@ __global__ void fout_kernel(const StepArgs a, double *out) {
         const int gxm = gx == 0 ? Lx - 1 : gx - 1, gxp = gx == Lx - 1 ? 0 : gx + 1;
         const int gym = gy == 0 ? Ly - 1 : gy - 1, gyp = gy == Ly - 1 ? 0 : gy + 1;
         R ft[9];
-        pull9<S>(src, a.pitch, Lx, gx, gy, gxm, gxp, gym, gyp, ft);
+        pull9<S>(src, (int)a.pitch, Lx, gx, gy, gxm, gxp, gym, gyp, ft);
         for (int q = 0; q < 9; ++q) out[q * N + c] = (double)ft[q];
     }
 }

@@ -128,6 +128,8 @@ def lib() -> C.CDLL:
             "swb_server_destroy": (i, [p]),
             "swb_server_submit": (i, [p, PP, p, d, d, d, i64, C.POINTER(i64)]),
             "swb_server_set_queue_limit": (i, [p, i64]),
+            "swb_server_set_policy": (i, [p, i, i64]),
+            "swb_count_droplets": (i, [p, i, i, d, C.POINTER(i64)]),
             "swb_server_poll": (i, [p, i64, p, C.POINTER(RequestInfo)]),
             "swb_server_cancel": (i, [p, i64]),
             "swb_server_stats_get": (i, [p, C.POINTER(ServerStats)]),

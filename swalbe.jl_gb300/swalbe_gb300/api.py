@@ -303,6 +303,16 @@ def wetted_(area_size: list, state: GB300State, hthresh: float = 0.055) -> None:
     area_size.append(int(state.measure_now(hthresh).wetted))
 
 
+def count_droplets(h, hthresh: float = 0.055) -> int:
+    """Droplets in a height field: connected components of h > hthresh,
+    8-connected and periodic (host code in the library)."""
+    a = _f64(h, np.shape(h))
+    n = C.c_int64()
+    check(lib().swb_count_droplets(a.ctypes.data, a.shape[0], a.shape[1], float(hthresh),
+                                   C.byref(n)))
+    return n.value
+
+
 def surfacearea_(state: GB300State, hthresh: float = 0.055):
     """(area_lv, red_energy) of surfacearea! (src/measures.jl:126-168) for the θ set."""
     m = state.measure_now(hthresh)
@@ -543,6 +553,13 @@ class Server:
 
     def set_queue_limit(self, n: int) -> None:
         check(lib().swb_server_set_queue_limit(self._h, int(n)))
+
+    def set_policy(self, policy: str = "fifo", max_resident_cells: int = 0) -> None:
+        """"fifo" or "sjf" (shortest job first by Lx*Ly*nsteps, shedding the
+        largest queued job when the queue is full), and an optional bound
+        on the summed cells of resident requests."""
+        code = {"fifo": 0, "sjf": 1}[policy]
+        check(lib().swb_server_set_policy(self._h, code, int(max_resident_cells)))
 
     def submit(self, sysc: SysConst, h0, nsteps: int, theta0=None, dtheta=0.0, v=0.0):
         """Request id, or None when the queue is full (counted as rejected)."""

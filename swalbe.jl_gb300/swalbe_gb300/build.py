@@ -29,6 +29,7 @@ UNITS = {
     "swb_batch.cu": [],
     "swb_server.cu": [],
     "swb_noalloc.cu": [],
+    "swb_analysis.cu": [],
 }
 
 

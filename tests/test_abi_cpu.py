@@ -89,3 +89,46 @@ def test_device_strings():
         sw.Sys(sw.SysConst(4, 4), "CPU")
     with pytest.raises(NotImplementedError):
         sw.Sys(sw.SysConst(4, 4), "GB300", kind="thermal")
+
+
+def _components_reference(h, thr):
+    """Breadth-first labelling, periodic 8-neighbourhood (test reference)."""
+    from collections import deque
+    Lx, Ly = h.shape
+    seen = np.zeros(h.shape, bool)
+    n = 0
+    for i in range(Lx):
+        for j in range(Ly):
+            if h[i, j] <= thr or seen[i, j]:
+                continue
+            n += 1
+            seen[i, j] = True
+            q = deque([(i, j)])
+            while q:
+                a, b = q.popleft()
+                for da in (-1, 0, 1):
+                    for db in (-1, 0, 1):
+                        x, y = (a + da) % Lx, (b + db) % Ly
+                        if h[x, y] > thr and not seen[x, y]:
+                            seen[x, y] = True
+                            q.append((x, y))
+    return n
+
+
+@pytest.mark.parametrize("shape,seed", [((37, 23), 1), ((64, 64), 2), ((1, 9), 3), ((5, 1), 4)])
+def test_count_droplets_matches_bfs(shape, seed):
+    """Host-only library function: no GPU needed."""
+    rng = np.random.default_rng(seed)
+    h = np.asfortranarray(rng.uniform(0, 0.1, shape))
+    assert sw.count_droplets(h) == _components_reference(h, 0.055)
+
+
+def test_count_droplets_periodic_and_diagonal():
+    h = np.full((10, 8), 0.05)
+    h[0, 3] = h[9, 3] = 1.0           # joined across the x boundary
+    h[4, 4] = h[5, 5] = 1.0           # joined diagonally
+    h[2, 0] = h[2, 7] = 1.0           # joined across the y boundary
+    h[7, 7] = h[8, 0] = 1.0           # diagonal across the y boundary
+    assert sw.count_droplets(h) == 4
+    assert sw.count_droplets(np.full((4, 4), 0.01)) == 0
+    assert sw.count_droplets(np.full((4, 4), 1.0)) == 1

@@ -343,6 +343,16 @@ def _wait(sv, rid, shape, timeout=60):
     raise TimeoutError(rid)
 
 
+def _wait_running(sv, rid, timeout=60):
+    import time
+    t0 = time.time()
+    while time.time() - t0 < timeout:
+        if sv.poll(rid)[2].status >= 1:
+            return
+        time.sleep(0.001)
+    raise TimeoutError(rid)
+
+
 def test_server_admission_by_hbm():
     sv = sw.Server(40 << 20, T=np.float32, steps_per_tick=20)
     big = sysc(1024, 1024)  # ~76 MB of state: larger than the budget
@@ -354,6 +364,56 @@ def test_server_admission_by_hbm():
         _wait(sv, i, None)
     st = sv.stats()
     assert st.completed == 4 and st.hbm_in_use == 0
+    sv.close()
+
+
+def test_server_sjf_admits_smallest_first():
+    # one resident at a time (bound of 128x128 cells); while A runs, C (large)
+    # and B (small) queue; shortest-job-first admits B before C
+    sv = sw.Server(1 << 30, T=np.float32, steps_per_tick=100)
+    sv.set_policy("sjf", 128 * 128)
+    a = sv.submit(sysc(128, 128), rough(128, 128, 1), 4000)
+    _wait_running(sv, a)
+    c = sv.submit(sysc(128, 128), rough(128, 128, 2), 2000)
+    b = sv.submit(sysc(32, 32), rough(32, 32, 3), 100)
+    for rid in (a, b, c):
+        _wait(sv, rid, None)
+    info = {rid: sv.poll(rid)[2] for rid in (a, b, c)}
+    assert info[b].t_admit < info[c].t_admit
+    assert info[a].t_admit <= info[b].t_admit
+    sv.close()
+
+
+def test_server_sjf_sheds_largest_when_full():
+    sv = sw.Server(1 << 30, T=np.float32, steps_per_tick=100)
+    sv.set_policy("sjf", 128 * 128)
+    sv.set_queue_limit(2)
+    a = sv.submit(sysc(128, 128), rough(128, 128, 1), 6000)
+    _wait_running(sv, a)  # resident: the bound keeps the others queued
+    big1 = sv.submit(sysc(128, 128), rough(128, 128, 2), 3000)
+    big2 = sv.submit(sysc(128, 128), rough(128, 128, 3), 2500)
+    small = sv.submit(sysc(32, 32), rough(32, 32, 4), 100)  # queue full: big1 is shed
+    assert small is not None
+    huge = sv.submit(sysc(128, 128), rough(128, 128, 5), 9000)  # larger than all queued
+    assert huge is None
+    for rid in (a, big2, small):
+        _wait(sv, rid, None)
+    done, _, info = sv.poll(big1)
+    assert not done and info.status == L.SWB_ERR_BUSY
+    sv.close()
+
+
+def test_server_fifo_refuses_when_full():
+    sv = sw.Server(1 << 30, T=np.float32, steps_per_tick=100)
+    sv.set_policy("fifo", 128 * 128)
+    sv.set_queue_limit(1)
+    a = sv.submit(sysc(128, 128), rough(128, 128, 1), 6000)
+    _wait_running(sv, a)
+    q = sv.submit(sysc(128, 128), rough(128, 128, 2), 100)
+    small = sv.submit(sysc(32, 32), rough(32, 32, 4), 100)
+    assert small is None  # FIFO never sheds a queued request
+    for rid in (a, q):
+        _wait(sv, rid, None)
     sv.close()
 
 
