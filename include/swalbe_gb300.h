@@ -55,7 +55,7 @@ typedef struct swb_params {
     int32_t Lx, Ly;       /* lattice size                                  */
     int32_t Tmax, tdump;  /* time steps, dump interval                     */
     double tau, cs, mu;   /* relaxation time, sound speed, kinematic visc.  */
-    double delta, kbt;    /* slip length, thermal energy (must be 0)        */
+    double delta, kbt;    /* slip length, thermal energy (0: no fluctuations) */
     double gamma;         /* surface tension                                */
     int32_t n, m;         /* disjoining-pressure exponents                  */
     double hmin, hcrit;   /* Π(hmin) = 0, stabiliser                        */
@@ -147,6 +147,14 @@ int swb_launch_count(uint64_t *count);
 int swb_set_theta(swb_state *s, double theta);
 int swb_set_theta_field(swb_state *s, const double *theta);
 int swb_set_theta_wave(swb_state *s, double theta0, double dtheta, double v);
+/* Moving substrate: the θ field set by swb_set_theta_field moves by
+ * (dx, dy) cells (periodically) after every tmove iterations, counted from
+ * this call -- move_substrate!(θ, input, t, tmove; direction) called at the
+ * end of each iteration (scripts/Moving_wettability_structs.jl:139-152;
+ * direction "diagonal" = (1, 1), "x" = (1, 0), "y" = (0, 1)).  The field is
+ * not copied: the step reads it at the moved index.  tmove = 0 stops it;
+ * setting a θ (field, scalar or wave) resets it. */
+int swb_set_substrate_motion(swb_state *s, int64_t tmove, int dx, int dy);
 
 /* inclination!(α, state; t, tstart, tsmooth) as the time_loop callback
  * (src/forcing.jl:363-368, src/simulate.jl:89).  loop_time = 0 uses the
@@ -223,6 +231,17 @@ int swb_measure_field_noalloc(const double *d_height, int Lx, int Ly, double hth
                               const double *d_cos_theta, double cos_theta, void *stream,
                               swb_measure *out);
 
+/* Thermal fluctuations (kbt > 0 in the params): every iteration adds
+ * -thermal!(h) to the force, Fx .= -h∇px .- slipx .- kbtx as the reference's
+ * thermal scripts do (src/forcing.jl:297-320, scripts/Rivulet_stability.jl:123).
+ * The normals come from Philox-4x32-10 keyed by the seed with counter (cell,
+ * iteration): reproducible, and the same stream in every precision mode and
+ * launch form (Julia's randn! stream cannot be reproduced).  Default seed 0. */
+int swb_set_thermal_seed(swb_state *s, uint64_t seed);
+/* thermal!(kbtx, kbty, height, kbt, mu, delta) of the current height for
+ * iteration t: the forces the step subtracts (host, column-major). */
+int swb_thermal_field(swb_state *s, int64_t t, double *fx, double *fy);
+
 /* Number of droplets in a host height field: connected components of the
  * cells with h > hthresh, 8-connected, periodic in x and y.  Host code, no
  * GPU.  No counterpart in the reference (its measures stop at wetted!,
@@ -238,6 +257,8 @@ int swb_op_filmpressure(swb_state *s);          /* src/pressure.jl:119-155 (uses
 int swb_op_hgradp(swb_state *s);                /* src/forcing.jl:168-187 */
 int swb_op_slippage(swb_state *s);              /* src/forcing.jl:42-56 */
 int swb_op_force_sum(swb_state *s);             /* src/simulate.jl:18-19 */
+int swb_op_thermal(swb_state *s, int64_t t);    /* Fx .-= kbtx, Fy .-= kbty: thermal! of iteration t
+                                                   (src/forcing.jl:297-320); no-op when kbt == 0 */
 int swb_op_inclination(swb_state *s, double ax, double ay, int64_t t, int64_t tstart,
                        int64_t tsmooth);        /* src/forcing.jl:363-368 */
 int swb_op_equilibrium(swb_state *s);           /* src/equilibrium.jl:63-119 */
@@ -260,6 +281,10 @@ int swb_batch_step(swb_batch *b, int64_t nsteps);
  * lattice saw a non-finite height. */
 int swb_batch_sync(swb_batch *b);
 /* Tile shape chosen by the autotuner (0 until the first step). */
+/* Strips of every lattice: nt threads (64, 128, 256; nt - 4 columns) and
+ * `rows` rows (4..512, capped at each lattice's height).  Default 64 x 32:
+ * the batch's parallelism comes from its many lattices, so strips are tall. */
+int swb_batch_set_geometry(swb_batch *b, int nt, int rows);
 int swb_batch_tile(swb_batch *b, int *tile_x, int *tile_y, int *steps_per_graph);
 
 /* ---------------------------------------------------------------------- */

@@ -54,7 +54,9 @@ class LoopOpts(C.Structure):
     _fields_ = [("theta_field", C.c_void_p), ("theta", C.c_double), ("record_dh", C.c_int),
                 ("callback", C.c_int), ("hthresh", C.c_double), ("incl_ax", C.c_double),
                 ("incl_ay", C.c_double), ("incl_loop_time", C.c_int), ("incl_t", C.c_long),
-                ("incl_tstart", C.c_long), ("incl_tsmooth", C.c_long)]
+                ("incl_tstart", C.c_long), ("incl_tsmooth", C.c_long),
+                ("thermal_seed", C.c_uint64), ("t_offset", C.c_long),
+                ("shift_tmove", C.c_long), ("shift_dx", C.c_int), ("shift_dy", C.c_int)]
 
 
 class LoopOut(C.Structure):
@@ -100,6 +102,9 @@ def lib() -> C.CDLL:
             "orc_fused_run": (i, [p, p, p, p, p, p, p, p, i, i, p, p, i]),
             "orc_pull_all": (None, [p, p, i, i]),
             "orc_max_threads": (i, []),
+            "orc_philox4x32_10": (None, [p, p, p]),
+            "orc_thermal_normals": (None, [C.c_uint64, C.c_uint64, C.c_int64, p, p]),
+            "orc_thermal": (None, [p, p, p, sz, d, d, d, C.c_uint64, C.c_int64]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -271,9 +276,14 @@ class LoopResult:
     wet: Optional[np.ndarray]
 
 
-def _opts(theta_field, theta, record_dh, callback, hthresh, incl):
+def _opts(theta_field, theta, record_dh, callback, hthresh, incl, seed=0, t_offset=0,
+          motion=None):
     tf = None if theta_field is None else _col(theta_field)
     o = LoopOpts()
+    if motion:  # (tmove, dx, dy): move_substrate! after every tmove iterations
+        o.shift_tmove, o.shift_dx, o.shift_dy = (int(v) for v in motion)
+    o.thermal_seed = int(seed)
+    o.t_offset = int(t_offset)
     o.theta_field = None if tf is None else tf.ctypes.data
     o.theta = float(theta)
     o.record_dh = int(record_dh)
@@ -290,7 +300,8 @@ def _opts(theta_field, theta, record_dh, callback, hthresh, incl):
 
 
 def time_loop_literal(P: Params, h0, steps, *, theta_field=None, theta=None, record_dh=False,
-                      callback=None, hthresh=0.055, incl=None, ux0=None, uy0=None) -> LoopResult:
+                      callback=None, hthresh=0.055, incl=None, ux0=None, uy0=None,
+                      seed=0) -> LoopResult:
     """Literal time_loop on a fresh Sys() state with height = h0 (src/simulate.jl:6-96)."""
     L = lib()
     Lx, Ly = P.Lx, P.Ly
@@ -306,7 +317,7 @@ def time_loop_literal(P: Params, h0, steps, *, theta_field=None, theta=None, rec
         if uy0 is not None:
             field(5, (Lx, Ly))[...] = _col(uy0)
         o, tf = _opts(theta_field, P.theta if theta is None else theta, record_dh, callback,
-                      hthresh, incl)
+                      hthresh, incl, seed)
         mass = np.full(steps, np.nan)
         dh = np.zeros(steps) if record_dh else None
         wet = np.zeros(steps, dtype=np.int64) if callback == "wetted" else None
@@ -333,12 +344,13 @@ class FusedState:
         self.press = np.zeros((Lx, Ly), order="F")
         self.kappa = np.zeros((Lx, Ly), order="F")
         self.fresh = True
+        self.t = 0  # iterations done (index of the thermal noise)
 
     def run(self, steps, *, theta_field=None, theta=None, record_dh=False, callback=None,
-            hthresh=0.055, incl=None, nthreads=0):
+            hthresh=0.055, incl=None, nthreads=0, seed=0, motion=None):
         P = self.P
         o, tf = _opts(theta_field, P.theta if theta is None else theta, record_dh, callback,
-                      hthresh, incl)
+                      hthresh, incl, seed, self.t, motion)
         mass = np.full(steps, np.nan)
         dh = np.zeros(steps) if record_dh else None
         wet = np.zeros(steps, dtype=np.int64) if callback == "wetted" else None
@@ -349,6 +361,7 @@ class FusedState:
                             C.byref(o), C.byref(out), int(nthreads))
         if steps > 0:
             self.fresh = False
+        self.t += steps
         return LoopResult(self.h, self.ux, self.uy, mass, dh, wet)
 
     def fout(self):
@@ -371,6 +384,7 @@ class LiteralState:
     def __init__(self, P: Params):
         self.P = P
         self._s = lib().orc_state_new(P.Lx, P.Ly)
+        self.t = 0
 
     def __del__(self):
         if getattr(self, "_s", None):
@@ -385,10 +399,11 @@ class LiteralState:
         return np.ctypeslib.as_array((C.c_double * n).from_address(ptr)).reshape(shape, order="F")
 
     def run(self, steps, *, theta_field=None, theta=None, record_dh=False, callback=None,
-            hthresh=0.055, incl=None) -> LoopResult:
+            hthresh=0.055, incl=None, seed=0, motion=None) -> LoopResult:
         P = self.P
         o, tf = _opts(theta_field, P.theta if theta is None else theta, record_dh, callback,
-                      hthresh, incl)
+                      hthresh, incl, seed, self.t, motion)
+        self.t += steps
         mass = np.full(steps, np.nan)
         dh = np.zeros(steps) if record_dh else None
         wet = np.zeros(steps, dtype=np.int64) if callback == "wetted" else None
@@ -397,3 +412,24 @@ class LiteralState:
         lib().orc_time_loop(self._s, C.byref(P), steps, C.byref(o), C.byref(out))
         return LoopResult(self.field("height").copy(order="F"), self.field("velx").copy(order="F"),
                           self.field("vely").copy(order="F"), mass, dh, wet)
+
+
+# ---------------------------------------------------------------- thermal
+def philox4x32_10(ctr, key):
+    """Philox-4x32-10 block (four 32-bit words) of counter `ctr` and key `key`."""
+    c = (C.c_uint32 * 4)(*[int(v) & 0xFFFFFFFF for v in ctr])
+    k = (C.c_uint32 * 2)(*[int(v) & 0xFFFFFFFF for v in key])
+    out = (C.c_uint32 * 4)()
+    lib().orc_philox4x32_10(c, k, out)
+    return list(out)
+
+
+def thermal(h, kbt, mu, delta, seed=0, t=1):
+    """thermal!(fx, fy, h, kbt, mu, delta) (src/forcing.jl:297-311) with the
+    counter-based normals of iteration t."""
+    hh = _col(h)
+    fx = np.zeros_like(hh)
+    fy = np.zeros_like(hh)
+    lib().orc_thermal(_p(fx), _p(fy), _p(hh), hh.size, float(kbt), float(mu), float(delta),
+                      int(seed), int(t))
+    return fx, fy

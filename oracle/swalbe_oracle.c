@@ -454,7 +454,76 @@ typedef struct {
     double incl_ax, incl_ay;   /* inclination! α                                */
     int incl_loop_time;        /* 1: t = loop iteration, 0: t = incl_t        */
     long incl_t, incl_tstart, incl_tsmooth;
+    uint64_t thermal_seed;     /* thermal! noise stream (used when kbt > 0)     */
+    long t_offset;             /* iterations done before this call (noise index) */
+    long shift_tmove;          /* moving θ field: move_substrate! every tmove     */
+    int shift_dx, shift_dy;    /* iterations by (dx, dy) cells; 0: fixed field  */
 } orc_loop_opts;
+
+/* Offset of the moving θ field at global iteration T: move_substrate!
+ * (scripts/Moving_wettability_structs.jl:139-152) circshifts the field by
+ * (dx, dy) at the end of every tmove-th iteration, so iteration T sees it
+ * moved k = (T - 1) / tmove times: field(i, j) = θ(i - k dx, j - k dy). */
+static void field_shift(const orc_loop_opts *o, long T, int Lx, int Ly, int *sx, int *sy) {
+    *sx = 0;
+    *sy = 0;
+    if (o->shift_tmove <= 0 || T < 1) return;
+    const long k = (T - 1) / o->shift_tmove;
+    *sx = (int)((k % Lx) * o->shift_dx % Lx);
+    *sy = (int)((k % Ly) * o->shift_dy % Ly);
+}
+
+/* ------------------------------------------------------------------ */
+/* thermal! (src/forcing.jl:297-320): per cell and component a standard  */
+/* normal times sqrt(2 kbt mu 6 h / (2h^2 + 6 h delta + 3 delta^2)).     */
+/* Julia's randn! stream cannot be reproduced, so the normals come from  */
+/* a counter-based generator shared with the GPU: Philox-4x32-10 (Salmon, */
+/* Moraes, Dror, Shaw, SC'11) keyed by the seed, counter (cell, t), then  */
+/* Box-Muller.  The reference pins only mean 0 and variance 2 kbt/11 at   */
+/* h = 1 (test/forcing.jl:141-164).                                       */
+/* ------------------------------------------------------------------ */
+void orc_philox4x32_10(const uint32_t ctr_in[4], const uint32_t key_in[2], uint32_t out[4]) {
+    uint32_t x0 = ctr_in[0], x1 = ctr_in[1], x2 = ctr_in[2], x3 = ctr_in[3];
+    uint32_t k0 = key_in[0], k1 = key_in[1];
+    for (int r = 0; r < 10; ++r) {
+        if (r) {
+            k0 += 0x9E3779B9u;
+            k1 += 0xBB67AE85u;
+        }
+        const uint64_t p0 = (uint64_t)0xD2511F53u * x0, p1 = (uint64_t)0xCD9E8D57u * x2;
+        const uint32_t y0 = (uint32_t)(p1 >> 32) ^ x1 ^ k0, y1 = (uint32_t)p1;
+        const uint32_t y2 = (uint32_t)(p0 >> 32) ^ x3 ^ k1, y3 = (uint32_t)p0;
+        x0 = y0; x1 = y1; x2 = y2; x3 = y3;
+    }
+    out[0] = x0; out[1] = x1; out[2] = x2; out[3] = x3;
+}
+
+/* Two standard normals for cell k at time_loop iteration t. */
+void orc_thermal_normals(uint64_t seed, uint64_t k, int64_t t, double *zx, double *zy) {
+    const uint32_t ctr[4] = {(uint32_t)k, (uint32_t)(uint64_t)t, (uint32_t)((uint64_t)t >> 32),
+                             (uint32_t)(k >> 32)};
+    const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+    uint32_t w[4];
+    orc_philox4x32_10(ctr, key, w);
+    const double u1 = (double)((((uint64_t)w[0] << 32) | w[1]) >> 11) * 0x1p-53 + 0x1p-54;
+    const double u2 = (double)((((uint64_t)w[2] << 32) | w[3]) >> 11) * 0x1p-53;
+    const double r = sqrt(-2.0 * log(u1));
+    *zx = r * cos(6.283185307179586 * u2);
+    *zy = r * sin(6.283185307179586 * u2);
+}
+
+/* thermal!(fx, fy, h, kbt, mu, delta) with the noise of iteration t. */
+void orc_thermal(double *fx, double *fy, const double *h, size_t N, double kbt, double mu,
+                 double delta, uint64_t seed, int64_t t) {
+    for (size_t k = 0; k < N; ++k) {
+        double zx, zy;
+        orc_thermal_normals(seed, k, t, &zx, &zy);
+        const double s = sqrt((((2.0 * kbt) * mu) * 6.0) * h[k] /
+                              (((2.0 * h[k]) * h[k] + (6.0 * h[k]) * delta) + (3.0 * delta) * delta));
+        fx[k] = zx * s;
+        fy[k] = zy * s;
+    }
+}
 
 /* Per-iteration outputs (each may be NULL): mass (only where t % tdump == 0,
  * NaN elsewhere), Δh, wetted count.  Index t-1 for loop iteration t. */
@@ -470,16 +539,36 @@ void orc_time_loop(orc_state *s, const orc_params *P, int Tmax, const orc_loop_o
                    orc_loop_out *out) {
     int Lx = s->Lx, Ly = s->Ly;
     size_t N = (size_t)Lx * Ly;
+    double *moved = (o->theta_field && o->shift_tmove > 0) ? malloc(N * sizeof(double)) : NULL;
     for (int t = 1; t <= Tmax; ++t) {
+        const double *theta_field = o->theta_field;
+        if (moved) {  /* the field as move_substrate! has left it */
+            int sx, sy;
+            field_shift(o, o->t_offset + t, Lx, Ly, &sx, &sy);
+            orc_circshift(moved, o->theta_field, Lx, Ly, sx, sy);
+            theta_field = moved;
+        }
         if (out && out->mass) out->mass[t - 1] = (P->tdump > 0 && t % P->tdump == 0)
                                                      ? orc_sum(s->height, N)
                                                      : NAN;
         if (o->record_dh && out && out->dh) out->dh[t - 1] = orc_dh(s->height, N);
-        orc_filmpressure(s->pressure, s->height, s->dgrad, Lx, Ly, P->gamma, o->theta_field,
+        orc_filmpressure(s->pressure, s->height, s->dgrad, Lx, Ly, P->gamma, theta_field,
                          o->theta, P->n, P->m, P->hmin, P->hcrit);
         orc_hgradp(s->hgx, s->hgy, s->height, s->pressure, s->dgrad, Lx, Ly);
         orc_slippage(s->slipx, s->slipy, s->height, s->velx, s->vely, N, P->delta, P->mu);
         orc_force_sum(s->Fx, s->Fy, s->hgx, s->hgy, s->slipx, s->slipy, N);
+        if (P->kbt > 0.0) {  /* Fx .= -h∇px .- slipx .- kbtx (scripts/Rivulet_stability.jl:123) */
+            for (size_t k = 0; k < N; ++k) {
+                double zx, zy;
+                orc_thermal_normals(o->thermal_seed, k, o->t_offset + t, &zx, &zy);
+                const double hk = s->height[k];
+                const double sg = sqrt((((2.0 * P->kbt) * P->mu) * 6.0) * hk /
+                                       (((2.0 * hk) * hk + (6.0 * hk) * P->delta) +
+                                        (3.0 * P->delta) * P->delta));
+                s->Fx[k] = s->Fx[k] - zx * sg;
+                s->Fy[k] = s->Fy[k] - zy * sg;
+            }
+        }
         if (o->callback == 1) {
             if (out && out->wet) out->wet[t - 1] = orc_wetted(s->height, N, o->hthresh);
         } else if (o->callback == 2) {
@@ -491,6 +580,7 @@ void orc_time_loop(orc_state *s, const orc_params *P, int Tmax, const orc_loop_o
         orc_bgk_stream(s->fout, s->feq, s->ftemp, s->Fx, s->Fy, Lx, Ly, P->tau);
         orc_moments(s->height, s->velx, s->vely, s->fout, N);
     }
+    free(moved);
 }
 
 /* ------------------------------------------------------------------ */
@@ -561,13 +651,17 @@ int orc_fused_run(const orc_params *P, double *fpost, double *fpost_tmp, double 
         if (o->record_dh && out && out->dh) out->dh[t - 1] = orc_dh(h, N);
         if (o->callback == 1 && out && out->wet) out->wet[t - 1] = orc_wetted(h, N, o->hthresh);
         /* pass 2: film pressure */
+        int fsx, fsy;
+        field_shift(o, o->t_offset + t, Lx, Ly, &fsx, &fsy);
 #pragma omp parallel for schedule(static)
         for (int j = 0; j < Ly; ++j)
             for (int i = 0; i < Lx; ++i) {
                 size_t k = IDX(i, j, Lx);
                 double v[9];
                 nb9(h, i, j, Lx, Ly, v);
-                double kap = o->theta_field ? kappa_field[k] : kap_s;
+                double kap = o->theta_field
+                                 ? kappa_field[IDX(wrapi(i - fsx, Lx), wrapi(j - fsy, Ly), Lx)]
+                                 : kap_s;
                 double x = P->hmin / (h[k] + P->hcrit);
                 double p = -P->gamma * (kap * (orc_power_broad(x, P->n) - orc_power_broad(x, P->m)));
                 double lap = (2.0 / 3.0) * (((v[1] + v[0]) + v[2]) + v[3]) +
@@ -594,6 +688,15 @@ int orc_fused_run(const orc_params *P, double *fpost, double *fpost_tmp, double 
                 double sx = ((6.0 * P->mu) * hk * ux[k]) / den;
                 double sy = ((6.0 * P->mu) * hk * uy[k]) / den;
                 double Fx = -hgx - sx, Fy = -hgy - sy;
+                if (P->kbt > 0.0) {
+                    double zx, zy;
+                    orc_thermal_normals(o->thermal_seed, k, o->t_offset + t, &zx, &zy);
+                    const double sg = sqrt((((2.0 * P->kbt) * P->mu) * 6.0) * hk /
+                                           (((2.0 * hk) * hk + (6.0 * hk) * P->delta) +
+                                            (3.0 * P->delta) * P->delta));
+                    Fx = Fx - zx * sg;
+                    Fy = Fy - zy * sg;
+                }
                 if (o->callback == 2) {
                     Fx = Fx + (hk * o->incl_ax) * sfac;
                     Fy = Fy + (hk * o->incl_ay) * sfac;

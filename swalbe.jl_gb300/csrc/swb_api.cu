@@ -91,8 +91,7 @@ int check_params(const swb_params *p, std::string *slot) {
     if (!(p->tau > 0.0)) return fail(slot, SWB_ERR_ARG, "tau must be > 0");
     if (p->n <= p->m || p->m < 1) return fail(slot, SWB_ERR_ARG, "need n > m >= 1");
     if (!(p->hmin > 0.0)) return fail(slot, SWB_ERR_ARG, "hmin must be > 0");
-    if (p->kbt != 0.0)
-        return fail(slot, SWB_ERR_UNSUPPORTED, "thermal fluctuations (kbt != 0) are not supported");
+    if (!(p->kbt >= 0.0)) return fail(slot, SWB_ERR_ARG, "kbt must be >= 0");
     return SWB_OK;
 }
 
@@ -115,6 +114,8 @@ void fill_args_from_params(StepArgs &a, const swb_params &p) {
     a.kap = host_kappa(p.theta, p.n, p.m, p.hmin);
     a.cos_theta = host_cospi(p.theta);
     a.hthresh = 0.055;
+    a.thermal = p.kbt > 0.0 ? 1 : 0;
+    a.k6 = ((2.0 * p.kbt) * p.mu) * 6.0;  // src/forcing.jl:300-302, left to right
 }
 
 __global__ void fill_kernel(double *d, long long n, double v) {
@@ -184,6 +185,13 @@ cudaError_t launch_moments(int precision, const StepArgs &a, cudaStream_t st) {
 cudaError_t launch_fout(int precision, const StepArgs &a, double *out, cudaStream_t st) {
     count_launches(1);
     return precision == SWB_F64 ? launch_fout_f64(a, out, st) : launch_fout_f32(precision, a, out, st);
+}
+cudaError_t launch_thermal_field(int precision, const StepArgs &a, long long t, double *fx,
+                                 double *fy, cudaStream_t st) {
+    count_launches(1);
+    return precision == SWB_F32 || precision == SWB_F16
+               ? launch_thermal_field_f32(precision, a, t, fx, fy, st)
+               : launch_thermal_field_f64(a, t, fx, fy, st);
 }
 cudaError_t launch_pressure_now(int precision, const StepArgs &a, double *out, cudaStream_t st) {
     count_launches(1);
@@ -397,11 +405,16 @@ int plain_iteration(swb_state *s) {
         s->plain_rec_head++;
     }
     const bool field = s->a.theta_mode == swb::THETA_FIELD;
+    int sx = 0, sy = 0;
+    swb::substrate_shift(s->a, t, &sx, &sy);
     CUDA_TRY(&s->err, swb::plain_filmpressure(ps, field ? s->plain_kapF : nullptr, s->a.kap,
-                                              p.gamma, p.n, p.m, p.hmin, p.hcrit, s->stream));
+                                              p.gamma, p.n, p.m, p.hmin, p.hcrit, sx, sy,
+                                              s->stream));
     CUDA_TRY(&s->err, swb::plain_hgradp(ps, s->stream));
     CUDA_TRY(&s->err, swb::plain_slippage(ps, p.delta, p.mu, s->stream));
     CUDA_TRY(&s->err, swb::plain_force_sum(ps, s->stream));
+    if (s->a.thermal)
+        CUDA_TRY(&s->err, swb::plain_thermal(ps, s->a.k6, p.delta, s->a.seed, t, s->stream));
     if (s->incl) {
         const double fac = incl_factor(s->incl_loop_time ? t : s->incl_t, s->incl_tstart,
                                        s->incl_tsmooth);
@@ -917,6 +930,7 @@ int swb_set_theta(swb_state *s, double theta) {
     if (s->a.theta_mode == swb::THETA_SCALAR && s->p.theta == theta) return SWB_OK;
     s->p.theta = theta;
     s->a.theta_mode = swb::THETA_SCALAR;
+    s->a.shift_tmove = 0;
     s->a.kap = host_kappa(theta, s->p.n, s->p.m, s->p.hmin);
     s->a.cos_theta = host_cospi(theta);
     s->invalidate_graph();
@@ -951,6 +965,22 @@ int swb_set_theta_field(swb_state *s, const double *theta) {
         if (rc) return rc;
     }
     a.theta_mode = swb::THETA_FIELD;
+    a.shift_tmove = 0;  // a new field starts at rest
+    s->invalidate_graph();
+    return SWB_OK;
+}
+
+int swb_set_substrate_motion(swb_state *s, int64_t tmove, int dx, int dy) {
+    if (!s) return fail(nullptr, SWB_ERR_ARG, "state is NULL");
+    if (tmove < 0 || dx < 0 || dy < 0 || tmove > (int64_t)INT32_MAX)
+        return fail(&s->err, SWB_ERR_ARG, "substrate motion: tmove, dx, dy must be >= 0");
+    if (tmove > 0 && s->a.theta_mode != swb::THETA_FIELD)
+        return fail(&s->err, SWB_ERR_UNSUPPORTED, "substrate motion moves a θ field: set one first");
+    CUDA_TRY(&s->err, cudaStreamSynchronize(s->stream));
+    s->a.shift_tmove = (int)tmove;
+    s->a.shift_dx = dx % s->p.Lx;
+    s->a.shift_dy = dy % s->p.Ly;
+    s->a.shift_t0 = s->steps;
     s->invalidate_graph();
     return SWB_OK;
 }
@@ -959,6 +989,7 @@ int swb_set_theta_wave(swb_state *s, double theta0, double dtheta, double v) {
     if (!s) return fail(nullptr, SWB_ERR_ARG, "state is NULL");
     if (s->plain()) return fail(&s->err, SWB_ERR_UNSUPPORTED, "moving wettability needs a fused mode");
     s->a.theta_mode = swb::THETA_WAVE;
+    s->a.shift_tmove = 0;
     s->a.theta0 = theta0;
     s->a.dtheta = dtheta;
     s->a.wave_v = v;
@@ -1146,6 +1177,35 @@ int swb_measure_now(swb_state *s, double hthresh, swb_measure *out) {
     return SWB_OK;
 }
 
+int swb_set_thermal_seed(swb_state *s, uint64_t seed) {
+    if (!s) return fail(nullptr, SWB_ERR_ARG, "state is NULL");
+    if (s->a.seed != seed) {
+        CUDA_TRY(&s->err, cudaStreamSynchronize(s->stream));
+        s->a.seed = seed;
+        s->invalidate_graph();
+    }
+    return SWB_OK;
+}
+
+int swb_thermal_field(swb_state *s, int64_t t, double *fx, double *fy) {
+    if (!s || !fx || !fy) return fail(s ? &s->err : nullptr, SWB_ERR_ARG, "NULL argument");
+    int rc = materialize(s);
+    if (rc) return rc;
+    rc = ensure_tmp(s, (size_t)2 * s->N * 8);
+    if (rc) return rc;
+    StepArgs a = s->a;
+    int prec = s->precision;
+    if (s->plain()) {
+        a.hF = s->ps.h;
+        prec = SWB_F64;
+    }
+    CUDA_TRY(&s->err, swb::launch_thermal_field(prec, a, t, s->dtmp, s->dtmp + s->N, s->stream));
+    CUDA_TRY(&s->err, cudaMemcpyAsync(fx, s->dtmp, s->N * 8, cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(&s->err, cudaMemcpyAsync(fy, s->dtmp + s->N, s->N * 8, cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(&s->err, cudaStreamSynchronize(s->stream));
+    return SWB_OK;
+}
+
 int swb_set_field_device(swb_state *s, int field, const double *dptr) {
     if (!s || !dptr) return fail(s ? &s->err : nullptr, SWB_ERR_ARG, "NULL argument");
     if (field != SWB_FIELD_HEIGHT && field != SWB_FIELD_VELX && field != SWB_FIELD_VELY)
@@ -1205,7 +1265,7 @@ int swb_op_filmpressure(swb_state *s) {
     const bool field = s->a.theta_mode == swb::THETA_FIELD;
     CUDA_TRY(&s->err, swb::plain_filmpressure(s->ps, field ? s->plain_kapF : nullptr, s->a.kap,
                                               s->p.gamma, s->p.n, s->p.m, s->p.hmin, s->p.hcrit,
-                                              s->stream));
+                                              0, 0, s->stream));
     return SWB_OK;
 }
 int swb_op_hgradp(swb_state *s) {
@@ -1221,6 +1281,12 @@ int swb_op_slippage(swb_state *s) {
 int swb_op_force_sum(swb_state *s) {
     PLAIN_ONLY(s);
     CUDA_TRY(&s->err, swb::plain_force_sum(s->ps, s->stream));
+    return SWB_OK;
+}
+int swb_op_thermal(swb_state *s, int64_t t) {
+    PLAIN_ONLY(s);
+    if (!s->a.thermal) return SWB_OK;
+    CUDA_TRY(&s->err, swb::plain_thermal(s->ps, s->a.k6, s->p.delta, s->a.seed, t, s->stream));
     return SWB_OK;
 }
 int swb_op_inclination(swb_state *s, double ax, double ay, int64_t t, int64_t tstart,

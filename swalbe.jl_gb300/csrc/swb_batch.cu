@@ -158,6 +158,7 @@ struct swb_batch {
     cudaGraphExec_t gexec = nullptr;
     int steps_per_graph = 32;
     int grid = 0;
+    int nt = swb::kBatchNT, rows = swb::kBatchRows;  // strip geometry of every lattice
     bool tuned = false, args_dirty = true, gvalid = false;
     long long steps = 0;
     std::string err;
@@ -189,6 +190,19 @@ struct swb_batch {
 
 namespace {
 
+// Packed table of (lattice, strip) entries, the lattices' reducers first.
+std::vector<TileRef> build_tiles(const std::vector<StepArgs> &args) {
+    std::vector<TileRef> tiles, reducers;
+    for (int i = 0; i < (int)args.size(); ++i) {
+        const StepArgs &a = args[i];
+        if (swb::needs_partials(a)) reducers.push_back({i, -1, 0});
+        for (int ty = 0; ty < a.tiles_y; ++ty)
+            for (int tx = 0; tx < a.tiles_x; ++tx) tiles.push_back({i, tx, ty});
+    }
+    tiles.insert(tiles.begin(), reducers.begin(), reducers.end());
+    return tiles;
+}
+
 int upload_args(swb_batch *b) {
     if (!b->args_dirty) return SWB_OK;
     B_TRY(b, cudaMemcpyAsync(b->d_args, b->args.data(), b->args.size() * sizeof(StepArgs),
@@ -203,7 +217,7 @@ int upload_args(swb_batch *b) {
 cudaError_t batch_sequence(swb_batch *b, int n, int grid) {
     cudaError_t e = cudaSuccess;
     for (int k = 0; k < n && e == cudaSuccess; ++k)
-        e = swb::launch_batch_step(b->precision, swb::kBatchNT, b->d_args, b->d_tiles, b->ntiles,
+        e = swb::launch_batch_step(b->precision, b->nt, b->d_args, b->d_tiles, b->ntiles,
                                    grid, k, b->stream);
     if (e == cudaSuccess && n > 0) e = swb::launch_batch_advance(b->d_args, b->count, n, b->stream);
     return e;
@@ -219,7 +233,7 @@ int autotune(swb_batch *b, long long &left) {
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int occ = swb::batch_blocks_per_sm(b->precision, swb::kBatchNT);
+    const int occ = swb::batch_blocks_per_sm(b->precision, b->nt);
     std::vector<int> cands = {b->ntiles};
     for (int k = 1; k <= occ; ++k) cands.push_back(std::min(b->ntiles, sms * k));
     std::sort(cands.begin(), cands.end());
@@ -273,7 +287,7 @@ int swb_batch_create(const swb_params *params, int count, int precision, swb_bat
         if (p.Lx < 1 || p.Ly < 1 || 9LL * (((long long)p.Lx * p.Ly + 63) / 64 * 64) >= (1LL << 31) || !(p.tau > 0) ||
             p.n <= p.m || p.m < 1 || !(p.hmin > 0))
             return swb::bfail(nullptr, SWB_ERR_ARG, "invalid params for lattice " + std::to_string(i));
-        if (p.kbt != 0.0) return swb::bfail(nullptr, SWB_ERR_UNSUPPORTED, "kbt != 0 is not supported");
+        if (!(p.kbt >= 0.0)) return swb::bfail(nullptr, SWB_ERR_ARG, "kbt must be >= 0");
     }
     swb_batch *b = new swb_batch();
     b->count = count;
@@ -308,16 +322,14 @@ int swb_batch_create(const swb_params *params, int count, int precision, swb_bat
     b->slab_bytes = off;
     BC_TRY(cudaMalloc((void **)&b->slab, off));
     BC_TRY(cudaMalloc((void **)&b->staging, (size_t)maxN * 8));
-    std::vector<TileRef> tiles, reducers;
     for (int i = 0; i < count; ++i) {
-        StepArgs a = swb::lattice_args(params[i], precision, b->slab + offs[i], b->layouts[i]);
+        StepArgs a = swb::lattice_args(params[i], precision, b->slab + offs[i], b->layouts[i],
+                                       b->nt, b->rows);
+        a.seed = (unsigned long long)i;  // thermal noise stream of lattice i
         b->args.push_back(a);
         BC_TRY(swb::lattice_init(a, precision, b->layouts[i], nullptr, b->stream));
-        if (swb::needs_partials(a)) reducers.push_back({i, -1, 0});
-        for (int ty = 0; ty < a.tiles_y; ++ty)
-            for (int tx = 0; tx < a.tiles_x; ++tx) tiles.push_back({i, tx, ty});
     }
-    tiles.insert(tiles.begin(), reducers.begin(), reducers.end());
+    const std::vector<TileRef> tiles = build_tiles(b->args);
     b->fields_current.assign(count, 1);
     b->ntiles = (int)tiles.size();
     BC_TRY(cudaMalloc((void **)&b->d_args, sizeof(StepArgs) * count));
@@ -418,10 +430,37 @@ int swb_batch_sync(swb_batch *b) {
     return SWB_OK;
 }
 
+int swb_batch_set_geometry(swb_batch *b, int nt, int rows) {
+    if (!b || (nt != 64 && nt != 128 && nt != 256) || rows < swb::kMinRows || rows > swb::kMaxRows)
+        return swb::bfail(b ? &b->err : nullptr, SWB_ERR_ARG,
+                          "batch geometry: nt must be 64, 128 or 256 and 4 <= rows <= 512");
+    B_TRY(b, cudaStreamSynchronize(b->stream));
+    b->nt = nt;
+    b->rows = rows;
+    for (int i = 0; i < b->count; ++i) {
+        int h = rows < b->params[i].Ly ? rows : b->params[i].Ly;
+        if (h < swb::kMinRows) h = swb::kMinRows;
+        swb::set_geometry(b->args[i], nt, h);
+    }
+    const std::vector<TileRef> tiles = build_tiles(b->args);
+    if ((int)tiles.size() > b->ntiles) {
+        cudaFree(b->d_tiles);
+        b->d_tiles = nullptr;
+        B_TRY(b, cudaMalloc((void **)&b->d_tiles, sizeof(TileRef) * tiles.size()));
+    }
+    B_TRY(b, cudaMemcpy(b->d_tiles, tiles.data(), sizeof(TileRef) * tiles.size(),
+                        cudaMemcpyHostToDevice));
+    b->ntiles = (int)tiles.size();
+    b->args_dirty = true;
+    b->tuned = false;  // re-pick the CTA count
+    b->invalidate();
+    return SWB_OK;
+}
+
 int swb_batch_tile(swb_batch *b, int *tile_x, int *tile_y, int *steps_per_graph) {
     if (!b) return swb::bfail(nullptr, SWB_ERR_ARG, "batch is NULL");
-    if (tile_x) *tile_x = b->tuned ? swb::kBatchNT - 4 : 0;
-    if (tile_y) *tile_y = b->tuned ? b->args[0].march_h : 0;
+    if (tile_x) *tile_x = b->tuned ? b->nt - 4 : 0;
+    if (tile_y) *tile_y = b->tuned ? b->rows : 0;
     if (steps_per_graph) *steps_per_graph = b->tuned ? b->steps_per_graph : 0;
     return SWB_OK;
 }

@@ -18,8 +18,9 @@ inline long long max_tiles(int Lx, int Ly) {  // per parity slot: strips or 2D t
     const long long tiles = (long long)((Lx + 31) / 32) * ((Ly + 15) / 16);
     return strips > tiles ? strips : tiles;
 }
-// CTA width of batched and served lattices (all share one launch).
-constexpr int kBatchNT = 128;
+// CTA width of batched and served lattices (all share one launch; 64 was
+// the fastest on GB300 for the 128^2..1024x256 ensemble).
+constexpr int kBatchNT = 64;
 // Default geometry for a lattice.  *nt on entry: 0 to choose the width too,
 // or a width (64, 128, 256) to keep; *h: rows per strip.
 void default_geometry(int Lx, int Ly, int precision, int *nt, int *h);
@@ -87,7 +88,27 @@ struct StepArgs {
     int march_nt, march_h;    // threads per CTA (strip width + 4) and rows per strip,
                               // or kTileGeom and kT2Y rows: 2D tiles of 32 x 16 cells
     unsigned int *bar;        // grid-barrier words of the multi-step kernel (kBarWords)
+    int thermal;              // kbt > 0: thermal! forces (src/forcing.jl:297-320)
+    double k6;                // ((2 kbt) mu) 6, the numerator's constant factor
+    unsigned long long seed;  // noise stream: Philox key
+    // moving substrate (θ field mode): the field moves by (shift_dx, shift_dy)
+    // cells after every shift_tmove iterations counted from shift_t0
+    long long shift_t0;
+    int shift_tmove, shift_dx, shift_dy;
 };
+
+// Offset of the moving θ field at iteration t (1-based): it has moved
+// k = (t - 1 - t0) / tmove times (move_substrate! runs at the end of every
+// tmove-th iteration, scripts/Moving_wettability_structs.jl:139-152), and
+// circshift by (dx, dy) means field(i, j) = original(i - k dx, j - k dy).
+__host__ __device__ inline void substrate_shift(const StepArgs &a, long long t, int *sx, int *sy) {
+    *sx = 0;
+    *sy = 0;
+    if (a.shift_tmove <= 0 || t - 1 - a.shift_t0 < a.shift_tmove) return;
+    const long long k = (t - 1 - a.shift_t0) / a.shift_tmove;
+    *sx = (int)((k % a.Lx) * a.shift_dx % a.Lx);
+    *sy = (int)((k % a.Ly) * a.shift_dy % a.Ly);
+}
 
 // Geometry value of the 2D-tile form: CTAs of 256 threads own 32 x 16 cells.
 constexpr int kTileGeom = 32;
@@ -148,6 +169,13 @@ constexpr unsigned int kBarWords = kBarStride * (1 + 2 * kBarGroups);
 cudaError_t launch_moments(int precision, const StepArgs &a, cudaStream_t st);
 cudaError_t launch_fout(int precision, const StepArgs &a, double *out, cudaStream_t st);
 cudaError_t launch_pressure_now(int precision, const StepArgs &a, double *out, cudaStream_t st);
+// thermal! forces of the current height field for iteration t (fx, fy: N doubles).
+cudaError_t launch_thermal_field(int precision, const StepArgs &a, long long t, double *fx,
+                                 double *fy, cudaStream_t st);
+cudaError_t launch_thermal_field_f64(const StepArgs &a, long long t, double *fx, double *fy,
+                                     cudaStream_t st);
+cudaError_t launch_thermal_field_f32(int precision, const StepArgs &a, long long t, double *fx,
+                                     double *fy, cudaStream_t st);
 cudaError_t launch_batch_step(int precision, int nt, const StepArgs *d_args,
                               const TileRef *d_tiles, int ntiles, int grid, int k,
                               cudaStream_t st);
@@ -177,10 +205,13 @@ struct PlainState {
     double *h, *ux, *uy, *vsq, *p, *Fx, *Fy, *sx, *sy, *hgx, *hgy;
 };
 cudaError_t plain_filmpressure(const PlainState &s, const double *kapF, double kap, double gamma,
-                               int n, int m, double hmin, double hcrit, cudaStream_t st);
+                               int n, int m, double hmin, double hcrit, int sx, int sy,
+                               cudaStream_t st);
 cudaError_t plain_hgradp(const PlainState &s, cudaStream_t st);
 cudaError_t plain_slippage(const PlainState &s, double delta, double mu, cudaStream_t st);
 cudaError_t plain_force_sum(const PlainState &s, cudaStream_t st);
+cudaError_t plain_thermal(const PlainState &s, double k6, double delta, unsigned long long seed,
+                          long long t, cudaStream_t st);
 cudaError_t plain_inclination(const PlainState &s, double ax, double ay, double fac,
                               cudaStream_t st);
 cudaError_t plain_equilibrium(const PlainState &s, double g, cudaStream_t st);

@@ -48,8 +48,15 @@ inline LatticeLayout lattice_layout(const swb_params &p, int precision) {
     return L;
 }
 
-// Step arguments of a lattice whose buffers start at `base`.
-inline StepArgs lattice_args(const swb_params &p, int precision, char *base, const LatticeLayout &L) {
+// Strip rows of batched and served lattices: the batch has parallelism from
+// its many lattices, so strips can be tall (fewer halo rows re-pulled; on
+// GB300 the ensemble ran 26 GLUPS at 124x4 strips, 45 GLUPS at 60x32).
+constexpr int kBatchRows = 32;
+
+// Step arguments of a lattice whose buffers start at `base`; strips of
+// nt threads and `rows` rows (capped at the lattice height).
+inline StepArgs lattice_args(const swb_params &p, int precision, char *base, const LatticeLayout &L,
+                             int nt = kBatchNT, int rows = kBatchRows) {
     StepArgs a{};
     a.Lx = p.Lx;
     a.Ly = p.Ly;
@@ -76,10 +83,13 @@ inline StepArgs lattice_args(const swb_params &p, int precision, char *base, con
     a.theta_mode = THETA_SCALAR;
     a.kap = host_kappa_shared(p.theta, p.n, p.m, p.hmin);
     a.cos_theta = host_cospi_shared(p.theta);
-    int nt = kBatchNT, h;  // one CTA width serves every lattice of a batch
-    default_geometry(p.Lx, p.Ly, precision, &nt, &h);
+    int h = rows < p.Ly ? rows : p.Ly;  // one CTA width serves every lattice of a batch
+    if (h < kMinRows) h = kMinRows;
     set_geometry(a, nt, h);
     a.hthresh = 0.055;
+    a.thermal = p.kbt > 0.0 ? 1 : 0;
+    a.k6 = ((2.0 * p.kbt) * p.mu) * 6.0;  // src/forcing.jl:300-302, left to right
+    a.seed = 0;
     a.mass_corr = (precision == SWB_F16) ? 1 : 0;
     a.records = nullptr;
     a.rec_cap = 0;

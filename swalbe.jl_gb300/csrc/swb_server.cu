@@ -108,6 +108,7 @@ bool admit_device(swb_server *sv, Req *r) {
         return false;
     }
     r->a = swb::lattice_args(r->p, sv->precision, r->dev, r->L);
+    r->a.seed = (unsigned long long)r->id;  // thermal noise stream of this request
     swb::set_wave(r->a, r->theta0, r->dtheta, r->v);
     const long long N = (long long)r->p.Lx * r->p.Ly;
     if ((size_t)N > sv->staging_elems) {
@@ -364,7 +365,7 @@ int swb_server_submit(swb_server *sv, const swb_params *p, const double *h0, dou
     if (p->Lx < 1 || p->Ly < 1 || 9LL * (((long long)p->Lx * p->Ly + 63) / 64 * 64) >= (1LL << 31) || !(p->tau > 0) ||
         p->n <= p->m || p->m < 1 || !(p->hmin > 0))
         return sfail(SWB_ERR_ARG, "invalid params");
-    if (p->kbt != 0.0) return sfail(SWB_ERR_UNSUPPORTED, "kbt != 0 is not supported");
+    if (!(p->kbt >= 0.0)) return sfail(SWB_ERR_ARG, "kbt must be >= 0");
     const double work = (double)p->Lx * p->Ly * (double)nsteps;
     {
         std::lock_guard<std::mutex> g(sv->mu);

@@ -62,6 +62,13 @@ cudaError_t launch_fout_f32(int precision, const StepArgs &a, double *out, cudaS
     return cudaGetLastError();
 }
 
+cudaError_t launch_thermal_field_f32(int precision, const StepArgs &a, long long t, double *fx,
+                                     double *fy, cudaStream_t st) {
+    const int g = grid_for((long long)a.Lx * a.Ly, 256);
+    DISPATCH_STORE(precision, (thermal_field_kernel<S><<<g, 256, 0, st>>>(a, t, fx, fy)));
+    return cudaGetLastError();
+}
+
 cudaError_t launch_pressure_now_f32(int precision, const StepArgs &a, double *out,
                                     cudaStream_t st) {
     const int g = grid_for((long long)a.Lx * a.Ly, 256);

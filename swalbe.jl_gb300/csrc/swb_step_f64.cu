@@ -57,6 +57,12 @@ cudaError_t launch_fout_f64(const StepArgs &a, double *out, cudaStream_t st) {
     return cudaGetLastError();
 }
 
+cudaError_t launch_thermal_field_f64(const StepArgs &a, long long t, double *fx, double *fy,
+                                     cudaStream_t st) {
+    thermal_field_kernel<StoreF64><<<grid_for((long long)a.Lx * a.Ly, 256), 256, 0, st>>>(a, t, fx, fy);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_pressure_now_f64(const StepArgs &a, double *out, cudaStream_t st) {
     pressure_now_kernel<StoreF64><<<grid_for((long long)a.Lx * a.Ly, 256), 256, 0, st>>>(a, out);
     return cudaGetLastError();
@@ -101,14 +107,22 @@ __device__ __forceinline__ Nb neighbours(long long c, int Lx, int Ly) {
     return n;
 }
 
+// (sx, sy): offset of a moving θ field (0 for a fixed one)
 __global__ void k_filmpressure(PlainState s, const double *kapF, double kap, double gamma, int n,
-                               int m, double hmin, double hcrit) {
+                               int m, double hmin, double hcrit, int sx, int sy) {
     PLAIN_LOOP(s) {
         const Nb b = neighbours(c, s.Lx, s.Ly);
         const double *h = s.h;
+        double k = kap;
+        if (kapF) {
+            int i = (int)(c % s.Lx) - sx, j = (int)(c / s.Lx) - sy;
+            if (i < 0) i += s.Lx;
+            if (j < 0) j += s.Ly;
+            k = kapF[(long long)j * s.Lx + i];
+        }
         s.p[c] = pressure_cell<true, double>(h[c], h[b.ip], h[b.jp], h[b.im], h[b.jm], h[b.ipjp],
-                                             h[b.imjp], h[b.imjm], h[b.ipjm],
-                                             kapF ? kapF[c] : kap, gamma, hmin, hcrit, n, m);
+                                             h[b.imjp], h[b.imjm], h[b.ipjm], k, gamma, hmin,
+                                             hcrit, n, m);
     }
 }
 
@@ -136,6 +150,19 @@ __global__ void k_force_sum(PlainState s) {
     PLAIN_LOOP(s) {
         s.Fx[c] = -s.hgx[c] - s.sx[c];
         s.Fy[c] = -s.hgy[c] - s.sy[c];
+    }
+}
+
+// Fx .-= kbtx, Fy .-= kbty with thermal!'s forces of iteration t
+// (src/forcing.jl:297-311; the force sum of scripts/Rivulet_stability.jl:123).
+__global__ void k_thermal(PlainState s, double k6, double delta, unsigned long long seed,
+                          long long t) {
+    PLAIN_LOOP(s) {
+        double zx, zy;
+        thermal_normals(seed, c, t, zx, zy);
+        const double sg = thermal_sigma<true, double>(k6, s.h[c], delta);
+        s.Fx[c] = s.Fx[c] - zx * sg;
+        s.Fy[c] = s.Fy[c] - zy * sg;
     }
 }
 
@@ -199,8 +226,9 @@ __global__ void k_moments(PlainState s) {
     } while (0)
 
 cudaError_t plain_filmpressure(const PlainState &s, const double *kapF, double kap, double gamma,
-                               int n, int m, double hmin, double hcrit, cudaStream_t st) {
-    PLAIN_LAUNCH(k_filmpressure, s, st, kapF, kap, gamma, n, m, hmin, hcrit);
+                               int n, int m, double hmin, double hcrit, int sx, int sy,
+                               cudaStream_t st) {
+    PLAIN_LAUNCH(k_filmpressure, s, st, kapF, kap, gamma, n, m, hmin, hcrit, sx, sy);
 }
 cudaError_t plain_hgradp(const PlainState &s, cudaStream_t st) { PLAIN_LAUNCH(k_hgradp, s, st); }
 cudaError_t plain_slippage(const PlainState &s, double delta, double mu, cudaStream_t st) {
@@ -208,6 +236,10 @@ cudaError_t plain_slippage(const PlainState &s, double delta, double mu, cudaStr
 }
 cudaError_t plain_force_sum(const PlainState &s, cudaStream_t st) {
     PLAIN_LAUNCH(k_force_sum, s, st);
+}
+cudaError_t plain_thermal(const PlainState &s, double k6, double delta, unsigned long long seed,
+                          long long t, cudaStream_t st) {
+    PLAIN_LAUNCH(k_thermal, s, st, k6, delta, seed, t);
 }
 cudaError_t plain_inclination(const PlainState &s, double ax, double ay, double fac,
                               cudaStream_t st) {

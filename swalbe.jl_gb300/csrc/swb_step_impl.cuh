@@ -488,6 +488,67 @@ __device__ void reduce_step(const StepArgs &a, long long s, PartT<double> *redd)
     }
 }
 
+// ------------------------------------------------------------ thermal noise
+// thermal! (src/forcing.jl:297-320) draws two standard normals per cell and
+// iteration.  They come from Philox-4x32-10 (Salmon et al., SC'11; the same
+// generator as the oracle) with key = seed and counter = (cell, t), and the
+// Box-Muller transform: Float64 in the literal mode, FP32 otherwise.
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        if (r) {
+            k.x += 0x9E3779B9u;
+            k.y += 0xBB67AE85u;
+        }
+        const unsigned int hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+        const unsigned int hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+        c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+    }
+    return c;
+}
+
+__device__ __forceinline__ uint4 thermal_bits(unsigned long long seed, long long cell,
+                                              long long t) {
+    const unsigned long long k = (unsigned long long)cell, tu = (unsigned long long)t;
+    return philox4x32_10(make_uint4((unsigned)k, (unsigned)tu, (unsigned)(tu >> 32),
+                                    (unsigned)(k >> 32)),
+                         make_uint2((unsigned)seed, (unsigned)(seed >> 32)));
+}
+
+__device__ __forceinline__ void thermal_normals(unsigned long long seed, long long cell,
+                                                long long t, double &zx, double &zy) {
+    const uint4 w = thermal_bits(seed, cell, t);
+    const double u1 =
+        (double)(((((unsigned long long)w.x) << 32) | w.y) >> 11) * 0x1p-53 + 0x1p-54;
+    const double u2 = (double)(((((unsigned long long)w.z) << 32) | w.w) >> 11) * 0x1p-53;
+    const double r = sqrt(-2.0 * log(u1));
+    zx = r * cos(6.283185307179586 * u2);
+    zy = r * sin(6.283185307179586 * u2);
+}
+
+__device__ __forceinline__ void thermal_normals(unsigned long long seed, long long cell,
+                                                long long t, float &zx, float &zy) {
+    const uint4 w = thermal_bits(seed, cell, t);
+    const float u1 = (float)(w.x >> 8) * 0x1p-24f + 0x1p-25f;
+    const float u2 = (float)(w.z >> 8) * 0x1p-24f;
+    const float r = sqrtf(-2.0f * logf(u1));
+    float sn, cs;
+    sincospif(2.0f * u2, &sn, &cs);
+    zx = r * cs;
+    zy = r * sn;
+}
+
+// Standard deviation of the thermal force at height h:
+// sqrt(2 kbt mu 6 h / (2h^2 + 6 h delta + 3 delta^2)), in the reference's order.
+template <bool LIT, class R>
+__device__ __forceinline__ R thermal_sigma(R k6, R h, R delta) {
+    if constexpr (LIT)
+        return sqrt(k6 * h / (((R(2) * h) * h + (R(6) * h) * delta) + (R(3) * delta) * delta));
+    else
+        return sqrtf(qdiv(k6 * h, __fmaf_rn(__fmaf_rn(R(2), h, R(6) * delta), h,
+                                             (R(3) * delta) * delta)));
+}
+
 // Per-tile constants of the force and collision stage.
 template <class R>
 struct CellConst {
@@ -542,6 +603,13 @@ __device__ __forceinline__ void collide_cell(const StepArgs &a,
         const R sy = (cc.mu6 * h * uy) / den;
         Fx = -hgx - sx;
         Fy = -hgy - sy;
+        if (a.thermal) {  // Fx .= -h∇px .- slipx .- kbtx (scripts/Rivulet_stability.jl:123)
+            R zx, zy;
+            thermal_normals(a.seed, (long long)cell, tt, zx, zy);
+            const R sg = thermal_sigma<true, R>(R(a.k6), h, R(a.delta));
+            Fx = Fx - zx * sg;
+            Fy = Fy - zy * sg;
+        }
         if (a.incl) {  // inclination! (src/forcing.jl:364-365)
             Fx = Fx + (h * R(a.ax)) * cc.incl_fac;
             Fy = Fy + (h * R(a.ay)) * cc.incl_fac;
@@ -550,6 +618,13 @@ __device__ __forceinline__ void collide_cell(const StepArgs &a,
         const R c = qdiv(cc.mu6 * h, __fmaf_rn(__fmaf_rn(R(2), h, cc.delta6), h, cc.delta3sq));
         Fx = __fmaf_rn(-h, gpx, -(c * ux));
         Fy = __fmaf_rn(-h, gpy, -(c * uy));
+        if (a.thermal) {
+            R zx, zy;
+            thermal_normals(a.seed, (long long)cell, tt, zx, zy);
+            const R sg = thermal_sigma<false, R>(R(a.k6), h, R(a.delta));
+            Fx = __fmaf_rn(-zx, sg, Fx);
+            Fy = __fmaf_rn(-zy, sg, Fy);
+        }
         if (a.incl) {
             Fx = __fmaf_rn(h * R(a.ax), cc.incl_fac, Fx);
             Fy = __fmaf_rn(h * R(a.ay), cc.incl_fac, Fy);
@@ -671,6 +746,11 @@ __device__ __forceinline__ void march_run(const StepArgs &a, int bx, int by, lon
     // kappa and cospi(θ) of this column: constant (scalar θ) or θ(x, t) of
     // the moving-wettability mode, which depends on x only
     const int mode = a.theta_mode;
+    // θ field: column of this thread and row offset in the (possibly moving) field
+    int fsx = 0, fsy = 0;
+    if (mode == THETA_FIELD) substrate_shift(a, tt, &fsx, &fsy);
+    const int gxf = fsx ? (gx - fsx < 0 ? gx - fsx + Lx : gx - fsx) : gx;
+    auto frow = [&](int gyy) { return fsy ? (gyy - fsy < 0 ? gyy - fsy + Ly : gyy - fsy) : gyy; };
     R kap_col = R(a.kap), cos_col = R(a.cos_theta);
     if (mode == THETA_WAVE) {
         const R th = R(a.theta0) + R(a.dtheta) * sinpi_r(R(2) * (R(gx) - R(a.wave_v) * R(tt)) / R(Lx));
@@ -707,7 +787,7 @@ __device__ __forceinline__ void march_run(const StepArgs &a, int bx, int by, lon
         const int r = yy - y0 + 2;  // >= 1
         const R *hm = sm.h[(r + 7) & 7], *hc = sm.h[r & 7], *hp = sm.h[(r + 1) & 7];
         const R kap = mode == THETA_FIELD
-                          ? reinterpret_cast<const R *>(a.kapF)[wrow(yy) * Lx + gx]
+                          ? reinterpret_cast<const R *>(a.kapF)[frow(wrow(yy)) * Lx + gxf]
                           : kap_col;
         // ip = h[i-1,j], jp = h[i,j-1], im = h[i+1,j], jm = h[i,j+1], ...
         sm.p[r & 3][t] = pressure_cell<LIT, R>(hc[t], hc[t - 1], hm[t], hc[t + 1], hp[t],
@@ -782,7 +862,7 @@ __device__ __forceinline__ void march_run(const StepArgs &a, int bx, int by, lon
                          hp[t - 1], gx2, gy2);
                 part.area += sqrt(gx2 * gx2 + gy2 * gy2 + R(1));
                 if (mode == THETA_FIELD)
-                    part.cossum += reinterpret_cast<const R *>(a.cosF)[cell];
+                    part.cossum += reinterpret_cast<const R *>(a.cosF)[frow(gy) * Lx + gxf];
                 else if (mode == THETA_WAVE)
                     part.cossum += cos_col;
             }
@@ -857,6 +937,8 @@ __device__ __forceinline__ void tile2d_run(const StepArgs &a, int bx, int by, lo
     const R gamma = R(a.gamma), hmin = R(a.hmin), hcrit = R(a.hcrit);
     const int mode = a.theta_mode;
     const double corr = (!FRESH && a.mass_corr) ? __ldcg(&a.ctl->corr[tt & 1]) : 0.0;
+    int fsx = 0, fsy = 0;  // offset of a moving θ field
+    if (mode == THETA_FIELD) substrate_shift(a, tt, &fsx, &fsy);
 
     // A. pulls and moments
     R ft[3][9];
@@ -908,8 +990,8 @@ __device__ __forceinline__ void tile2d_run(const StepArgs &a, int bx, int by, lo
             if (mode != THETA_SCALAR) {
                 const int gx = wrapc(x0 - 1 + px, Lx);
                 if (mode == THETA_FIELD) {
-                    const int gy = wrapc(y0 - 1 + py, Ly);
-                    kap = reinterpret_cast<const R *>(a.kapF)[gy * Lx + gx];
+                    const int gy = wrapc(y0 - 1 + py - fsy, Ly);
+                    kap = reinterpret_cast<const R *>(a.kapF)[gy * Lx + wrapc(gx - fsx, Lx)];
                 } else {
                     const R th = R(a.theta0) + R(a.dtheta) * sinpi_r(R(2) * (R(gx) - R(a.wave_v) * R(tt)) / R(Lx));
                     kap = kappa_of(th, a.n, a.m, hmin);
@@ -965,7 +1047,8 @@ __device__ __forceinline__ void tile2d_run(const StepArgs &a, int bx, int by, lo
                 grad9<R>(hc[-1], hm[0], hc[1], hp[0], hm[-1], hm[1], hp[1], hp[-1], gx2, gy2);
                 part.area += sqrt(gx2 * gx2 + gy2 * gy2 + R(1));
                 if (mode == THETA_FIELD) {
-                    part.cossum += reinterpret_cast<const R *>(a.cosF)[cell];
+                    part.cossum += reinterpret_cast<const R *>(
+                        a.cosF)[wrapc(gy - fsy, Ly) * Lx + wrapc(gx - fsx, Lx)];
                 } else if (mode == THETA_WAVE) {
                     const R th = R(a.theta0) + R(a.dtheta) * sinpi_r(R(2) * (R(gx) - R(a.wave_v) * R(tt)) / R(Lx));
                     part.cossum += cospi_r(th);
@@ -1169,6 +1252,23 @@ __global__ void __launch_bounds__(NT) batch_advance_kernel(const StepArgs *__res
     if (threadIdx.x == 0) sa.ctl->step_base = s;
 }
 
+// thermal!(fx, fy, h, kbt, mu, delta) of the current height field for
+// iteration t: the fluctuating forces the fused step adds (swb_thermal_field).
+template <class S>
+__global__ void thermal_field_kernel(const StepArgs a, long long t, double *fx, double *fy) {
+    using R = typename S::real;
+    const long long N = (long long)a.Lx * a.Ly;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < N;
+         c += (long long)gridDim.x * blockDim.x) {
+        const R h = reinterpret_cast<const R *>(a.hF)[c];
+        R zx, zy;
+        thermal_normals(a.seed, c, t, zx, zy);
+        const R sg = thermal_sigma<S::kLiteral, R>(R(a.k6), h, R(a.delta));
+        fx[c] = (double)(zx * sg);
+        fy[c] = (double)(zy * sg);
+    }
+}
+
 // moments! into the fields (used when the host reads h/u).
 template <class S>
 __global__ void moments_kernel(const StepArgs a) {
@@ -1225,9 +1325,11 @@ __global__ void pressure_now_kernel(const StepArgs a, double *out) {
         R kap;
         if (a.theta_mode == THETA_SCALAR)
             kap = R(a.kap);
-        else if (a.theta_mode == THETA_FIELD)
-            kap = reinterpret_cast<const R *>(a.kapF)[c];
-        else
+        else if (a.theta_mode == THETA_FIELD) {
+            int sx, sy;
+            substrate_shift(a, t, &sx, &sy);
+            kap = reinterpret_cast<const R *>(a.kapF)[wrapc(j - sy, Ly) * Lx + wrapc(i - sx, Lx)];
+        } else
             kap = kappa_of(R(a.theta0) + R(a.dtheta) * sinpi_r(R(2) * (R(i) - R(a.wave_v) * R(t)) / R(Lx)),
                            a.n, a.m, R(a.hmin));
         out[c] = (double)pressure_cell<S::kLiteral, R>(

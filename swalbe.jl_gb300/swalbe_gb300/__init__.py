@@ -4,7 +4,7 @@ A drop-in for the time loop of Swalbe.jl: the same API (SysConst, Taumucs,
 Sys, time_loop, run_*) over a CUDA C-ABI library for sm_103a.
 """
 from .api import (Batch, BGKandStream_, GB300State, Server, Sys, SysConst, Taumucs, cospi,
-                  count_droplets,
+                  count_droplets, boxpattern, ellipsepattern, trianglepattern,
                   equilibrium_, filmpressure_, force_sum_, h_grad_p_, inclination_, moments_,
                   randinterface_, run_dropletforced, run_dropletpatterned, run_dropletrelax,
                   run_flat, run_random, run_rayleightaylor, singledroplet, slippage_,
@@ -14,7 +14,7 @@ from .build import LIB_PATH, build
 
 __all__ = [
     "Batch", "BGKandStream_", "GB300State", "Server", "Sys", "SysConst", "Taumucs", "cospi",
-    "count_droplets",
+    "count_droplets", "boxpattern", "ellipsepattern", "trianglepattern",
     "equilibrium_", "filmpressure_", "force_sum_", "h_grad_p_", "inclination_", "moments_",
     "randinterface_", "run_dropletforced", "run_dropletpatterned", "run_dropletrelax", "run_flat",
     "run_random", "run_rayleightaylor", "singledroplet", "slippage_", "surfacearea_", "time_loop",

@@ -130,6 +130,11 @@ def lib() -> C.CDLL:
             "swb_server_set_queue_limit": (i, [p, i64]),
             "swb_server_set_policy": (i, [p, i, i64]),
             "swb_count_droplets": (i, [p, i, i, d, C.POINTER(i64)]),
+            "swb_set_thermal_seed": (i, [p, C.c_uint64]),
+            "swb_thermal_field": (i, [p, i64, p, p]),
+            "swb_op_thermal": (i, [p, i64]),
+            "swb_batch_set_geometry": (i, [p, i, i]),
+            "swb_set_substrate_motion": (i, [p, i64, i, i]),
             "swb_server_poll": (i, [p, i64, p, C.POINTER(RequestInfo)]),
             "swb_server_cancel": (i, [p, i64]),
             "swb_server_stats_get": (i, [p, C.POINTER(ServerStats)]),

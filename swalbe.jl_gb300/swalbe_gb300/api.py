@@ -187,6 +187,14 @@ class GB300State:
     def set_theta_wave(self, theta0: float, dtheta: float, v: float) -> None:
         self._chk(lib().swb_set_theta_wave(self._h, theta0, dtheta, v))
 
+    def move_substrate(self, tmove: int, direction: str = "diagonal") -> None:
+        """move_substrate!(θ, input, t, tmove; direction) after every iteration
+        (scripts/Moving_wettability_structs.jl:139-152): the θ field set by
+        set_theta_field moves one cell along `direction` ("diagonal", "x",
+        "y") after every `tmove` iterations from now; tmove = 0 stops it."""
+        dx, dy = {"diagonal": (1, 1), "x": (1, 0), "y": (0, 1)}[direction]
+        self._chk(lib().swb_set_substrate_motion(self._h, int(tmove), dx, dy))
+
     def set_inclination(self, alpha, t=1000, tstart=0, tsmooth=1, loop_time=False) -> None:
         self._chk(lib().swb_set_inclination(self._h, float(alpha[0]), float(alpha[1]),
                                             int(loop_time), int(t), int(tstart), int(tsmooth)))
@@ -209,6 +217,18 @@ class GB300State:
         a = C.c_int()
         self._chk(lib().swb_get_step_mode(self._h, C.byref(a)))
         return {1: "per_iteration", 2: "multi"}[a.value]
+
+    def set_thermal_seed(self, seed: int) -> None:
+        """Key of the thermal noise stream (Philox-4x32-10; counter = cell, iteration)."""
+        self._chk(lib().swb_set_thermal_seed(self._h, int(seed)))
+
+    def thermal_field(self, t: int):
+        """(kbtx, kbty): thermal!'s forces on the current height for iteration t."""
+        shape = self.shape
+        fx = np.empty(shape, order="F")
+        fy = np.empty(shape, order="F")
+        self._chk(lib().swb_thermal_field(self._h, int(t), fx.ctypes.data, fy.ctypes.data))
+        return fx, fy
 
     def set_mass_correction(self, on: bool) -> None:
         self._chk(lib().swb_set_mass_correction(self._h, int(bool(on))))
@@ -241,9 +261,15 @@ class GB300State:
 
 
 def Sys(sysc: SysConst, device: str = "GB300", T=np.float64, kind: str = "simple") -> GB300State:
-    """Sys(sysc, device; T, kind) (src/initialize.jl:491-572): zero populations, h = 1."""
-    if kind != "simple":
-        raise NotImplementedError(f"kind={kind!r}: only 'simple' states run on the GB300 path")
+    """Sys(sysc, device; T, kind) (src/initialize.jl:491-572): zero populations, h = 1.
+
+    kind="thermal" adds thermal!'s fluctuating forces every iteration when
+    kbt > 0 (src/forcing.jl:297-320); a "simple" state has no fluctuation
+    fields in the reference, so its kbt has no effect here either."""
+    if kind not in ("simple", "thermal"):
+        raise NotImplementedError(f"kind={kind!r}: 'simple' and 'thermal' states run on the GB300 path")
+    if kind == "simple" and sysc.param.kbt != 0.0:
+        sysc = SysConst(sysc.Lx, sysc.Ly, sysc.param.replace(kbt=0.0))
     return GB300State(sysc, _precision(device, T))
 
 
@@ -260,6 +286,12 @@ def filmpressure_(state: GB300State, sysc: SysConst, θ=None, theta=None) -> Non
     th = θ if θ is not None else theta
     state.set_theta(sysc.param.theta if th is None else th)
     state._chk(lib().swb_op_filmpressure(state.handle))
+
+
+def thermal_(state: GB300State, t: int) -> None:
+    """Fx .-= kbtx, Fy .-= kbty with thermal!'s forces of iteration t
+    (src/forcing.jl:297-320), on a "GB300-plain" state after force_sum_."""
+    state._chk(lib().swb_op_thermal(state.handle, int(t)))
 
 
 def h_grad_p_(state: GB300State) -> None:
@@ -416,6 +448,110 @@ def two_caps(Lx: int, Ly: int, r1, r2, θ1, θ2, c1, c2) -> np.ndarray:
     return np.asfortranarray(np.where(h < 0, 0.05, h))
 
 
+# ------------------------------------------------------------------ substrate patterns
+# boxpattern / ellipsepattern / trianglepattern (src/initialvalues.jl:423-581)
+# build a contact-angle field with a patch of θ0 + δa.  The reference tests
+# membership of the lattice point (i, j) (1-based) in a LazySets polygon or
+# ellipsoid and writes θ[j, i] (rows and columns swapped, kept here), and it
+# moves vertices that fall off the lattice onto coordinate 1 (x first; y only
+# when x was on the lattice).
+class Polygon:
+    """Convex polygon (the convex hull of its vertices, closed)."""
+
+    def __init__(self, vertices):
+        pts = sorted({(float(x), float(y)) for x, y in vertices})
+
+        def cross(o, a, b):
+            return (a[0] - o[0]) * (b[1] - o[1]) - (a[1] - o[1]) * (b[0] - o[0])
+
+        lower, upper = [], []
+        for p in pts:  # Andrew's monotone chain, counter-clockwise
+            while len(lower) >= 2 and cross(lower[-2], lower[-1], p) <= 0:
+                lower.pop()
+            lower.append(p)
+        for p in reversed(pts):
+            while len(upper) >= 2 and cross(upper[-2], upper[-1], p) <= 0:
+                upper.pop()
+            upper.append(p)
+        self.vertices = lower[:-1] + upper[:-1]
+
+    def __contains__(self, pt) -> bool:
+        v = self.vertices
+        x, y = float(pt[0]), float(pt[1])
+        if len(v) == 1:
+            return (x, y) == v[0]
+        for k in range(len(v)):
+            (ax, ay), (bx, by) = v[k], v[(k + 1) % len(v)]
+            if (bx - ax) * (y - ay) - (by - ay) * (x - ax) < -1e-12 * max(1.0, abs(bx - ax) + abs(by - ay)):
+                return False
+        if len(v) == 2:  # a segment: also within its extent
+            return min(v[0][0], v[1][0]) <= x <= max(v[0][0], v[1][0]) and \
+                min(v[0][1], v[1][1]) <= y <= max(v[0][1], v[1][1])
+        return True
+
+
+class Ellipse:
+    """Closed ellipse {x : (x - c)ᵀ Q⁻¹ (x - c) <= 1}, Q = diag(a², b²)."""
+
+    def __init__(self, center, a, b):
+        self.center = (float(center[0]), float(center[1]))
+        self.q = (float(a) ** 2, float(b) ** 2)
+
+    def __contains__(self, pt) -> bool:
+        dx, dy = float(pt[0]) - self.center[0], float(pt[1]) - self.center[1]
+        return dx * (dx / self.q[0]) + dy * (dy / self.q[1]) <= 1.0
+
+
+def _clamp_vertices(xs, ys, shape):
+    for k in range(len(xs)):
+        if xs[k] < 1 or xs[k] > shape[0]:
+            xs[k] = 1.0
+        elif ys[k] < 1 or ys[k] > shape[1]:
+            ys[k] = 1.0
+    return list(zip(xs, ys))
+
+
+def _paint(theta, theta0, da, region):
+    th = np.array(theta, dtype=np.float64, order="F", copy=True)
+    n1, n2 = th.shape
+    for i in range(1, n1 + 1):
+        for j in range(1, n2 + 1):
+            th[j - 1, i - 1] = theta0 + da if (i, j) in region else theta0
+    return th
+
+
+def boxpattern(theta, theta0, center=None, δa=1 / 36, side=20, **kw):
+    """boxpattern(θ, θ₀; center, δₐ, side) (src/initialvalues.jl:423-458): (θ, P)."""
+    da = kw.get("delta_a", δa)
+    sh = np.shape(theta)
+    c = (sh[0] // 2, sh[1] // 2) if center is None else center
+    xs = [c[0] - side / 2, c[0] - side / 2, c[0] + side / 2, c[0] + side / 2]
+    ys = [c[1] - side / 2, c[1] + side / 2, c[1] - side / 2, c[1] + side / 2]
+    P = Polygon(_clamp_vertices(xs, ys, sh))
+    return _paint(theta, theta0, da, P), P
+
+
+def ellipsepattern(theta, theta0, center=None, δa=1 / 36, a=10, b=5, **kw):
+    """ellipsepattern(θ, θ₀; center, δₐ, a, b) (src/initialvalues.jl:489-510): (θ, P)."""
+    da = kw.get("delta_a", δa)
+    sh = np.shape(theta)
+    c = (sh[0] // 2, sh[1] // 2) if center is None else center
+    P = Ellipse(c, a, b)
+    return _paint(theta, theta0, da, P), P
+
+
+def trianglepattern(theta, theta0, center=None, δa=1 / 36, side=60, **kw):
+    """trianglepattern(θ, θ₀; center, δₐ, side) (src/initialvalues.jl:552-581): (θ, P)."""
+    da = kw.get("delta_a", δa)
+    sh = np.shape(theta)
+    c = (sh[0] // 2, sh[1] // 2) if center is None else center
+    height = np.sqrt(3) / 2 * side
+    xs = [c[0] - side / 2, c[0] + side / 2, c[0]]
+    ys = [c[1] - height / 3, c[1] - height / 3, c[1] + 2 * height / 3]
+    P = Polygon(_clamp_vertices(xs, ys, sh))
+    return _paint(theta, theta0, da, P), P
+
+
 # ------------------------------------------------------------------ run_* drivers
 def _new(sysc, device, T):
     return Sys(sysc, device, T=T)
@@ -518,6 +654,10 @@ class Batch:
         out = np.empty((s.Lx, s.Ly), order="F")
         check(lib().swb_batch_get_height(self._h, i, out.ctypes.data))
         return out
+
+    def set_geometry(self, nt: int = 64, rows: int = 32) -> None:
+        """Strips of every lattice: nt threads (nt - 4 columns) x rows."""
+        check(lib().swb_batch_set_geometry(self._h, int(nt), int(rows)))
 
     def set_theta_wave(self, i: int, theta0: float, dtheta: float, v: float) -> None:
         check(lib().swb_batch_set_theta_wave(self._h, i, theta0, dtheta, v))

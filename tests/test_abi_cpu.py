@@ -41,11 +41,11 @@ def test_create_rejects_bad_params(lib, bad):
     assert lib.swb_last_error(None)
 
 
-def test_thermal_is_unsupported(lib):
-    s = sw.SysConst(8, 8, sw.Taumucs(kbt=1e-6))
+def test_negative_kbt_is_rejected(lib):
+    s = sw.SysConst(8, 8, sw.Taumucs(kbt=-1e-6))
     h = C.c_void_p()
     p = s.c_params()
-    assert lib.swb_create(C.byref(p), L.SWB_F32, C.byref(h)) == L.SWB_ERR_UNSUPPORTED
+    assert lib.swb_create(C.byref(p), L.SWB_F32, C.byref(h)) == L.SWB_ERR_ARG
 
 
 def test_state_bytes(lib):
@@ -88,7 +88,7 @@ def test_device_strings():
     with pytest.raises(ValueError):
         sw.Sys(sw.SysConst(4, 4), "CPU")
     with pytest.raises(NotImplementedError):
-        sw.Sys(sw.SysConst(4, 4), "GB300", kind="thermal")
+        sw.Sys(sw.SysConst(4, 4), "GB300", kind="exotic")
 
 
 def _components_reference(h, thr):
