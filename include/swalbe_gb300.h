@@ -209,6 +209,16 @@ int swb_set_measures(swb_state *s, int mask, double hthresh);
  * moments!.  Asynchronous.  SWB_ERR_NAN is reported by the next
  * synchronising call after a non-finite height was seen. */
 int swb_step(swb_state *s, int64_t nsteps);
+/* snapshot!(fluid, height, t; dumping) (src/measures.jl:99-105) on the
+ * device: after every iteration t with t % dumping == 0 the height is copied
+ * into a device ring of `capacity` fields (Float64, column-major), without a
+ * host round trip.  dumping = 0 turns it off (and frees the ring).
+ * swb_get_snapshots copies the snapshots taken since the last call, oldest
+ * first (each row Lx*Ly doubles, the reference's vec(h)), with their
+ * iterations in `times` (may be NULL); if more than `capacity` were taken,
+ * only the newest `capacity` remain. */
+int swb_set_snapshots(swb_state *s, int64_t dumping, int64_t capacity);
+int swb_get_snapshots(swb_state *s, double *out, int64_t cap, int64_t *count, int64_t *times);
 int swb_sync(swb_state *s);
 /* Number of iterations completed since swb_create. */
 int swb_steps_done(swb_state *s, int64_t *t);
@@ -339,6 +349,31 @@ int swb_server_poll(swb_server *sv, int64_t id, double *h_out, swb_request_info 
 int swb_server_cancel(swb_server *sv, int64_t id);
 int swb_server_stats_get(swb_server *sv, swb_server_stats *st);
 double swb_server_clock(swb_server *sv);
+
+/* ---------------------------------------------------------------------- */
+/* One dimension: the D1Q3 solver (src/collide.jl:179-212,                 */
+/* src/simulate.jl:98-179), for one or many 1D lattices.                    */
+/* ---------------------------------------------------------------------- */
+/* Sys(sysc::SysConst_1D) (src/initialize.jl:587-599) for each of `count`
+ * lattices: L = params[i].Lx (>= 3), params[i].Ly = 1; zero populations,
+ * height 1, velocity 0.  SWB_F64 (the reference's arithmetic, bit for bit)
+ * or SWB_F32.  rec_cap > 0 keeps the measures (mass, wetted count,
+ * max/min) of the last rec_cap iterations of each lattice.  Every
+ * swb1d_step runs all lattices together, one CTA each. */
+typedef struct swb1d swb1d;
+#define SWB1D_FIELD_THETA 20 /* θ field (time_loop(sys, state, θ::Vector))          */
+#define SWB1D_FIELD_GAMMA 21 /* γ field and its ∇γ force (run_gamma, src/simulate.jl:518-556) */
+int swb1d_create(const swb_params *params, int count, int precision, int rec_cap, swb1d **out);
+int swb1d_destroy(swb1d *b);
+/* height, vel (SWB_FIELD_HEIGHT, SWB_FIELD_VELX), SWB1D_FIELD_THETA and
+ * SWB1D_FIELD_GAMMA (NULL clears them); host arrays of L doubles. */
+int swb1d_set_field(swb1d *b, int idx, int field, const double *host);
+/* height, vel, pressure (SWB_FIELD_PRESSURE) or the populations
+ * (SWB_FIELD_FOUT, L x 3 column-major, the reference's fout).  Syncs. */
+int swb1d_get_field(swb1d *b, int idx, int field, double *host);
+int swb1d_step(swb1d *b, int64_t nsteps);
+int swb1d_sync(swb1d *b);
+int swb1d_get_measures(swb1d *b, int idx, swb_measure *out, int64_t cap, int64_t *count);
 
 #ifdef __cplusplus
 }

@@ -105,6 +105,15 @@ def lib() -> C.CDLL:
             "orc_philox4x32_10": (None, [p, p, p]),
             "orc_thermal_normals": (None, [C.c_uint64, C.c_uint64, C.c_int64, p, p]),
             "orc_thermal": (None, [p, p, p, sz, d, d, d, C.c_uint64, C.c_int64]),
+            "orc1_filmpressure": (None, [p, p, i, d, p, p, d, i, i, d, d]),
+            "orc1_hgradp": (None, [p, p, p, i]),
+            "orc1_slippage": (None, [p, p, p, i, d, d]),
+            "orc1_gradgamma": (None, [p, p, i]),
+            "orc1_equilibrium": (None, [p, p, p, i, d]),
+            "orc1_bgk_stream": (None, [p, p, p, p, i, d]),
+            "orc1_moments": (None, [p, p, p, i]),
+            "orc1_time_loop": (None, [p, p, p, p, p, i, p, p, p, p]),
+            "orc1_two_droplets": (None, [p, i, d, d, d, d, d, d]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -433,3 +442,72 @@ def thermal(h, kbt, mu, delta, seed=0, t=1):
     lib().orc_thermal(_p(fx), _p(fy), _p(hh), hh.size, float(kbt), float(mu), float(delta),
                       int(seed), int(t))
     return fx, fy
+
+
+# ---------------------------------------------------------------- D1Q3
+def _v(a):
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float64))
+
+
+def equilibrium_1d(h, u, g=0.0):
+    """equilibrium!(feq, height, velocity, gravity) (src/equilibrium.jl:169-181): L x 3."""
+    h, u = _v(h), _v(u)
+    feq = np.zeros((h.size, 3), order="F")
+    lib().orc1_equilibrium(_p(feq), _p(h), _p(u), h.size, float(g))
+    return feq
+
+
+def bgk_stream_1d(feq, ftemp, F, tau):
+    """BGKandStream!(fout, feq, ftemp, F, τ) (src/collide.jl:179-201): (fout, ftemp)."""
+    fe = np.asfortranarray(feq, dtype=np.float64)
+    ft = np.asfortranarray(ftemp, dtype=np.float64).copy(order="F")
+    FF = _v(F)
+    fout = np.zeros_like(ft)
+    lib().orc1_bgk_stream(_p(fout), _p(fe), _p(ft), _p(FF), fe.shape[0], float(tau))
+    return fout, ft
+
+
+def slippage_1d(h, u, delta, mu):
+    h, u = _v(h), _v(u)
+    out = np.zeros_like(h)
+    lib().orc1_slippage(_p(out), _p(h), _p(u), h.size, float(delta), float(mu))
+    return out
+
+
+def singledroplet_1d(L, radius, theta, center, hcrit=0.05):
+    """singledroplet(height::Vector, radius, θ, center; hcrit) (src/initialvalues.jl:226-243)."""
+    h = np.zeros(L)
+    for i in range(1, L + 1):
+        circ = np.sqrt((i - center) ** 2)
+        h[i - 1] = (np.cos(np.arcsin(circ / radius)) - cospi(theta)) * radius if circ <= radius else hcrit
+    return np.where(h <= hcrit, hcrit, h)
+
+
+def two_droplets(L, r1=230, r2=230, th1=1 / 9, th2=1 / 9, center=None):
+    """two_droplets(sys; r₁, r₂, θ₁, θ₂, center) (src/initialvalues.jl:277-323)."""
+    c = (L / 3, 2 * L / 3) if center is None else center
+    h = np.zeros(L)
+    lib().orc1_two_droplets(_p(h), int(L), float(r1), float(r2), float(th1), float(th2),
+                            float(c[0]), float(c[1]))
+    return h
+
+
+class State1D:
+    """A D1Q3 State (src/initialize.jl:587-599): fout, ftemp, height, vel."""
+
+    def __init__(self, P: Params, h0=None):
+        self.P = P
+        L = P.Lx
+        self.fout = np.zeros((L, 3), order="F")
+        self.ftemp = np.zeros((L, 3), order="F")
+        self.h = np.ones(L) if h0 is None else _v(h0).copy()
+        self.u = np.zeros(L)
+
+    def run(self, steps, theta_field=None, gamma_field=None, record_dh=False, wetted=False):
+        dh = np.zeros(steps) if record_dh else None
+        wet = np.zeros(steps, dtype=np.int64) if wetted else None
+        tf = None if theta_field is None else _v(theta_field)
+        gf = None if gamma_field is None else _v(gamma_field)
+        lib().orc1_time_loop(_p(self.fout), _p(self.ftemp), _p(self.h), _p(self.u), C.byref(self.P),
+                             int(steps), _p(tf), _p(gf), _p(dh), _p(wet))
+        return dh if not wetted else (dh, wet)

@@ -740,3 +740,131 @@ int orc_max_threads(void) {
     return 1;
 #endif
 }
+
+/* ================================================================== */
+/* One dimension, D1Q3 (literal; each op one pass over the lattice).   */
+/* ================================================================== */
+static inline int wrap1(int i, int L) { return i < 0 ? i + L : (i >= L ? i - L : i); }
+
+/* filmpressure!(state::LBM_state_1D, sys; θ, γ) (src/pressure.jl:231-256,
+ * 285-315 with a γ field).  theta_field / gamma_field may be NULL. */
+void orc1_filmpressure(double *p, const double *h, int L, double gamma, const double *gamma_field,
+                       const double *theta_field, double theta, int n, int m, double hmin,
+                       double hcrit) {
+    for (int i = 0; i < L; ++i) {
+        const double th = theta_field ? theta_field[i] : theta;
+        const double g = gamma_field ? gamma_field[i] : gamma;
+        const double kap = (((1.0 - orc_cospi(th)) * (n - 1)) * (m - 1)) / ((n - m) * hmin);
+        const double x = hmin / (h[i] + hcrit);
+        p[i] = -g * (kap * (orc_power_broad(x, n) - orc_power_broad(x, m)));
+    }
+    for (int i = 0; i < L; ++i) {
+        const double g = gamma_field ? gamma_field[i] : gamma;
+        const double hip = h[wrap1(i - 1, L)], him = h[wrap1(i + 1, L)];
+        p[i] = p[i] - g * ((hip - 2.0 * h[i]) + him);
+    }
+}
+
+/* h∇p!(state::LBM_state_1D) (src/forcing.jl:189-198). */
+void orc1_hgradp(double *hgp, const double *h, const double *p, int L) {
+    for (int i = 0; i < L; ++i)
+        hgp[i] = (h[i] * -0.5) * (p[wrap1(i - 1, L)] - p[wrap1(i + 1, L)]);
+}
+
+/* slippage!(slip, height, vel, δ, μ) (src/forcing.jl:68-71). */
+void orc1_slippage(double *slip, const double *h, const double *u, int L, double delta,
+                   double mu) {
+    for (int i = 0; i < L; ++i)
+        slip[i] = ((6.0 * mu) * h[i] * u[i]) /
+                  ((2.0 * (h[i] * h[i]) + (6.0 * delta) * h[i]) + 3.0 * (delta * delta));
+}
+
+/* ∇γ!(state) (src/forcing.jl:423-432). */
+void orc1_gradgamma(double *dg, const double *gam, int L) {
+    for (int i = 0; i < L; ++i)
+        dg[i] = (-3.0 / 2.0) * ((gam[wrap1(i - 1, L)] - gam[wrap1(i + 1, L)]) / 2.0);
+}
+
+/* equilibrium!(feq, height, velocity, gravity) (src/equilibrium.jl:169-181);
+ * feq is L x 3 column-major. */
+void orc1_equilibrium(double *feq, const double *h, const double *u, int L, double g) {
+    for (int i = 0; i < L; ++i) {
+        const double uu = u[i] * u[i];
+        feq[i] = h[i] * ((1.0 - (0.5 * g) * h[i]) - uu);
+        feq[L + i] = h[i] * (((0.25 * g) * h[i] + 0.5 * u[i]) + 0.5 * uu);
+        feq[2 * L + i] = h[i] * (((0.25 * g) * h[i] - 0.5 * u[i]) + 0.5 * uu);
+    }
+}
+
+/* BGKandStream!(fout, feq, ftemp, F, τ) (src/collide.jl:179-201). */
+void orc1_bgk_stream(double *fout, const double *feq, double *ftemp, const double *F, int L,
+                     double tau) {
+    const double omeg = 1.0 - 1.0 / tau, it = 1.0 / tau;
+    double *fo = malloc(3 * (size_t)L * sizeof(double));
+    for (int i = 0; i < L; ++i) {
+        fo[i] = omeg * ftemp[i] + it * feq[i];
+        fo[L + i] = omeg * ftemp[L + i] + it * feq[L + i] + 0.5 * F[i];
+        fo[2 * L + i] = omeg * ftemp[2 * L + i] + it * feq[2 * L + i] - 0.5 * F[i];
+    }
+    for (int i = 0; i < L; ++i) {
+        ftemp[i] = fo[i];
+        ftemp[L + i] = fo[L + wrap1(i - 1, L)];
+        ftemp[2 * L + i] = fo[2 * L + wrap1(i + 1, L)];
+    }
+    memcpy(fout, ftemp, 3 * (size_t)L * sizeof(double));
+    free(fo);
+}
+
+/* moments!(height::Vector, vel, fout) (src/moments.jl:54-62). */
+void orc1_moments(double *h, double *u, const double *fout, int L) {
+    for (int i = 0; i < L; ++i) {
+        h[i] = (fout[i] + fout[L + i]) + fout[2 * L + i];
+        u[i] = (fout[L + i] - fout[2 * L + i]) / h[i];
+    }
+}
+
+/* time_loop(sys::SysConst_1D, state[, θ | Δh | wetted!, area])
+ * (src/simulate.jl:98-179), and
+ * run_gamma's loop (src/simulate.jl:518-556) when gamma_field is given: the
+ * pressure uses the γ field and F .= -h∇p .- slip .- ∇γ.  State arrays:
+ * fout, ftemp (L x 3), h, u (L).  dh (may be NULL): max - min of h at the
+ * start of each iteration. */
+void orc1_time_loop(double *fout, double *ftemp, double *h, double *u, const orc_params *P,
+                    int Tmax, const double *theta_field, const double *gamma_field,
+                    double *dh, int64_t *wet) {
+    const int L = P->Lx;
+    double *p = malloc((size_t)L * sizeof(double)), *hgp = malloc((size_t)L * sizeof(double));
+    double *slip = malloc((size_t)L * sizeof(double)), *F = malloc((size_t)L * sizeof(double));
+    double *feq = malloc(3 * (size_t)L * sizeof(double)), *dg = NULL;
+    if (gamma_field) {
+        dg = malloc((size_t)L * sizeof(double));
+        orc1_gradgamma(dg, gamma_field, L);
+    }
+    for (int t = 1; t <= Tmax; ++t) {
+        if (dh) dh[t - 1] = orc_dh(h, (size_t)L);
+        orc1_filmpressure(p, h, L, P->gamma, gamma_field, theta_field, P->theta, P->n, P->m,
+                          P->hmin, P->hcrit);
+        orc1_hgradp(hgp, h, p, L);
+        orc1_slippage(slip, h, u, L, P->delta, P->mu);
+        for (int i = 0; i < L; ++i) F[i] = dg ? (-hgp[i] - slip[i]) - dg[i] : -hgp[i] - slip[i];
+        if (wet) wet[t - 1] = orc_wetted(h, (size_t)L, 0.055);  /* f(measure, state) */
+        orc1_equilibrium(feq, h, u, L, P->g);
+        orc1_bgk_stream(fout, feq, ftemp, F, L, P->tau);
+        orc1_moments(h, u, fout, L);
+    }
+    free(p); free(hgp); free(slip); free(F); free(feq); free(dg);
+}
+
+/* two_droplets(sys; r₁, r₂, θ₁, θ₂, center) (src/initialvalues.jl:277-323). */
+void orc1_two_droplets(double *h, int L, double r1, double r2, double th1, double th2, double c1,
+                       double c2) {
+    for (int i = 1; i <= L; ++i) {
+        const double a = sqrt((i - c1) * (i - c1)), b = sqrt((i - c2) * (i - c2));
+        double d1 = a <= r1 ? (cos(asin(a / r1)) - orc_cospi(th1)) * r1 : 0.05;
+        double d2 = b <= r2 ? (cos(asin(b / r2)) - orc_cospi(th2)) * r2 : 0.05;
+        if (d1 < 0) d1 = 0.05;
+        if (d2 < 0) d2 = 0.05;
+        double v = d1 + d2 - 0.05;
+        h[i - 1] = v < 0 ? 0.05 : v;
+    }
+}

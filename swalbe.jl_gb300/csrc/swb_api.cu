@@ -172,6 +172,7 @@ namespace swb {
 void set_global_error(const char *msg) { g_err = msg; }
 static std::atomic<unsigned long long> g_launches{0};
 void count_launches(unsigned long long n) { g_launches += n; }
+unsigned long long launches_so_far() { return g_launches.load(); }
 
 cudaError_t launch_fused_step(int precision, const StepArgs &a, int k, cudaStream_t st) {
     count_launches(1);
@@ -198,12 +199,13 @@ cudaError_t launch_pressure_now(int precision, const StepArgs &a, double *out, c
     return precision == SWB_F64 ? launch_pressure_now_f64(a, out, st)
                                 : launch_pressure_now_f32(precision, a, out, st);
 }
-cudaError_t launch_batch_step(int precision, int nt, const StepArgs *d_args,
+cudaError_t launch_batch_step(int precision, int nt, bool gen, const StepArgs *d_args,
                               const TileRef *d_tiles, int ntiles, int grid, int k,
                               cudaStream_t st) {
     count_launches(1);
-    return precision == SWB_F64 ? launch_batch_step_f64(nt, d_args, d_tiles, ntiles, grid, k, st)
-                                : launch_batch_step_f32(precision, nt, d_args, d_tiles, ntiles, grid, k, st);
+    return precision == SWB_F64
+               ? launch_batch_step_f64(nt, gen, d_args, d_tiles, ntiles, grid, k, st)
+               : launch_batch_step_f32(precision, nt, gen, d_args, d_tiles, ntiles, grid, k, st);
 }
 int batch_blocks_per_sm(int precision, int nt) {
     return precision == SWB_F64 ? batch_blocks_per_sm_f64(nt) : batch_blocks_per_sm_f32(precision, nt);
@@ -243,6 +245,7 @@ struct swb_state {
     long long N = 0, pitch = 0;
     cudaStream_t stream = nullptr;
     cudaStream_t own_stream = nullptr;  // the state's own stream
+    unsigned long long graph_launches = 0;  // kernels in the captured graph
     std::vector<void *> allocs;
     StepArgs a{};
     PlainState ps{};
@@ -277,6 +280,10 @@ struct swb_state {
     bool gvalid = false;
     double *dtmp = nullptr;
     size_t dtmp_bytes = 0;
+    // snapshots: device ring of snap_cap heights taken every snap_every iterations
+    long long snap_every = 0, snap_cap = 0, snap_count = 0, snap_read = 0;
+    double *snap = nullptr;
+    std::vector<long long> snap_t;
     std::string err;
 
     int rb() const { return real_bytes(precision); }
@@ -358,6 +365,11 @@ __global__ void set_fresh_kernel(Control *c) {
     c->fresh_step = c->step_base + 1;
     c->corr[0] = 0.0;
     c->corr[1] = 0.0;
+}
+__global__ void f2d_kernel(const float *src, double *dst, long long n) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        dst[i] = (double)src[i];
 }
 __global__ void d2f_kernel(const double *src, float *dst, long long n) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
@@ -512,12 +524,15 @@ constexpr int kTuneProbe = 16;
 // kernel) in ms, or a negative value on error.
 float tune_probe(swb_state *s, cudaEvent_t e0, cudaEvent_t e1) {
     cudaGraphExec_t gx = nullptr;
+    unsigned long long nodes = 0;
     if (!s->persist) {
         cudaGraph_t g = nullptr;
         if (cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
             return -1.f;
+        const unsigned long long c0 = swb::launches_so_far();
         cudaError_t le = launch_sequence(s, kTuneProbe);
-        swb::count_launches(0ULL - (unsigned long long)(kTuneProbe + 1));  // captured, not run
+        nodes = swb::launches_so_far() - c0;
+        swb::count_launches(0ULL - nodes);  // captured, not run
         cudaError_t ce = cudaStreamEndCapture(s->stream, &g);
         if (le != cudaSuccess || ce != cudaSuccess) {
             if (g) cudaGraphDestroy(g);
@@ -533,7 +548,7 @@ float tune_probe(swb_state *s, cudaEvent_t e0, cudaEvent_t e1) {
         cudaError_t e;
         if (gx) {
             e = cudaGraphLaunch(gx, s->stream);
-            swb::count_launches(kTuneProbe + 1);
+            swb::count_launches(nodes);
         } else {
             e = run_sequence(s, kTuneProbe);
         }
@@ -630,8 +645,10 @@ int fused_steps(swb_state *s, long long nsteps) {
         if (!s->gvalid) {
             cudaGraph_t g = nullptr;
             CUDA_TRY(&s->err, cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+            const unsigned long long c0 = swb::launches_so_far();
             cudaError_t le = launch_sequence(s, kGraphSteps);
-            swb::count_launches(0ULL - (unsigned long long)(kGraphSteps + 1));  // captured, not run
+            s->graph_launches = swb::launches_so_far() - c0;
+            swb::count_launches(0ULL - s->graph_launches);  // captured, not run
             cudaError_t ce = cudaStreamEndCapture(s->stream, &g);
             if (le != cudaSuccess) {
                 if (g) cudaGraphDestroy(g);
@@ -646,7 +663,7 @@ int fused_steps(swb_state *s, long long nsteps) {
         }
         while (left >= s->gsteps) {
             CUDA_TRY(&s->err, cudaGraphLaunch(s->gexec, s->stream));
-            swb::count_launches(s->gsteps + 1);
+            swb::count_launches(s->graph_launches);
             left -= s->gsteps;
         }
     }
@@ -1107,17 +1124,99 @@ int swb_set_measures(swb_state *s, int mask, double hthresh) {
     return SWB_OK;
 }
 
-int swb_step(swb_state *s, int64_t nsteps) {
-    if (!s) return fail(nullptr, SWB_ERR_ARG, "state is NULL");
-    if (nsteps < 0) return fail(&s->err, SWB_ERR_ARG, "nsteps must be >= 0");
+namespace {
+int run_steps(swb_state *s, long long n) {
     if (s->plain()) {
-        for (int64_t k = 0; k < nsteps; ++k) {
+        for (long long k = 0; k < n; ++k) {
             int rc = plain_iteration(s);
             if (rc) return rc;
         }
         return SWB_OK;
     }
-    return fused_steps(s, nsteps);
+    return fused_steps(s, n);
+}
+
+// snapshot!(fluid, height, t) (src/measures.jl:99-105) of the height after
+// the current iteration, into the next slot of the device ring.
+int take_snapshot(swb_state *s) {
+    int rc = materialize(s);
+    if (rc) return rc;
+    const long long N = s->N;
+    double *dst = s->snap + (size_t)(s->snap_count % s->snap_cap) * N;
+    if (s->plain()) {
+        CUDA_TRY(&s->err, cudaMemcpyAsync(dst, s->ps.h, N * 8, cudaMemcpyDeviceToDevice, s->stream));
+    } else if (s->rb() == 8) {
+        CUDA_TRY(&s->err, cudaMemcpyAsync(dst, s->a.hF, N * 8, cudaMemcpyDeviceToDevice, s->stream));
+    } else {
+        f2d_kernel<<<blocks_for(N), 256, 0, s->stream>>>((const float *)s->a.hF, dst, N);
+        swb::count_launches(1);
+        CUDA_TRY(&s->err, cudaGetLastError());
+    }
+    s->snap_t[(size_t)(s->snap_count % s->snap_cap)] = s->steps;
+    s->snap_count++;
+    return SWB_OK;
+}
+}  // namespace
+
+int swb_step(swb_state *s, int64_t nsteps) {
+    if (!s) return fail(nullptr, SWB_ERR_ARG, "state is NULL");
+    if (nsteps < 0) return fail(&s->err, SWB_ERR_ARG, "nsteps must be >= 0");
+    if (s->snap_every <= 0) return run_steps(s, nsteps);
+    // run to each multiple of the dump interval, then take the snapshot
+    long long left = nsteps;
+    while (left > 0) {
+        const long long to_dump = s->snap_every - s->steps % s->snap_every;
+        const long long n = left < to_dump ? left : to_dump;
+        int rc = run_steps(s, n);
+        if (rc) return rc;
+        left -= n;
+        if (s->steps % s->snap_every == 0) {
+            rc = take_snapshot(s);
+            if (rc) return rc;
+        }
+    }
+    return SWB_OK;
+}
+
+int swb_set_snapshots(swb_state *s, int64_t dumping, int64_t capacity) {
+    if (!s) return fail(nullptr, SWB_ERR_ARG, "state is NULL");
+    if (dumping < 0 || (dumping > 0 && capacity < 1))
+        return fail(&s->err, SWB_ERR_ARG, "snapshots: dumping >= 0 and capacity >= 1");
+    CUDA_TRY(&s->err, cudaStreamSynchronize(s->stream));
+    if (s->snap) {
+        cudaFree(s->snap);
+        for (auto &q : s->allocs)
+            if (q == s->snap) q = nullptr;
+        s->snap = nullptr;
+    }
+    s->snap_every = dumping;
+    s->snap_cap = dumping > 0 ? capacity : 0;
+    s->snap_count = s->snap_read = 0;
+    s->snap_t.assign((size_t)s->snap_cap, 0);
+    if (dumping > 0)
+        CUDA_TRY(&s->err, s->alloc((void **)&s->snap, (size_t)capacity * s->N * 8));
+    return SWB_OK;
+}
+
+int swb_get_snapshots(swb_state *s, double *out, int64_t cap, int64_t *count, int64_t *times) {
+    if (!s || !count || (cap > 0 && !out)) return fail(s ? &s->err : nullptr, SWB_ERR_ARG, "NULL argument");
+    *count = 0;
+    if (!s->snap) return SWB_OK;
+    long long first = s->snap_read;
+    if (s->snap_count - first > s->snap_cap) first = s->snap_count - s->snap_cap;  // overwritten
+    long long n = s->snap_count - first;
+    if (n > cap) n = cap;
+    const long long N = s->N;
+    for (long long k = 0; k < n; ++k) {
+        const long long slot = (first + k) % s->snap_cap;
+        CUDA_TRY(&s->err, cudaMemcpyAsync(out + (size_t)k * N, s->snap + (size_t)slot * N, N * 8,
+                                          cudaMemcpyDeviceToHost, s->stream));
+        if (times) times[k] = s->snap_t[(size_t)slot];
+    }
+    CUDA_TRY(&s->err, cudaStreamSynchronize(s->stream));
+    s->snap_read = first + n;
+    *count = n;
+    return SWB_OK;
 }
 
 int swb_sync(swb_state *s) {

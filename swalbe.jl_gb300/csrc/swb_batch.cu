@@ -216,8 +216,10 @@ int upload_args(swb_batch *b) {
 // n batched step launches (k = 0..n-1) and the advance kernel closing them.
 cudaError_t batch_sequence(swb_batch *b, int n, int grid) {
     cudaError_t e = cudaSuccess;
+    bool gen = false;  // the general kernel if any lattice needs it
+    for (const StepArgs &a : b->args) gen = gen || swb::step_general(a);
     for (int k = 0; k < n && e == cudaSuccess; ++k)
-        e = swb::launch_batch_step(b->precision, b->nt, b->d_args, b->d_tiles, b->ntiles,
+        e = swb::launch_batch_step(b->precision, b->nt, gen, b->d_args, b->d_tiles, b->ntiles,
                                    grid, k, b->stream);
     if (e == cudaSuccess && n > 0) e = swb::launch_batch_advance(b->d_args, b->count, n, b->stream);
     return e;

@@ -135,6 +135,12 @@ struct TileRef {
     int tx, ty;
 };
 
+// Whether a lattice's step needs the general kernel (θ field or wave,
+// thermal noise, inclination) rather than the common one.
+inline bool step_general(const StepArgs &a) {
+    return a.thermal || a.incl || a.theta_mode != THETA_SCALAR;
+}
+
 // Whether the step kernels of a lattice produce per-step partial measures.
 __host__ __device__ inline bool needs_partials(const StepArgs &a) { return a.meas_mask != 0 || a.mass_corr != 0; }
 
@@ -142,6 +148,8 @@ __host__ __device__ inline bool needs_partials(const StepArgs &a) { return a.mea
 void set_global_error(const char *msg);
 // Counts kernel launches issued by the library (swb_launch_count).
 void count_launches(unsigned long long n);
+// Launches counted so far (to account for kernels captured into graphs).
+unsigned long long launches_so_far();
 
 // ---- launchers (defined in the .cu files) ----
 // precision: SWB_F64 (swb_step_f64.cu) / SWB_F32, SWB_F16 (swb_step_f32.cu)
@@ -176,7 +184,8 @@ cudaError_t launch_thermal_field_f64(const StepArgs &a, long long t, double *fx,
                                      cudaStream_t st);
 cudaError_t launch_thermal_field_f32(int precision, const StepArgs &a, long long t, double *fx,
                                      double *fy, cudaStream_t st);
-cudaError_t launch_batch_step(int precision, int nt, const StepArgs *d_args,
+// gen: some lattice of the batch needs the general kernel (step_general).
+cudaError_t launch_batch_step(int precision, int nt, bool gen, const StepArgs *d_args,
                               const TileRef *d_tiles, int ntiles, int grid, int k,
                               cudaStream_t st);
 int batch_blocks_per_sm(int precision, int nt);
@@ -184,14 +193,14 @@ cudaError_t launch_fused_step_f64(const StepArgs &a, int k, cudaStream_t st);
 cudaError_t launch_moments_f64(const StepArgs &a, cudaStream_t st);
 cudaError_t launch_fout_f64(const StepArgs &a, double *out, cudaStream_t st);
 cudaError_t launch_pressure_now_f64(const StepArgs &a, double *out, cudaStream_t st);
-cudaError_t launch_batch_step_f64(int nt, const StepArgs *d_args, const TileRef *d_tiles,
+cudaError_t launch_batch_step_f64(int nt, bool gen, const StepArgs *d_args, const TileRef *d_tiles,
                                   int ntiles, int grid, int k, cudaStream_t st);
 cudaError_t launch_fused_step_f32(int precision, const StepArgs &a, int k, cudaStream_t st);
 cudaError_t launch_moments_f32(int precision, const StepArgs &a, cudaStream_t st);
 cudaError_t launch_fout_f32(int precision, const StepArgs &a, double *out, cudaStream_t st);
 cudaError_t launch_pressure_now_f32(int precision, const StepArgs &a, double *out,
                                     cudaStream_t st);
-cudaError_t launch_batch_step_f32(int precision, int nt, const StepArgs *d_args,
+cudaError_t launch_batch_step_f32(int precision, int nt, bool gen, const StepArgs *d_args,
                                   const TileRef *d_tiles, int ntiles, int grid, int k,
                                   cudaStream_t st);
 int batch_blocks_per_sm_f64(int nt);

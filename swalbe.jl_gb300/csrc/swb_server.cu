@@ -256,9 +256,11 @@ void worker_main(swb_server *sv) {
         const int grid = std::min(ntiles, sms * occ);
         const double tb = sv->now();
         cudaError_t e = cudaSuccess;
+        bool gen = false;  // the general kernel if any resident request needs it
+        for (Req *r : sv->active) gen = gen || swb::step_general(r->a);
         for (int64_t k = 0; k < tick && e == cudaSuccess; ++k)
-            e = swb::launch_batch_step(sv->precision, swb::kBatchNT, sv->d_args, sv->d_tiles, ntiles,
-                                       grid, (int)k, sv->stream);
+            e = swb::launch_batch_step(sv->precision, swb::kBatchNT, gen, sv->d_args, sv->d_tiles,
+                                       ntiles, grid, (int)k, sv->stream);
         if (e == cudaSuccess)
             e = swb::launch_batch_advance(sv->d_args, (int)sv->active.size(), (int)tick, sv->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(sv->stream);

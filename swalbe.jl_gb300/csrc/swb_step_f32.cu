@@ -45,7 +45,10 @@ cudaError_t launch_fused_step_f32(int precision, const StepArgs &a, int k, cudaS
     if (a.march_nt == kTileGeom) {
         DISPATCH_STORE(precision, (fused_tile_kernel<S><<<grid, kT2NT, 0, st>>>(a, k)));
     } else {
-        DISPATCH_STORE(precision, DISPATCH_NT(a.march_nt, (fused_step_kernel<S, NT><<<grid, NT, 0, st>>>(a, k))));
+        if (step_general(a))
+            DISPATCH_STORE(precision, DISPATCH_NT(a.march_nt, (fused_step_kernel<S, NT, true><<<grid, NT, 0, st>>>(a, k))));
+        else
+            DISPATCH_STORE(precision, DISPATCH_NT(a.march_nt, (fused_step_kernel<S, NT, false><<<grid, NT, 0, st>>>(a, k))));
     }
     return cudaGetLastError();
 }
@@ -76,16 +79,19 @@ cudaError_t launch_pressure_now_f32(int precision, const StepArgs &a, double *ou
     return cudaGetLastError();
 }
 
-cudaError_t launch_batch_step_f32(int precision, int nt, const StepArgs *d_args,
+cudaError_t launch_batch_step_f32(int precision, int nt, bool gen, const StepArgs *d_args,
                                   const TileRef *d_tiles, int ntiles, int grid, int k,
                                   cudaStream_t st) {
-    DISPATCH_STORE(precision, DISPATCH_NT(nt, (batch_step_kernel<S, NT><<<grid, NT, 0, st>>>(d_args, d_tiles, ntiles, k))));
+    if (gen)
+        DISPATCH_STORE(precision, DISPATCH_NT(nt, (batch_step_kernel<S, NT, true><<<grid, NT, 0, st>>>(d_args, d_tiles, ntiles, k))));
+    else
+        DISPATCH_STORE(precision, DISPATCH_NT(nt, (batch_step_kernel<S, NT, false><<<grid, NT, 0, st>>>(d_args, d_tiles, ntiles, k))));
     return cudaGetLastError();
 }
 
 int batch_blocks_per_sm_f32(int precision, int nt) {
     int n = 0;
-    DISPATCH_STORE(precision, DISPATCH_NT(nt, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_step_kernel<S, NT>, NT, 0)));
+    DISPATCH_STORE(precision, DISPATCH_NT(nt, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_step_kernel<S, NT, false>, NT, 0)));
     return n < 1 ? 1 : n;
 }
 

@@ -25,7 +25,10 @@ namespace swb {
 
 cudaError_t launch_fused_step_f64(const StepArgs &a, int k, cudaStream_t st) {
     const int grid = step_grid(a, k);
-    DISPATCH_NT(a.march_nt, (fused_step_kernel<StoreF64, NT><<<grid, NT, 0, st>>>(a, k)));
+    if (step_general(a))
+        DISPATCH_NT(a.march_nt, (fused_step_kernel<StoreF64, NT, true><<<grid, NT, 0, st>>>(a, k)));
+    else
+        DISPATCH_NT(a.march_nt, (fused_step_kernel<StoreF64, NT, false><<<grid, NT, 0, st>>>(a, k)));
     return cudaGetLastError();
 }
 
@@ -68,15 +71,18 @@ cudaError_t launch_pressure_now_f64(const StepArgs &a, double *out, cudaStream_t
     return cudaGetLastError();
 }
 
-cudaError_t launch_batch_step_f64(int nt, const StepArgs *d_args, const TileRef *d_tiles,
+cudaError_t launch_batch_step_f64(int nt, bool gen, const StepArgs *d_args, const TileRef *d_tiles,
                                   int ntiles, int grid, int k, cudaStream_t st) {
-    DISPATCH_NT(nt, (batch_step_kernel<StoreF64, NT><<<grid, NT, 0, st>>>(d_args, d_tiles, ntiles, k)));
+    if (gen)
+        DISPATCH_NT(nt, (batch_step_kernel<StoreF64, NT, true><<<grid, NT, 0, st>>>(d_args, d_tiles, ntiles, k)));
+    else
+        DISPATCH_NT(nt, (batch_step_kernel<StoreF64, NT, false><<<grid, NT, 0, st>>>(d_args, d_tiles, ntiles, k)));
     return cudaGetLastError();
 }
 
 int batch_blocks_per_sm_f64(int nt) {
     int n = 0;
-    DISPATCH_NT(nt, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_step_kernel<StoreF64, NT>, NT, 0));
+    DISPATCH_NT(nt, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_step_kernel<StoreF64, NT, false>, NT, 0));
     return n < 1 ? 1 : n;
 }
 
@@ -158,11 +164,10 @@ __global__ void k_force_sum(PlainState s) {
 __global__ void k_thermal(PlainState s, double k6, double delta, unsigned long long seed,
                           long long t) {
     PLAIN_LOOP(s) {
-        double zx, zy;
-        thermal_normals(seed, c, t, zx, zy);
-        const double sg = thermal_sigma<true, double>(k6, s.h[c], delta);
-        s.Fx[c] = s.Fx[c] - zx * sg;
-        s.Fy[c] = s.Fy[c] - zy * sg;
+        double kx, ky;
+        thermal_force<true, double>(seed, c, t, k6, s.h[c], delta, &kx, &ky);
+        s.Fx[c] = s.Fx[c] - kx;
+        s.Fy[c] = s.Fy[c] - ky;
     }
 }
 

@@ -538,6 +538,13 @@ __device__ __forceinline__ void thermal_normals(unsigned long long seed, long lo
     zy = r * sn;
 }
 
+// thermal!'s force on a cell: (zx, zy) * sigma(h).  Not inlined: the noise
+// (Philox, log, sin/cos) stays out of the register budget of steps without
+// fluctuations.
+template <bool LIT, class R>
+__device__ __noinline__ void thermal_force(unsigned long long seed, long long cell, long long t,
+                                           R k6, R h, R delta, R *fx, R *fy);
+
 // Standard deviation of the thermal force at height h:
 // sqrt(2 kbt mu 6 h / (2h^2 + 6 h delta + 3 delta^2)), in the reference's order.
 template <bool LIT, class R>
@@ -547,6 +554,16 @@ __device__ __forceinline__ R thermal_sigma(R k6, R h, R delta) {
     else
         return sqrtf(qdiv(k6 * h, __fmaf_rn(__fmaf_rn(R(2), h, R(6) * delta), h,
                                              (R(3) * delta) * delta)));
+}
+
+template <bool LIT, class R>
+__device__ __noinline__ void thermal_force(unsigned long long seed, long long cell, long long t,
+                                           R k6, R h, R delta, R *fx, R *fy) {
+    R zx, zy;
+    thermal_normals(seed, cell, t, zx, zy);
+    const R sg = thermal_sigma<LIT, R>(k6, h, delta);
+    *fx = zx * sg;
+    *fy = zy * sg;
 }
 
 // Per-tile constants of the force and collision stage.
@@ -581,7 +598,9 @@ __device__ __forceinline__ CellConst<R> cell_consts(const StepArgs &a, long long
 // equilibrium! and BGKandStream! (src/collide.jl:267-280).  (gpx, gpy) is
 // ∇p at the cell (h∇p!, src/forcing.jl:181-184); *hlo_p the rounding
 // residue of the pulled height (FP32 arithmetic; not read for a fresh step).
-template <class S, bool FRESH, bool TAU1>
+// GEN = false compiles out the rare forces (thermal, inclination) for the
+// common step; the caller guarantees they are off.
+template <class S, bool FRESH, bool TAU1, bool GEN>
 __device__ __forceinline__ void collide_cell(const StepArgs &a,
                                              const CellConst<typename S::real> &cc,
                                              const void *src, void *dst, int gx, int gy, int gxm,
@@ -603,14 +622,13 @@ __device__ __forceinline__ void collide_cell(const StepArgs &a,
         const R sy = (cc.mu6 * h * uy) / den;
         Fx = -hgx - sx;
         Fy = -hgy - sy;
-        if (a.thermal) {  // Fx .= -h∇px .- slipx .- kbtx (scripts/Rivulet_stability.jl:123)
-            R zx, zy;
-            thermal_normals(a.seed, (long long)cell, tt, zx, zy);
-            const R sg = thermal_sigma<true, R>(R(a.k6), h, R(a.delta));
-            Fx = Fx - zx * sg;
-            Fy = Fy - zy * sg;
+        if (GEN && a.thermal) {  // Fx .= -h∇px .- slipx .- kbtx (scripts/Rivulet_stability.jl:123)
+            R kx, ky;
+            thermal_force<true, R>(a.seed, (long long)cell, tt, R(a.k6), h, R(a.delta), &kx, &ky);
+            Fx = Fx - kx;
+            Fy = Fy - ky;
         }
-        if (a.incl) {  // inclination! (src/forcing.jl:364-365)
+        if (GEN && a.incl) {  // inclination! (src/forcing.jl:364-365)
             Fx = Fx + (h * R(a.ax)) * cc.incl_fac;
             Fy = Fy + (h * R(a.ay)) * cc.incl_fac;
         }
@@ -618,14 +636,13 @@ __device__ __forceinline__ void collide_cell(const StepArgs &a,
         const R c = qdiv(cc.mu6 * h, __fmaf_rn(__fmaf_rn(R(2), h, cc.delta6), h, cc.delta3sq));
         Fx = __fmaf_rn(-h, gpx, -(c * ux));
         Fy = __fmaf_rn(-h, gpy, -(c * uy));
-        if (a.thermal) {
-            R zx, zy;
-            thermal_normals(a.seed, (long long)cell, tt, zx, zy);
-            const R sg = thermal_sigma<false, R>(R(a.k6), h, R(a.delta));
-            Fx = __fmaf_rn(-zx, sg, Fx);
-            Fy = __fmaf_rn(-zy, sg, Fy);
+        if (GEN && a.thermal) {
+            R kx, ky;
+            thermal_force<false, R>(a.seed, (long long)cell, tt, R(a.k6), h, R(a.delta), &kx, &ky);
+            Fx = Fx - kx;
+            Fy = Fy - ky;
         }
-        if (a.incl) {
+        if (GEN && a.incl) {
             Fx = __fmaf_rn(h * R(a.ax), cc.incl_fac, Fx);
             Fy = __fmaf_rn(h * R(a.ay), cc.incl_fac, Fy);
         }
@@ -712,7 +729,7 @@ __device__ __forceinline__ void collide_cell(const StepArgs &a,
 // compiled for the iteration's rare cases: FRESH (the first iteration after
 // the fields were set: h, u come from the fields) and TAU1 (τ = 1: the
 // previous populations drop out of the collision).
-template <class S, int NT, bool FRESH, bool TAU1>
+template <class S, int NT, bool FRESH, bool TAU1, bool GEN>
 __device__ __forceinline__ void march_run(const StepArgs &a, int bx, int by, long long done,
                                           MarchSmem<S, NT> &sm) {
     using R = typename S::real;
@@ -745,7 +762,7 @@ __device__ __forceinline__ void march_run(const StepArgs &a, int bx, int by, lon
     const double corr = (!LIT && !FRESH && a.mass_corr) ? __ldcg(&a.ctl->corr[tt & 1]) : 0.0;
     // kappa and cospi(θ) of this column: constant (scalar θ) or θ(x, t) of
     // the moving-wettability mode, which depends on x only
-    const int mode = a.theta_mode;
+    const int mode = GEN ? a.theta_mode : THETA_SCALAR;  // GEN = false: scalar θ
     // θ field: column of this thread and row offset in the (possibly moving) field
     int fsx = 0, fsy = 0;
     if (mode == THETA_FIELD) substrate_shift(a, tt, &fsx, &fsy);
@@ -844,8 +861,8 @@ __device__ __forceinline__ void march_run(const StepArgs &a, int bx, int by, lon
         R gpx, gpy;
         grad9<R>(pc[t - 1], pm[t], pc[t + 1], pp[t], pm[t - 1], pm[t + 1], pp[t + 1], pp[t - 1],
                  gpx, gpy);
-        collide_cell<S, FRESH, TAU1>(a, cc, src, dst, gx, gy, gxm, gxp, cell, tt, h, ux, uy, gpx,
-                                     gpy, &sm.lo[r & 3][t]);
+        collide_cell<S, FRESH, TAU1, GEN>(a, cc, src, dst, gx, gy, gxm, gxp, cell, tt, h, ux, uy,
+                                          gpx, gpy, &sm.lo[r & 3][t]);
         // measures of the height at the start of this iteration
         if (!isfinite(h)) any_nan = 1;
         if (measure) {
@@ -867,27 +884,31 @@ __device__ __forceinline__ void march_run(const StepArgs &a, int bx, int by, lon
                     part.cossum += cos_col;
             }
         }
-    }
+        }
     any_nan = __syncthreads_or(any_nan);
     if (any_nan && t == 0) a.ctl->nan_flag = 1;
     if (measure) write_partials<NT, R>(a, part, tt, by * a.tiles_x + bx, sm.red);
 }
 
-// Iteration done + 1 of strip (bx, by), dispatched on its rare cases.
-template <class S, int NT>
+// Iteration done + 1 of strip (bx, by), dispatched on its rare cases: the
+// first iteration after the fields were set (FRESH) and τ = 1 (TAU1).  GEN
+// is chosen per launch by the host (step_general): the common kernel
+// (scalar θ, no thermal noise, no inclination) leaves that code out and so
+// needs fewer registers, which keeps more CTAs per SM.
+template <class S, int NT, bool GEN>
 __device__ __forceinline__ void march_tile(const StepArgs &a, int bx, int by, long long done,
                                            MarchSmem<S, NT> &sm) {
     const bool fresh = done + 1 == __ldcg(&a.ctl->fresh_step);
     if (fresh) {
         if (a.tau_is_one)
-            march_run<S, NT, true, true>(a, bx, by, done, sm);
+            march_run<S, NT, true, true, GEN>(a, bx, by, done, sm);
         else
-            march_run<S, NT, true, false>(a, bx, by, done, sm);
+            march_run<S, NT, true, false, GEN>(a, bx, by, done, sm);
     } else {
         if (a.tau_is_one)
-            march_run<S, NT, false, true>(a, bx, by, done, sm);
+            march_run<S, NT, false, true, GEN>(a, bx, by, done, sm);
         else
-            march_run<S, NT, false, false>(a, bx, by, done, sm);
+            march_run<S, NT, false, false, GEN>(a, bx, by, done, sm);
     }
 }
 
@@ -1031,8 +1052,8 @@ __device__ __forceinline__ void tile2d_run(const StepArgs &a, int bx, int by, lo
         const R *pc = sm.p + (oy + 1) * kT2PX + ox + 1, *pm = pc - kT2PX, *pp = pc + kT2PX;
         R gpx, gpy;
         grad9<R>(pc[-1], pm[0], pc[1], pp[0], pm[-1], pm[1], pp[1], pp[-1], gpx, gpy);
-        collide_cell<S, FRESH, TAU1>(a, cc, src, dst, gx, gy, gxm, gxp, cell, tt, h, ux, uy, gpx,
-                                     gpy, &sm.lo[o]);
+        collide_cell<S, FRESH, TAU1, true>(a, cc, src, dst, gx, gy, gxm, gxp, cell, tt, h, ux, uy,
+                                           gpx, gpy, &sm.lo[o]);
         if (!isfinite(h)) any_nan = 1;
         if (measure) {
             mass_add(part, h);
@@ -1179,7 +1200,7 @@ __global__ void __launch_bounds__(NT, T2D ? 2 : 1) fused_run_kernel(const StepAr
             if constexpr (T2D)
                 tile2d_tile<S>(a, e % a.tiles_x, e / a.tiles_x, base + k, sm);
             else
-                march_tile<S, NT>(a, e % a.tiles_x, e / a.tiles_x, base + k, sm);
+                march_tile<S, NT, true>(a, e % a.tiles_x, e / a.tiles_x, base + k, sm);
             __syncthreads();
         }
         if (!grid_barrier(a.bar, &a.ctl->bar_err, (unsigned int)G)) return;
@@ -1193,7 +1214,7 @@ __global__ void __launch_bounds__(NT, T2D ? 2 : 1) fused_run_kernel(const StepAr
 
 // Single lattice: one CTA per strip, plus (when measures are kept and k > 0)
 // a reducer CTA, block 0, for the previous iteration's measures.
-template <class S, int NT>
+template <class S, int NT, bool GEN>
 __global__ void __launch_bounds__(NT) fused_step_kernel(const StepArgs a, int k) {
     __shared__ MarchSmem<S, NT> sm;
     int b = blockIdx.x;
@@ -1204,7 +1225,7 @@ __global__ void __launch_bounds__(NT) fused_step_kernel(const StepArgs a, int k)
         }
         b -= 1;
     }
-    march_tile<S, NT>(a, b % a.tiles_x, b / a.tiles_x, a.ctl->step_base + k, sm);
+    march_tile<S, NT, GEN>(a, b % a.tiles_x, b / a.tiles_x, a.ctl->step_base + k, sm);
 }
 
 // Closes a sequence of n step launches: the last iteration's measures, then
@@ -1220,7 +1241,7 @@ __global__ void __launch_bounds__(NT) advance_kernel(const StepArgs a, int n) {
 
 // Batch: persistent CTAs walk a packed table of strips of many lattices;
 // entries with tx = -1 reduce their lattice's previous iteration.
-template <class S, int NT>
+template <class S, int NT, bool GEN>
 __global__ void __launch_bounds__(NT) batch_step_kernel(const StepArgs *__restrict__ args,
                                                         const TileRef *__restrict__ tiles,
                                                         int ntiles, int k) {
@@ -1231,7 +1252,7 @@ __global__ void __launch_bounds__(NT) batch_step_kernel(const StepArgs *__restri
         if (threadIdx.x == 0) sa = args[tr.lattice];
         __syncthreads();
         if (tr.tx >= 0)
-            march_tile<S, NT>(sa, tr.tx, tr.ty, sa.ctl->step_base + k, sm);
+            march_tile<S, NT, GEN>(sa, tr.tx, tr.ty, sa.ctl->step_base + k, sm);
         else if (k > 0)
             reduce_step<NT>(sa, sa.ctl->step_base + k, sm.redd);
         __syncthreads();

@@ -29,6 +29,8 @@ SWB_F64, SWB_F32, SWB_F16, SWB_PLAIN64 = 0, 1, 2, 3
 FIELD = {"height": 0, "velx": 1, "vely": 2, "pressure": 3, "fout": 4, "feq": 5, "Fx": 6, "Fy": 7,
          "slipx": 8, "slipy": 9, "h∇px": 10, "h∇py": 11, "vsq": 12}
 
+FIELD_HEIGHT, FIELD_VELX, FIELD_VELY, FIELD_PRESSURE, FIELD_FOUT = 0, 1, 2, 3, 4
+
 MEAS_MASS, MEAS_WETTED, MEAS_MAXMIN, MEAS_AREA, MEAS_ALL = 1, 2, 4, 8, 15
 STEP_AUTO, STEP_PER_ITERATION, STEP_MULTI = 0, 1, 2
 
@@ -135,6 +137,15 @@ def lib() -> C.CDLL:
             "swb_op_thermal": (i, [p, i64]),
             "swb_batch_set_geometry": (i, [p, i, i]),
             "swb_set_substrate_motion": (i, [p, i64, i, i]),
+            "swb_set_snapshots": (i, [p, i64, i64]),
+            "swb_get_snapshots": (i, [p, p, i64, C.POINTER(i64), p]),
+            "swb1d_create": (i, [C.POINTER(Params), i, i, i, C.POINTER(p)]),
+            "swb1d_destroy": (i, [p]),
+            "swb1d_set_field": (i, [p, i, i, p]),
+            "swb1d_get_field": (i, [p, i, i, p]),
+            "swb1d_step": (i, [p, i64]),
+            "swb1d_sync": (i, [p]),
+            "swb1d_get_measures": (i, [p, i, p, i64, C.POINTER(i64)]),
             "swb_server_poll": (i, [p, i64, p, C.POINTER(RequestInfo)]),
             "swb_server_cancel": (i, [p, i64]),
             "swb_server_stats_get": (i, [p, C.POINTER(ServerStats)]),

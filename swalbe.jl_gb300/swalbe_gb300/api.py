@@ -9,6 +9,7 @@ same: ``Sys(sys, "GB300")`` instead of ``Sys(sys, "GPU")``, then
 from __future__ import annotations
 
 import ctypes as C
+import functools
 import math
 from typing import Callable, Optional, Sequence
 
@@ -218,6 +219,32 @@ class GB300State:
         self._chk(lib().swb_get_step_mode(self._h, C.byref(a)))
         return {1: "per_iteration", 2: "multi"}[a.value]
 
+    def set_snapshots(self, dumping: int, capacity: int = 64) -> None:
+        """snapshot!(fluid, height, t; dumping) on the device: the height
+        after every `dumping`-th iteration goes into a device ring of
+        `capacity` fields (0 turns it off)."""
+        self._chk(lib().swb_set_snapshots(self._h, int(dumping), int(capacity)))
+
+    def snapshots(self, cap: int = 1 << 12):
+        """(times, rows): the snapshots taken since the last call, oldest
+        first; row k is vec(h) (column-major) as in the reference's snapshot
+        matrix."""
+        n = self.shape[0] * self.shape[1]
+        out = []
+        times = []
+        while True:
+            k = min(cap, 64)
+            buf = np.empty((k, n))
+            ts = np.empty(k, dtype=np.int64)
+            cnt = C.c_int64()
+            self._chk(lib().swb_get_snapshots(self._h, buf.ctypes.data, k, C.byref(cnt),
+                                              ts.ctypes.data))
+            out.append(buf[:cnt.value])
+            times.extend(ts[:cnt.value].tolist())
+            if cnt.value < k:
+                break
+        return times, np.concatenate(out, axis=0)
+
     def set_thermal_seed(self, seed: int) -> None:
         """Key of the thermal noise stream (Philox-4x32-10; counter = cell, iteration)."""
         self._chk(lib().swb_set_thermal_seed(self._h, int(seed)))
@@ -261,6 +288,11 @@ class GB300State:
 
 
 def Sys(sysc: SysConst, device: str = "GB300", T=np.float64, kind: str = "simple") -> GB300State:
+    from . import d1
+    if isinstance(sysc, d1.SysConst_1D):  # Sys(sysc::SysConst_1D; T, kind)
+        if kind != "simple":
+            raise NotImplementedError(f"kind={kind!r}: 1D states are 'simple' (use set_gamma for γ fields)")
+        return d1.State1D(sysc, T)
     """Sys(sysc, device; T, kind) (src/initialize.jl:491-572): zero populations, h = 1.
 
     kind="thermal" adds thermal!'s fluctuating forces every iteration when
@@ -353,7 +385,8 @@ def surfacearea_(state: GB300State, hthresh: float = 0.055):
 
 # ------------------------------------------------------------------ time loop
 def time_loop(sysc: SysConst, state: GB300State, *args, verbose: bool = False):
-    """time_loop(sys, state[, θ | Δh | f, measure]) (src/simulate.jl:6-96).
+    """time_loop(sys, state[, θ | Δh | f, measure]) (src/simulate.jl:6-96);
+    a SysConst_1D dispatches to the 1D method (src/simulate.jl:98-179).
 
     - ``time_loop(sys, state)``: θ = sys.param.θ;
     - ``time_loop(sys, state, θ)``: θ a number or an Lx x Ly array;
@@ -362,6 +395,9 @@ def time_loop(sysc: SysConst, state: GB300State, *args, verbose: bool = False):
       each step; ``wetted_`` and ``inclination_`` run fused on the device, any
       other callable needs a ``"GB300-plain"`` state (it is called between ops).
     """
+    from . import d1
+    if isinstance(sysc, d1.SysConst_1D):
+        return d1.time_loop(sysc, state, *args, verbose=verbose)
     P = sysc.param
     Tmax = P.Tmax
     mask = L.MEAS_MASS
@@ -420,6 +456,9 @@ def _plain_iteration_with_callback(sysc, state, f: Callable, measure):
 
 # ------------------------------------------------------------------ initial values
 def singledroplet(height: np.ndarray, radius, θ, center) -> np.ndarray:
+    if np.ndim(height) == 1:  # singledroplet(height::Vector, ...) (src/initialvalues.jl:226-243)
+        from .d1 import singledroplet_1d
+        return singledroplet_1d(np.asarray(height, dtype=np.float64), radius, θ, center)
     """singledroplet(height, radius, θ, center) (src/initialvalues.jl:203-224); 1-based center."""
     lx, ly = height.shape
     i = np.arange(1, lx + 1, dtype=np.float64)[:, None]
@@ -448,13 +487,42 @@ def two_caps(Lx: int, Ly: int, r1, r2, θ1, θ2, c1, c2) -> np.ndarray:
     return np.asfortranarray(np.where(h < 0, 0.05, h))
 
 
+# ------------------------------------------------------------------ snapshots / restart
+def snapshot_(snap: np.ndarray, field, t: int, dumping: int = 1000) -> None:
+    """snapshot!(snap, field, t; dumping) (src/measures.jl:99-105): row
+    t ÷ dumping (1-based) of `snap` becomes vec(field) when t % dumping == 0."""
+    if t % dumping == 0:
+        snap[t // dumping - 1, :] = np.asarray(field).ravel(order="F")
+
+
+def save_snapshots(path: str, times, rows) -> None:
+    """Snapshots as an .npz archive with one vec(h) per key "h_<t>" (the key
+    names restart_from_height reads, src/initialvalues.jl:358-382)."""
+    np.savez(path, **{f"h_{int(t)}": np.asarray(r) for t, r in zip(times, rows)})
+
+
+def restart_from_height(data, kind: str = "npz", timestep: int = 0, size=(512, 512)):
+    """restart_from_height(data; kind, timestep, size) (src/initialvalues.jl:
+    358-382): the height stored under "h_<timestep>", or the last stored one
+    for timestep = 0, reshaped to `size` (column-major).  Archives written by
+    save_snapshots (kind "npz"); the reference's JLD2 (HDF5) and BSON
+    containers need readers this package does not bundle."""
+    if kind != "npz":
+        raise NotImplementedError(f"kind={kind!r}: only .npz snapshot archives are read here")
+    with np.load(data) as f:
+        keys = list(f.keys())
+        key = keys[-1] if timestep == 0 else f"h_{int(timestep)}"
+        return np.asfortranarray(np.asarray(f[key]).reshape(size, order="F"))
+
+
 # ------------------------------------------------------------------ substrate patterns
 # boxpattern / ellipsepattern / trianglepattern (src/initialvalues.jl:423-581)
 # build a contact-angle field with a patch of θ0 + δa.  The reference tests
 # membership of the lattice point (i, j) (1-based) in a LazySets polygon or
 # ellipsoid and writes θ[j, i] (rows and columns swapped, kept here), and it
 # moves vertices that fall off the lattice onto coordinate 1 (x first; y only
-# when x was on the lattice).
+# when x was on the lattice).  Because of the swapped write the reference's generators need a
+# square field (a rectangular one runs out of bounds there and here).
 class Polygon:
     """Convex polygon (the convex hull of its vertices, closed)."""
 
@@ -557,6 +625,22 @@ def _new(sysc, device, T):
     return Sys(sysc, device, T=T)
 
 
+def _one_dim(name):
+    """The reference dispatches the drivers on the system type; a
+    SysConst_1D call goes to the 1D method of the same name (which, as in
+    the reference, takes no device argument)."""
+    def deco(fn2d):
+        @functools.wraps(fn2d)
+        def wrapper(sysc, *args, **kw):
+            from . import d1
+            if isinstance(sysc, d1.SysConst_1D):
+                return getattr(d1, name)(sysc, *args, **kw)
+            return fn2d(sysc, *args, **kw)
+        return wrapper
+    return deco
+
+
+@_one_dim("run_flat")
 def run_flat(sysc: SysConst, device: str = "GB300", verbos: bool = True, T=np.float64):
     """run_flat(sys, device) (src/simulate.jl:236-245)."""
     state = _new(sysc, device, T)
@@ -565,6 +649,7 @@ def run_flat(sysc: SysConst, device: str = "GB300", verbos: bool = True, T=np.fl
     return state.height
 
 
+@_one_dim("run_random")
 def run_random(sysc: SysConst, device: str = "GB300", h0=1.0, ϵ=0.01, verbos=True, T=np.float64,
                rng=None):
     """run_random(sys, device; h₀, ϵ) (src/simulate.jl:286-294); θ = 1/9 as there."""
@@ -576,6 +661,7 @@ def run_random(sysc: SysConst, device: str = "GB300", h0=1.0, ϵ=0.01, verbos=Tr
     return state.height
 
 
+@_one_dim("run_rayleightaylor")
 def run_rayleightaylor(sysc: SysConst, device: str = "GB300", kx=15, ky=18, h0=1.0, ϵ=0.001,
                        verbos=True, T=np.float64):
     """run_rayleightaylor(sys, device; kx, ky, h₀, ϵ) (src/simulate.jl:338-358)."""
@@ -589,6 +675,7 @@ def run_rayleightaylor(sysc: SysConst, device: str = "GB300", kx=15, ky=18, h0=1
     return state.height, diff
 
 
+@_one_dim("run_dropletrelax")
 def run_dropletrelax(sysc: SysConst, device: str = "GB300", radius=20, theta0=1 / 6, center=None,
                      verbos=True, T=np.float64):
     """run_dropletrelax(sys, device; radius, theta0, center) (src/simulate.jl:384-399)."""

@@ -30,6 +30,7 @@ UNITS = {
     "swb_server.cu": [],
     "swb_noalloc.cu": [],
     "swb_analysis.cu": [],
+    "swb_d1q3.cu": ["--fmad=false"],
 }
 
 
