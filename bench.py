@@ -57,8 +57,8 @@ def parse():
     ap.add_argument("--step-mode", default="per_iteration", choices=["per_iteration", "multi"],
                     help="launch form for --profile-case")
     ap.add_argument("--case-steps", type=int, default=12)
-    ap.add_argument("--workload", choices=["ensemble", "serving"],
-                    help="print the ensemble (config 4) or serving (config 5) line only")
+    ap.add_argument("--workload", choices=["ensemble", "serving", "spinodal"],
+                    help="print the ensemble, serving or spinodal-comparison line only")
     return ap.parse_args()
 
 
@@ -423,7 +423,7 @@ def side_runs(sw, L, np, torch, hbm):
 
 
 def ensemble_run(sw, np, count=512, steps=200, plain_sample=8):
-    """Config 4: `count` two-cap coalescence lattices (128², 256², 512²,
+    """Coalescence ensemble: `count` two-cap lattices (128², 256², 512²,
     1024x256) advanced together in FP32 by the batch kernel, against the
     plain one-at-a-time paths on a sample of the same instances."""
     from swalbe_gb300 import configs
@@ -534,11 +534,53 @@ def serving_run(sw, np, duration=12.0, rate=200.0, budget=24 << 30, steps_per_ti
     return res
 
 
+def spinodal_run(sw, np, L_, steps=100000):
+    """Spinodal dewetting of a 2048² film (h = 1 + U[-0.1, 0.1], seed 3,
+    γ = 0.01, θ = 1/9): FP32 and FP16-storage runs against the Float64 run
+    of the same film, after `steps` iterations: relative L2 of h, mass drift
+    (FP64 sums of the per-iteration mass), droplets (h > 0.055, periodic
+    8-connected)."""
+    from swalbe_gb300 import configs
+    sysc, h0, _ = configs.spinodal_2048()
+    out = {"steps": steps, "lattice": [sysc.Lx, sysc.Ly]}
+    res = {}
+    for name, T in (("f64", np.float64), ("f32", np.float32), ("f16", np.float16)):
+        st = sw.Sys(sysc, "GB300", T=T)
+        st.set_measures(L_.MEAS_MASS)
+        st.height = h0
+        t0 = time.perf_counter()
+        done, masses = 0, []
+        while done < steps:
+            n = min(20000, steps - done)
+            st.step(n)
+            masses += [r.mass for r in st.measures()]
+            done += n
+        st.sync()
+        dt = time.perf_counter() - t0
+        h = st.height
+        m = np.array(masses)
+        res[name] = h
+        out[name] = {"seconds": dt, "MLUPS": sysc.Lx * sysc.Ly * steps / dt / 1e6,
+                     "mass_drift_max": float(np.abs(m - m[0]).max() / m[0]),
+                     "droplets": sw.count_droplets(h), "hmax": float(h.max()),
+                     "hmin": float(h.min())}
+        del st
+    ref = res["f64"]
+    for name in ("f32", "f16"):
+        out[name]["rel_l2_h_vs_f64"] = float(np.linalg.norm(res[name] - ref) / np.linalg.norm(ref))
+    return out
+
+
 def run_workload(args):
     import numpy as np
 
     import swalbe_gb300 as sw
+    from swalbe_gb300 import _lib as L_
     sw.build()
+    if args.workload == "spinodal":
+        r = spinodal_run(sw, np, L_, steps=args.case_steps if args.case_steps != 12 else 100000)
+        print(json.dumps({"workload": "spinodal_2048", **r}), flush=True)
+        return
     if args.workload == "ensemble":
         r = ensemble_run(sw, np)
         line = {"metric": "MLUPS", "value": r["batch_f32"]["MLUPS"], "unit": "MLUPS",

@@ -1,4 +1,4 @@
-"""Seeded synthetic inputs for the five benchmark configurations.
+"""Seeded synthetic inputs for the benchmark workloads.
 
 The reference publishes no benchmark inputs; these generators produce the
 shapes, sizes and value distributions each configuration describes, from
@@ -20,7 +20,7 @@ CAP_HMAX = 20.0
 
 
 def droplet_relax_256():
-    """Config 1: 256², Float64, τ=1, γ=0.01, δ=1, θ=1/9, n=9, m=3, hmin=0.1,
+    """Relaxing droplet: 256², Float64, τ=1, γ=0.01, δ=1, θ=1/9, n=9, m=3, hmin=0.1,
     hcrit=0.05; h = max(0.05, cap) of a sphere R=60 centred at (128, 128)
     (1-based) with apex height 20 ⇒ θ0 = acos(1 - 20/60)/π; 10,000 steps.
 
@@ -35,14 +35,14 @@ def droplet_relax_256():
 
 
 def rayleigh_taylor_512(seed: int = 2):
-    """Config 2: 512², g=-0.001, γ=0.0005, θ=1/9, h = 1 + U[-0.01, 0.01]."""
+    """Rayleigh–Taylor film: 512², g=-0.001, γ=0.0005, θ=1/9, h = 1 + U[-0.01, 0.01]."""
     sysc = SysConst(512, 512, Taumucs(Tmax=50000, tdump=5000, g=-0.001, gamma=0.0005))
     rng = np.random.default_rng(seed)
     return sysc, np.asfortranarray(1.0 + rng.uniform(-0.01, 0.01, (512, 512))), 50000
 
 
 def spinodal_2048(seed: int = 3):
-    """Config 3: 2048², γ=0.01, θ=1/9, h = 1 + U[-0.1, 0.1], 100,000 steps."""
+    """Spinodal dewetting film: 2048², γ=0.01, θ=1/9, h = 1 + U[-0.1, 0.1], 100,000 steps."""
     sysc = SysConst(2048, 2048, Taumucs(Tmax=100000, tdump=10000))
     rng = np.random.default_rng(seed)
     return sysc, np.asfortranarray(1.0 + rng.uniform(-0.1, 0.1, (2048, 2048))), 100000
@@ -55,7 +55,7 @@ class EnsembleMember:
 
 
 def ensemble(count: int = 512, seed: int = 4, steps: int = 20000) -> Tuple[List[EnsembleMember], int]:
-    """Config 4: `count` coalescence instances; sizes from {128², 256², 512²,
+    """Coalescence ensemble: `count` instances; sizes from {128², 256², 512²,
     1024x256}; two caps of sphere radii U[0.15, 0.40]·Ly (scaled down where
     both would not fit side by side, or where the taller cap would exceed
     CAP_HMAX) separated by an edge gap of U{2..10} cells; θ ~ U[1/18, 1/4]
@@ -92,7 +92,7 @@ def ensemble(count: int = 512, seed: int = 4, steps: int = 20000) -> Tuple[List[
         left = (Lx - (2 * a1 + gap + 2 * a2)) / 2  # the pair is centred in x
         c1 = (left + a1, Ly / 2)
         c2 = (left + 2 * a1 + gap + a2, Ly / 2)
-        # the precursor floor max(0.05, ·) as in config 1: combining caps with
+        # the precursor floor max(0.05, ·) as in the droplet case: combining caps with
         # the reference's rule (clamp only negatives) leaves rim cells of
         # ~1e-6 height, where u = j/h diverges within a few steps
         h0 = np.asfortranarray(np.maximum(two_caps(Lx, Ly, r1, r2, th, th, c1, c2), 0.05))
@@ -121,7 +121,7 @@ class Request:
 def serving_stream(rate: float = 200.0, duration: float = 10.0, seed: int = 5,
                    side_choices: Optional[List[int]] = None, step_range=(1000, 100000),
                    h_amp: float = 0.05) -> List[Request]:
-    """Config 5: Poisson arrivals (mean `rate`/s); Lx, Ly uniform on multiples
+    """Serving stream: Poisson arrivals (mean `rate`/s); Lx, Ly uniform on multiples
     of 64 in [64, 2048]; steps uniform in `step_range`; θ0 ~ U[1/18, 1/4];
     g ~ U[-1e-3, 0]; moving wettability θ(x,t) = θ0 + Δθ sin(2π(x - v t)/Lx)
     with Δθ = 1/36, v = 1/98 (scripts/Moving_wettability_structs.jl:183-186);
@@ -142,3 +142,12 @@ def serving_stream(rate: float = 200.0, duration: float = 10.0, seed: int = 5,
         reqs.append(Request(t, SysConst(Lx, Ly, Taumucs(Tmax=steps, theta=th0, g=g)), steps, th0,
                             sub, h_amp))
     return reqs
+
+
+def shard(items: list, rank: int, world: int) -> list:
+    """The share of independent simulations (ensemble members, requests) rank
+    `rank` of `world` runs: round robin, so every rank gets lattices of every
+    size.  No data moves between ranks."""
+    if world < 1 or not 0 <= rank < world:
+        raise ValueError("need 0 <= rank < world")
+    return list(items)[rank::world]
