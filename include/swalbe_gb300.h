@@ -166,12 +166,12 @@ int swb_set_inclination(swb_state *s, double ax, double ay, int loop_time, int64
 /* Geometry of the fused step: CTAs of nt threads (64, 128, 256) own strips
  * of nt-4 columns and h rows (4..512) that they march row by row; or, with
  * nt = 32 (SWB_F32 / SWB_F16 only; h is ignored), CTAs of 256 threads own
- * 2D tiles of 32 x 16 cells whose loads are all issued at once.  By default SWB_F64 / SWB_F32
+ * 2D tiles of 32 x 16 cells whose loads are all issued at once.  By default
  * states autotune it on their first swb_step of >= 512 steps (timing a few
- * geometries on those real steps; remembered per lattice size), and SWB_F16
- * states use a size rule.  Setting it (or (0, 0): the size rule) turns the
- * autotuner off.  Results do not depend on it, except through the order of
- * the FP64 mass sum that drives the SWB_F16 mass correction. */
+ * geometries on those real steps; remembered per lattice size).  Setting it
+ * (or (0, 0): a size rule) turns the autotuner off.  Results do not depend
+ * on it: the per-cell arithmetic is the same in every form, and the mass that
+ * drives the SWB_F32 / SWB_F16 mass correction is an exact fixed-point sum. */
 int swb_set_geometry(swb_state *s, int nt, int h);
 int swb_get_geometry(swb_state *s, int *nt, int *h);
 
@@ -196,9 +196,13 @@ int swb_set_step_mode(swb_state *s, int mode);
 int swb_get_step_mode(swb_state *s, int *mode);
 
 /* SWB_F32 / SWB_F16: hold the total mass at its value when the fields were
- * last set, by an FP64-measured correction spread over the cells (default:
- * on for SWB_F16; off for SWB_F32, whose compensated f0 closure already
- * conserves mass to ~1e-12; no effect in SWB_F64, the reference's arithmetic). */
+ * last set, by a correction spread over the cells, two iterations behind
+ * the measurement (default: on for SWB_F16, whose FP16 populations cannot
+ * hold the rounding residues; off for SWB_F32, whose populations keep the
+ * mass to ~1e-12 relative without it).  The mass is measured exactly (a
+ * fixed-point sum in units of 2^-32 per cell), so the correction, and the
+ * results, do not depend on the geometry.  It costs a reduction per
+ * iteration.  No effect in SWB_F64, the reference's arithmetic. */
 int swb_set_mass_correction(swb_state *s, int on);
 
 /* Which measures swb_step records each iteration (SWB_MEAS_* mask). */
@@ -290,7 +294,6 @@ int swb_batch_step(swb_batch *b, int64_t nsteps);
 /* Waits for the batch; SWB_ERR_NAN (lattice index in swb_last_error) if a
  * lattice saw a non-finite height. */
 int swb_batch_sync(swb_batch *b);
-/* Tile shape chosen by the autotuner (0 until the first step). */
 /* Strips of every lattice: nt threads (64, 128, 256; nt - 4 columns) and
  * `rows` rows (4..512, capped at each lattice's height).  Default 64 x 32:
  * the batch's parallelism comes from its many lattices, so strips are tall. */

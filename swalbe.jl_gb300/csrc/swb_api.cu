@@ -632,8 +632,7 @@ int autotune_geometry(swb_state *s, long long &left) {
 int fused_steps(swb_state *s, long long nsteps) {
     long long left = nsteps;
     const long long steps0 = s->steps;
-    if (!s->tuned && s->autotune && left >= kTuneMinSteps &&
-        (s->precision == SWB_F64 || s->precision == SWB_F32)) {
+    if (!s->tuned && s->autotune && left >= kTuneMinSteps) {
         int rc = autotune_geometry(s, left);
         if (rc) return rc;
     }
@@ -748,6 +747,7 @@ int swb_create(const swb_params *p, int precision, swb_state **out) {
     s->pitch = pitch_of(s->N);
     fill_args_from_params(s->a, *p);
     s->a.pitch = s->pitch;
+    s->a.mass_fixed = (precision == SWB_F32 || precision == SWB_F16) ? 1 : 0;
     s->a.mass_corr = (precision == SWB_F16) ? 1 : 0;
     auto bad = [&](int code) {
         std::string m = s->err.empty() ? g_err : s->err;

@@ -241,10 +241,7 @@ int layout(swb1d *b, int i, char *base) {
     a.h = base + o; o += al((size_t)L * rb);
     a.u = base + o; o += al((size_t)L * rb);
     a.p = base + o; o += al((size_t)L * rb);
-    char *kap = base + o; o += al((size_t)L * rb);
-    char *gam = base + o; o += al((size_t)L * rb);
-    char *dg = base + o; o += al((size_t)L * rb);
-    (void)kap; (void)gam; (void)dg;
+    o += 3 * al((size_t)L * rb);  // κ, γ, ∇γ: addressed through field_ptr
     a.rec = b->rec_cap ? reinterpret_cast<Record *>(base + o) : nullptr;
     a.rec_cap = b->rec_cap;
     return SWB_OK;

@@ -79,6 +79,7 @@ struct StepArgs {
     int meas_mask;
     double hthresh;
     int mass_corr;
+    int mass_fixed;           // FP32 arithmetic: block masses are fixed-point sums (kMassUnit)
     double *partials;         // [2][max_tiles][kNPart]: slot by iteration parity
     Record *records;          // ring of rec_cap records (may be null if meas_mask == 0)
     int rec_cap;

@@ -90,6 +90,7 @@ inline StepArgs lattice_args(const swb_params &p, int precision, char *base, con
     a.thermal = p.kbt > 0.0 ? 1 : 0;
     a.k6 = ((2.0 * p.kbt) * p.mu) * 6.0;  // src/forcing.jl:300-302, left to right
     a.seed = 0;
+    a.mass_fixed = (precision == SWB_F32 || precision == SWB_F16) ? 1 : 0;
     a.mass_corr = (precision == SWB_F16) ? 1 : 0;
     a.records = nullptr;
     a.rec_cap = 0;

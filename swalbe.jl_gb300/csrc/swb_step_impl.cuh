@@ -291,29 +291,56 @@ __device__ __forceinline__ unsigned int mix32(unsigned int a, unsigned int b) {
     return x;
 }
 
-// v + c with stochastic rounding to the ulp of v (c is far below one ulp:
-// the per-cell share of the mass correction).
+// v + c with stochastic rounding to the ulp of v: c (a few ulp at most: the
+// rounding residues of the cell and its share of the mass correction) is
+// rounded down or up to a multiple of ulp(v) with probabilities that make the
+// result exact in expectation.  ulp(v) and 1/ulp(v) are powers of two built
+// from v's exponent field, so c / ulp is exact.
 __device__ __forceinline__ float add_stochastic(float v, float c, unsigned int rnd) {
-    int ex = (__float_as_int(v) >> 23) & 0xff;
-    float ulp = __int_as_float(max(ex - 23, 1) << 23);
-    float r = c * __frcp_rn(ulp);
-    float fl = floorf(r);
-    float u = (float)(rnd >> 8) * (1.0f / 16777216.0f);
-    float k = fl + ((u < r - fl) ? 1.0f : 0.0f);
-    return v + k * ulp;
+    const int eu = max(((__float_as_int(v) >> 23) & 0xff) - 23, 1);  // exponent field of ulp(v)
+    const float ulp = __int_as_float(eu << 23);
+    const float r = c * __int_as_float((254 - eu) << 23);
+    const float fl = floorf(r);
+    const float u = (float)(rnd >> 8) * (1.0f / 16777216.0f);
+    const float k = fl + ((u < r - fl) ? 1.0f : 0.0f);
+    return __fmaf_rn(k, ulp, v);
 }
 
 // ------------------------------------------------------------ reductions
-// Per-block partial measures in the compute type R.  The mass is a two-term
-// (hi + lo) compensated sum so that FP32 blocks keep FP64-grade mass; only the
-// per-block result is converted to double, which keeps FP64 instructions (1/64
-// of the FP32 rate on GB300) out of the per-cell path.
+// Per-block partial measures in the compute type R.  Float64 states sum the
+// mass as a two-term (hi + lo) compensated sum.  FP32-arithmetic states sum it
+// in fixed point instead: each cell's h and rounding residue are converted to
+// integers in units of 2^-32 and added as 64-bit integers, so the sum is exact
+// and does not depend on the order of the additions.  The strip geometry, the
+// 2D tiles, a batch's layout and the reduction trees then all give the same
+// bits for the mass, and so for the mass correction that is driven by it:
+// FP32 results do not depend on how the lattice is cut into CTAs.  Only the
+// per-block result leaves the compute type, which keeps FP64 instructions
+// (1/64 of the FP32 rate on GB300) out of the per-cell path.
 template <class R>
 struct PartT {
     R mhi, mlo;
     int wet;
     R hmax, hmin, area, cossum;
 };
+
+// FP32 cells: the mass in units of kMassUnit.  A block holds at most
+// 252 x 512 cells, so the 64-bit sum is exact for mean heights below 1.6e4.
+constexpr float kMassScale = 0x1p32f;
+constexpr double kMassUnit = 0x1p-32;
+struct PartQ {
+    long long mq;
+    int wet;
+    float hmax, hmin, area, cossum;
+};
+
+// The per-cell partials of the step kernels of compute type R.
+template <class R>
+struct StepPartSel { using type = PartT<R>; };
+template <>
+struct StepPartSel<float> { using type = PartQ; };
+template <class R>
+using StepPart = typename StepPartSel<R>::type;
 
 template <class R>
 __device__ __forceinline__ void part_init(PartT<R> &p) {
@@ -324,6 +351,15 @@ __device__ __forceinline__ void part_init(PartT<R> &p) {
     p.hmin = R(INFINITY);
     p.area = R(0);
     p.cossum = R(0);
+}
+
+__device__ __forceinline__ void part_init(PartQ &p) {
+    p.mq = 0;
+    p.wet = 0;
+    p.hmax = -INFINITY;
+    p.hmin = INFINITY;
+    p.area = 0.0f;
+    p.cossum = 0.0f;
 }
 
 // (s, e) = a + b exactly (Knuth's TwoSum).
@@ -342,6 +378,19 @@ __device__ __forceinline__ void mass_add(PartT<R> &p, R v) {
     p.mlo = p.mlo + e;
 }
 
+// h of a cell: v * 2^32 is exact (a power-of-two scaling) and an integer for
+// v >= 2^-9; the conversion rounds smaller heights to the unit.
+__device__ __forceinline__ void mass_add(PartQ &p, float v) {
+    p.mq += __float2ll_rn(v * kMassScale);
+}
+
+// The rounding residue of a cell's pulled height (a few ulp of h).
+template <class R>
+__device__ __forceinline__ void mass_add_lo(PartT<R> &p, R lo) { p.mlo = p.mlo + lo; }
+__device__ __forceinline__ void mass_add_lo(PartQ &p, float lo) {
+    p.mq += __float2ll_rn(lo * kMassScale);
+}
+
 template <class R>
 __device__ __forceinline__ void part_merge(PartT<R> &a, const PartT<R> &b) {
     R s, e;
@@ -351,6 +400,15 @@ __device__ __forceinline__ void part_merge(PartT<R> &a, const PartT<R> &b) {
     a.wet += b.wet;
     a.hmax = fmax(a.hmax, b.hmax);
     a.hmin = fmin(a.hmin, b.hmin);
+    a.area += b.area;
+    a.cossum += b.cossum;
+}
+
+__device__ __forceinline__ void part_merge(PartQ &a, const PartQ &b) {
+    a.mq += b.mq;
+    a.wet += b.wet;
+    a.hmax = fmaxf(a.hmax, b.hmax);
+    a.hmin = fminf(a.hmin, b.hmin);
     a.area += b.area;
     a.cossum += b.cossum;
 }
@@ -368,16 +426,90 @@ __device__ __forceinline__ PartT<R> part_shfl(const PartT<R> &p, int off) {
     return o;
 }
 
+__device__ __forceinline__ PartQ part_shfl(const PartQ &p, int off) {
+    PartQ o;
+    o.mq = __shfl_down_sync(0xffffffffu, p.mq, off);
+    o.wet = __shfl_down_sync(0xffffffffu, p.wet, off);
+    o.hmax = __shfl_down_sync(0xffffffffu, p.hmax, off);
+    o.hmin = __shfl_down_sync(0xffffffffu, p.hmin, off);
+    o.area = __shfl_down_sync(0xffffffffu, p.area, off);
+    o.cossum = __shfl_down_sync(0xffffffffu, p.cossum, off);
+    return o;
+}
+
+// The mass slot of a block partial: a double, or the 64 bits of the
+// fixed-point sum.
+template <class R>
+__device__ __forceinline__ double part_mass_slot(const PartT<R> &p) {
+    return (double)p.mhi + (double)p.mlo;
+}
+__device__ __forceinline__ double part_mass_slot(const PartQ &p) {
+    return __longlong_as_double(p.mq);
+}
+
+// Lattice-wide accumulation of the reducer: the block masses as doubles
+// (Float64 states) or as a 128-bit fixed-point integer hi * 2^64 + lo
+// (FP32 states: exact for any lattice the state can hold).
+struct RedPart {
+    double m;
+    long long qhi;
+    unsigned long long qlo;
+    int wet;
+    double hmax, hmin, area, cossum;
+};
+
+__device__ __forceinline__ void part_init(RedPart &p) {
+    p.m = 0.0;
+    p.qhi = 0;
+    p.qlo = 0;
+    p.wet = 0;
+    p.hmax = -INFINITY;
+    p.hmin = INFINITY;
+    p.area = 0.0;
+    p.cossum = 0.0;
+}
+
+__device__ __forceinline__ void fix_add(long long &hi, unsigned long long &lo, long long v) {
+    const unsigned long long n = lo + (unsigned long long)v;
+    hi += (v < 0 ? -1 : 0) + (n < lo ? 1 : 0);
+    lo = n;
+}
+
+__device__ __forceinline__ void part_merge(RedPart &a, const RedPart &b) {
+    a.m += b.m;
+    const unsigned long long n = a.qlo + b.qlo;
+    a.qhi += b.qhi + (n < a.qlo ? 1 : 0);
+    a.qlo = n;
+    a.wet += b.wet;
+    a.hmax = fmax(a.hmax, b.hmax);
+    a.hmin = fmin(a.hmin, b.hmin);
+    a.area += b.area;
+    a.cossum += b.cossum;
+}
+
+__device__ __forceinline__ RedPart part_shfl(const RedPart &p, int off) {
+    RedPart o;
+    o.m = __shfl_down_sync(0xffffffffu, p.m, off);
+    o.qhi = __shfl_down_sync(0xffffffffu, p.qhi, off);
+    o.qlo = __shfl_down_sync(0xffffffffu, p.qlo, off);
+    o.wet = __shfl_down_sync(0xffffffffu, p.wet, off);
+    o.hmax = __shfl_down_sync(0xffffffffu, p.hmax, off);
+    o.hmin = __shfl_down_sync(0xffffffffu, p.hmin, off);
+    o.area = __shfl_down_sync(0xffffffffu, p.area, off);
+    o.cossum = __shfl_down_sync(0xffffffffu, p.cossum, off);
+    return o;
+}
+
 // Block-wide reduction; the result is valid in thread 0.  red: NT/32 slots.
-template <int NT, class R>
-__device__ __forceinline__ PartT<R> block_reduce(PartT<R> p, PartT<R> *red) {
+template <int NT, class P>
+__device__ __forceinline__ P block_reduce(P p, P *red) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) part_merge(p, part_shfl(p, off));
     if (lane == 0) red[warp] = p;
     __syncthreads();
     if (warp == 0) {
-        PartT<R> q;
+        P q;
         part_init(q);
         if (lane < NT / 32) q = red[lane];
 #pragma unroll
@@ -409,18 +541,18 @@ struct MarchSmem {
     R jx[4][NT];
     R jy[4][NT];
     R lo[4][NT];  // FP32 paths: rounding error of the pulled height
-    PartT<R> red[NT / 32];
-    PartT<double> redd[NT / 32];
+    StepPart<R> red[NT / 32];
+    RedPart redd[NT / 32];
 };
 
 // Block partial measures of iteration t into its parity slot.
-template <int NT, class R>
-__device__ __forceinline__ void write_partials(const StepArgs &a, const PartT<R> &part,
-                                               long long t, int blin, PartT<R> *red) {
-    const PartT<R> tot = block_reduce<NT>(part, red);
+template <int NT, class P>
+__device__ __forceinline__ void write_partials(const StepArgs &a, const P &part, long long t,
+                                               int blin, P *red) {
+    const P tot = block_reduce<NT>(part, red);
     if (threadIdx.x == 0) {
         double *pp = a.partials + ((size_t)(t & 1) * (size_t)a.part_stride + (size_t)blin) * kNPart;
-        pp[0] = (double)tot.mhi + (double)tot.mlo;
+        pp[0] = part_mass_slot(tot);
         pp[1] = (double)tot.wet;
         pp[2] = (double)tot.hmax;
         pp[3] = (double)tot.hmin;
@@ -430,35 +562,47 @@ __device__ __forceinline__ void write_partials(const StepArgs &a, const PartT<R>
 }
 
 // Lattice-wide measures of iteration s (its partials are complete: they were
-// written by an earlier launch): Float64, fixed order, so deterministic.
-// Writes the per-step record and, for the FP16 mass correction, the
-// correction of iteration s + 2.  M(s) is the mass of the populations
+// written by an earlier launch), in a fixed order, so deterministic; the mass
+// of FP32 states exactly (a 128-bit fixed-point sum of the blocks' exact
+// 64-bit sums), so independent of the blocks as well.  Writes the per-step
+// record and, for the FP32/FP16 mass correction, the correction of
+// iteration s + 2.  M(s) is the mass of the populations
 // iteration s pulled; the corrections c(s) and c(s+1) were applied after that
 // and are not in it, so
 //   c(s+2) = (M_target - M(s) - N (c(s) + c(s+1))) / N
 // makes M(s+3) = M_target up to three steps of rounding noise.
 template <int NT>
-__device__ void reduce_step(const StepArgs &a, long long s, PartT<double> *redd) {
+__device__ void reduce_step(const StepArgs &a, long long s, RedPart *redd) {
     const int nblocks = a.tiles_x * a.tiles_y;
     const double *base = a.partials + (size_t)(s & 1) * (size_t)a.part_stride * kNPart;
-    // plain Float64 sums over the block partials (each already a compensated
-    // sum): ~1e-15 relative for a few thousand blocks.  Unrolled so that many
+    // Float64 states: plain sums over the block partials (each already a
+    // compensated sum): ~1e-15 relative for a few thousand blocks.  Unrolled so that many
     // partials are in flight at once: this CTA runs beside the strips and must
     // not become the launch's straggler.
+    // a partial is 48 bytes, 16-byte aligned: three 16-byte loads each
+    static_assert(kNPart == 6, "partials of six doubles");
+    const bool fixed = a.mass_fixed != 0;
     double m = 0.0, wt = 0.0, ar = 0.0, cs = 0.0, mx = -INFINITY, mn = INFINITY;
-#pragma unroll 4
+    long long qhi = 0;
+    unsigned long long qlo = 0;
+#pragma unroll 8
     for (int b = threadIdx.x; b < nblocks; b += NT) {
-        const double *pp = base + (size_t)b * kNPart;
-        m += __ldcg(pp + 0);
-        wt += __ldcg(pp + 1);
-        mx = fmax(mx, __ldcg(pp + 2));
-        mn = fmin(mn, __ldcg(pp + 3));
-        ar += __ldcg(pp + 4);
-        cs += __ldcg(pp + 5);
+        const double2 *pp = reinterpret_cast<const double2 *>(base + (size_t)b * kNPart);
+        const double2 v0 = __ldcg(pp), v1 = __ldcg(pp + 1), v2 = __ldcg(pp + 2);
+        if (fixed)
+            fix_add(qhi, qlo, __double_as_longlong(v0.x));
+        else
+            m += v0.x;
+        wt += v0.y;
+        mx = fmax(mx, v1.x);
+        mn = fmin(mn, v1.y);
+        ar += v2.x;
+        cs += v2.y;
     }
-    PartT<double> acc;
-    acc.mhi = m;
-    acc.mlo = 0.0;
+    RedPart acc;
+    acc.m = m;
+    acc.qhi = qhi;
+    acc.qlo = qlo;
     acc.wet = (int)wt;
     acc.hmax = mx;
     acc.hmin = mn;
@@ -467,7 +611,8 @@ __device__ void reduce_step(const StepArgs &a, long long s, PartT<double> *redd)
     acc = block_reduce<NT>(acc, redd);
     if (threadIdx.x == 0) {
         Control *c = a.ctl;
-        const double mass = acc.mhi + acc.mlo;
+        const double mass =
+            fixed ? ((double)acc.qhi * 0x1p64 + (double)acc.qlo) * kMassUnit : acc.m;
         if (a.meas_mask) {
             Record &r = a.records[(s - 1) % a.rec_cap];
             r.t = s;
@@ -671,13 +816,20 @@ __device__ __forceinline__ void collide_cell(const StepArgs &a,
     } else {
         // FP32 arithmetic.  f0 closes the mass balance with the values as
         // stored: f0 = M - Σ_{q>0} f_q, where M (the pulled mass, hi + lo)
-        // is what the cell must hold.  e, the exact rounding error of f0
-        // (Fast2Sum), the lo part of M and the FP64-measured correction
-        // are then put back: FP32 populations fold them into f1 and f3
-        // equally (momentum unchanged), resolved to ~ulp(f1); FP16
-        // populations add them to f0 by stochastic rounding, so that the
-        // per-cell storage error is unbiased (round-to-nearest would drop
-        // the sub-ulp term every step and drift).
+        // is what the cell must hold.  The residue c (e, the exact rounding
+        // error of f0 (Fast2Sum), the lo part of M and the cell's share of
+        // the mass correction) is added to f0 by stochastic rounding, so it
+        // stays in the cell, at rest, in expectation: no bias, whatever the
+        // state.  FP32 populations also keep what that rounding left out:
+        // c - k ulp(f0) is zero-mean and resolved by ulp(f5), so folding it
+        // into f5 and f7 keeps the mass (~1e-12 relative over 100,000
+        // iterations) without a systematic transport.  Folding all of c into
+        // a moving pair instead moves the residue to the neighbours every
+        // iteration, which biases slow dynamics: 2-3e-4 relative L2 in h
+        // against Float64 after 100,000 iterations of spinodal dewetting on
+        // 2048², against 6e-7 this way (measured on GB300).  FP16
+        // populations cannot hold the left-out part; their mass is kept by
+        // the FP64-measured correction.
         // Opposite populations (q+, q-) share their equilibrium's even part
         // A and odd part B (feq = A ± B, src/equilibrium.jl:67-114) and their
         // force source ±S (src/collide.jl:272-280).
@@ -709,17 +861,19 @@ __device__ __forceinline__ void collide_cell(const StepArgs &a,
         // Σ_q fpost_q = (1-1/τ) Σ ft + Σ feq/τ = h once h is the pulled mass
         const R mc = (TAU1 || !FRESH) ? h : cc.omeg * hft + cc.invtau * h;
         const R ssum = small8(fo);
-        R f0 = mc - ssum;
+        const R f0 = mc - ssum;
         const R e = (mc - f0) - ssum;
+        const R c = e + hlo + R(cc.corr);
+        fo[0] = add_stochastic((float)f0, (float)c, mix32((unsigned)cell, (unsigned)tt));
         if constexpr (!S::kHalf) {
-            const R dd = R(0.5) * (e + hlo + R(cc.corr));
-            fo[1] = fo[1] + dd;
-            fo[3] = fo[3] + dd;
-        } else {
-            f0 = add_stochastic((float)f0, (float)(e + hlo + R(cc.corr)),
-                                mix32((unsigned)cell, (unsigned)tt));
+            // What the rounding left out, c - k ulp(f0): zero-mean whatever
+            // the state, at most ~ulp(f0), and on a grid that ulp(f5) = ulp(f0)/16
+            // resolves, so folding it into the diagonal pair keeps the mass
+            // (momentum unchanged) without a systematic transport.
+            const R d = R(0.5) * (c - (fo[0] - f0));
+            fo[5] = fo[5] + d;
+            fo[7] = fo[7] + d;
         }
-        fo[0] = f0;
 #pragma unroll
         for (int q = 0; q < 9; ++q) S::st(dst, pitch, q, cell, fo[q]);
     }
@@ -830,7 +984,7 @@ __device__ __forceinline__ void march_run(const StepArgs &a, int bx, int by, lon
     const CellConst<R> cc = cell_consts<R>(a, tt, corr);
     const R thr = R(a.hthresh);
     const bool measure = a.meas_mask || a.mass_corr;
-    PartT<R> part;
+    StepPart<R> part;
     part_init(part);
     int any_nan = 0;
 
@@ -867,7 +1021,7 @@ __device__ __forceinline__ void march_run(const StepArgs &a, int bx, int by, lon
         if (!isfinite(h)) any_nan = 1;
         if (measure) {
             mass_add(part, h);
-            if constexpr (!LIT && !FRESH) part.mlo += sm.lo[r & 3][t];
+            if constexpr (!LIT && !FRESH) mass_add_lo(part, sm.lo[r & 3][t]);
             const bool wet = h > thr;
             part.wet += wet ? 1 : 0;
             part.hmax = fmax(part.hmax, h);
@@ -887,7 +1041,7 @@ __device__ __forceinline__ void march_run(const StepArgs &a, int bx, int by, lon
         }
     any_nan = __syncthreads_or(any_nan);
     if (any_nan && t == 0) a.ctl->nan_flag = 1;
-    if (measure) write_partials<NT, R>(a, part, tt, by * a.tiles_x + bx, sm.red);
+    if (measure) write_partials<NT>(a, part, tt, by * a.tiles_x + bx, sm.red);
 }
 
 // Iteration done + 1 of strip (bx, by), dispatched on its rare cases: the
@@ -939,8 +1093,8 @@ struct TileSmem {
     R jx[kT2Out];
     R jy[kT2Out];
     R lo[kT2Out];
-    PartT<R> red[kT2NT / 32];
-    PartT<double> redd[kT2NT / 32];
+    StepPart<R> red[kT2NT / 32];
+    RedPart redd[kT2NT / 32];
 };
 
 template <class S, bool FRESH, bool TAU1>
@@ -1029,7 +1183,7 @@ __device__ __forceinline__ void tile2d_run(const StepArgs &a, int bx, int by, lo
     const CellConst<R> cc = cell_consts<R>(a, tt, corr);
     const R thr = R(a.hthresh);
     const bool measure = a.meas_mask || a.mass_corr;
-    PartT<R> part;
+    StepPart<R> part;
     part_init(part);
     int any_nan = 0;
 #pragma unroll 1
@@ -1057,7 +1211,7 @@ __device__ __forceinline__ void tile2d_run(const StepArgs &a, int bx, int by, lo
         if (!isfinite(h)) any_nan = 1;
         if (measure) {
             mass_add(part, h);
-            if constexpr (!FRESH) part.mlo += sm.lo[o];
+            if constexpr (!FRESH) mass_add_lo(part, sm.lo[o]);
             const bool wet = h > thr;
             part.wet += wet ? 1 : 0;
             part.hmax = fmax(part.hmax, h);
@@ -1079,7 +1233,7 @@ __device__ __forceinline__ void tile2d_run(const StepArgs &a, int bx, int by, lo
     }
     any_nan = __syncthreads_or(any_nan);
     if (any_nan && t == 0) a.ctl->nan_flag = 1;
-    if (measure) write_partials<kT2NT, R>(a, part, tt, by * a.tiles_x + bx, sm.red);
+    if (measure) write_partials<kT2NT>(a, part, tt, by * a.tiles_x + bx, sm.red);
 }
 
 template <class S>
@@ -1232,7 +1386,7 @@ __global__ void __launch_bounds__(NT) fused_step_kernel(const StepArgs a, int k)
 // the step counter.  One CTA.
 template <int NT>
 __global__ void __launch_bounds__(NT) advance_kernel(const StepArgs a, int n) {
-    __shared__ PartT<double> redd[NT / 32];
+    __shared__ RedPart redd[NT / 32];
     const long long s = a.ctl->step_base + n;
     if (needs_partials(a) && n > 0) reduce_step<NT>(a, s, redd);
     __syncthreads();
@@ -1263,7 +1417,7 @@ __global__ void __launch_bounds__(NT) batch_step_kernel(const StepArgs *__restri
 template <int NT>
 __global__ void __launch_bounds__(NT) batch_advance_kernel(const StepArgs *__restrict__ args,
                                                            int n) {
-    __shared__ PartT<double> redd[NT / 32];
+    __shared__ RedPart redd[NT / 32];
     __shared__ StepArgs sa;
     if (threadIdx.x == 0) sa = args[blockIdx.x];
     __syncthreads();
