@@ -398,6 +398,8 @@ int check_nan(swb_state *s) {
         CUDA_TRY(&s->err, cudaMemsetAsync(s->a.bar, 0, swb::kBarWords * sizeof(unsigned int),
                                           s->stream));
         CUDA_TRY(&s->err, cudaMemsetAsync(&s->a.ctl->bar_err, 0, sizeof(int), s->stream));
+        // the measures of the abandoned iterations were never reduced
+        CUDA_TRY(&s->err, cudaMemsetAsync(s->a.ctl->acc, 0, sizeof(s->a.ctl->acc), s->stream));
         CUDA_TRY(&s->err, cudaStreamSynchronize(s->stream));
         return fail(&s->err, SWB_ERR_CUDA, "multi-step kernel: grid barrier wait timed out");
     }

@@ -27,6 +27,11 @@ void default_geometry(int Lx, int Ly, int precision, int *nt, int *h);
 
 // Measure partials per block: mass, wetted, hmax, hmin, area, cos-sum.
 constexpr int kNPart = 6;
+// Integer measure accumulators of FP32-arithmetic states: fixed-point mass,
+// area and cos-sum (units of 2^-32 per cell), wetted count, and hmax / hmin
+// as order-preserving keys (0: no cell), each in kAccLanes lanes.
+enum { kAccMass, kAccWet, kAccHmax, kAccHmin, kAccArea, kAccCos, kAccFields };
+constexpr int kAccLanes = 32;
 // Capacity of the per-step measure ring of a single state (records).
 constexpr int kRecCap = 65536;
 
@@ -46,6 +51,10 @@ struct Control {
     long long rec_head;      // records written (monotone)
     int bar_err;             // a grid-barrier wait of the multi-step kernel gave up
     int pad1;
+    // FP32-arithmetic states: the per-iteration measures, accumulated by
+    // integer atomics of every CTA into one of kAccLanes lanes (slot t & 1),
+    // read and cleared by the reducer of iteration t (order-free, exact)
+    unsigned long long acc[2][kAccFields][kAccLanes];
 };
 
 struct Record {              // one time_loop iteration

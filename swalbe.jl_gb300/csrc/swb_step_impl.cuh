@@ -324,14 +324,15 @@ struct PartT {
     R hmax, hmin, area, cossum;
 };
 
-// FP32 cells: the mass in units of kMassUnit.  A block holds at most
-// 252 x 512 cells, so the 64-bit sum is exact for mean heights below 1.6e4.
+// FP32 cells: the mass, area and cos-sum in units of kMassUnit.  A block
+// holds at most 252 x 512 cells, so its 64-bit sums are exact for mean
+// heights below 1.6e4.
 constexpr float kMassScale = 0x1p32f;
 constexpr double kMassUnit = 0x1p-32;
 struct PartQ {
-    long long mq;
+    long long mq, area, cossum;
     int wet;
-    float hmax, hmin, area, cossum;
+    float hmax, hmin;
 };
 
 // The per-cell partials of the step kernels of compute type R.
@@ -355,11 +356,11 @@ __device__ __forceinline__ void part_init(PartT<R> &p) {
 
 __device__ __forceinline__ void part_init(PartQ &p) {
     p.mq = 0;
+    p.area = 0;
+    p.cossum = 0;
     p.wet = 0;
     p.hmax = -INFINITY;
     p.hmin = INFINITY;
-    p.area = 0.0f;
-    p.cossum = 0.0f;
 }
 
 // (s, e) = a + b exactly (Knuth's TwoSum).
@@ -391,6 +392,18 @@ __device__ __forceinline__ void mass_add_lo(PartQ &p, float lo) {
     p.mq += __float2ll_rn(lo * kMassScale);
 }
 
+// A wetted cell's surface element and cos θ (surfacearea!, src/measures.jl).
+template <class R>
+__device__ __forceinline__ void area_add(PartT<R> &p, R v) { p.area += v; }
+__device__ __forceinline__ void area_add(PartQ &p, float v) {
+    p.area += __float2ll_rn(v * kMassScale);
+}
+template <class R>
+__device__ __forceinline__ void cos_add(PartT<R> &p, R v) { p.cossum += v; }
+__device__ __forceinline__ void cos_add(PartQ &p, float v) {
+    p.cossum += __float2ll_rn(v * kMassScale);
+}
+
 template <class R>
 __device__ __forceinline__ void part_merge(PartT<R> &a, const PartT<R> &b) {
     R s, e;
@@ -406,11 +419,11 @@ __device__ __forceinline__ void part_merge(PartT<R> &a, const PartT<R> &b) {
 
 __device__ __forceinline__ void part_merge(PartQ &a, const PartQ &b) {
     a.mq += b.mq;
+    a.area += b.area;
+    a.cossum += b.cossum;
     a.wet += b.wet;
     a.hmax = fmaxf(a.hmax, b.hmax);
     a.hmin = fminf(a.hmin, b.hmin);
-    a.area += b.area;
-    a.cossum += b.cossum;
 }
 
 template <class R>
@@ -429,39 +442,23 @@ __device__ __forceinline__ PartT<R> part_shfl(const PartT<R> &p, int off) {
 __device__ __forceinline__ PartQ part_shfl(const PartQ &p, int off) {
     PartQ o;
     o.mq = __shfl_down_sync(0xffffffffu, p.mq, off);
+    o.area = __shfl_down_sync(0xffffffffu, p.area, off);
+    o.cossum = __shfl_down_sync(0xffffffffu, p.cossum, off);
     o.wet = __shfl_down_sync(0xffffffffu, p.wet, off);
     o.hmax = __shfl_down_sync(0xffffffffu, p.hmax, off);
     o.hmin = __shfl_down_sync(0xffffffffu, p.hmin, off);
-    o.area = __shfl_down_sync(0xffffffffu, p.area, off);
-    o.cossum = __shfl_down_sync(0xffffffffu, p.cossum, off);
     return o;
 }
 
-// The mass slot of a block partial: a double, or the 64 bits of the
-// fixed-point sum.
-template <class R>
-__device__ __forceinline__ double part_mass_slot(const PartT<R> &p) {
-    return (double)p.mhi + (double)p.mlo;
-}
-__device__ __forceinline__ double part_mass_slot(const PartQ &p) {
-    return __longlong_as_double(p.mq);
-}
-
-// Lattice-wide accumulation of the reducer: the block masses as doubles
-// (Float64 states) or as a 128-bit fixed-point integer hi * 2^64 + lo
-// (FP32 states: exact for any lattice the state can hold).
+// Lattice-wide accumulation of the Float64 reducer.
 struct RedPart {
     double m;
-    long long qhi;
-    unsigned long long qlo;
     int wet;
     double hmax, hmin, area, cossum;
 };
 
 __device__ __forceinline__ void part_init(RedPart &p) {
     p.m = 0.0;
-    p.qhi = 0;
-    p.qlo = 0;
     p.wet = 0;
     p.hmax = -INFINITY;
     p.hmin = INFINITY;
@@ -469,17 +466,8 @@ __device__ __forceinline__ void part_init(RedPart &p) {
     p.cossum = 0.0;
 }
 
-__device__ __forceinline__ void fix_add(long long &hi, unsigned long long &lo, long long v) {
-    const unsigned long long n = lo + (unsigned long long)v;
-    hi += (v < 0 ? -1 : 0) + (n < lo ? 1 : 0);
-    lo = n;
-}
-
 __device__ __forceinline__ void part_merge(RedPart &a, const RedPart &b) {
     a.m += b.m;
-    const unsigned long long n = a.qlo + b.qlo;
-    a.qhi += b.qhi + (n < a.qlo ? 1 : 0);
-    a.qlo = n;
     a.wet += b.wet;
     a.hmax = fmax(a.hmax, b.hmax);
     a.hmin = fmin(a.hmin, b.hmin);
@@ -490,14 +478,52 @@ __device__ __forceinline__ void part_merge(RedPart &a, const RedPart &b) {
 __device__ __forceinline__ RedPart part_shfl(const RedPart &p, int off) {
     RedPart o;
     o.m = __shfl_down_sync(0xffffffffu, p.m, off);
-    o.qhi = __shfl_down_sync(0xffffffffu, p.qhi, off);
-    o.qlo = __shfl_down_sync(0xffffffffu, p.qlo, off);
     o.wet = __shfl_down_sync(0xffffffffu, p.wet, off);
     o.hmax = __shfl_down_sync(0xffffffffu, p.hmax, off);
     o.hmin = __shfl_down_sync(0xffffffffu, p.hmin, off);
     o.area = __shfl_down_sync(0xffffffffu, p.area, off);
     o.cossum = __shfl_down_sync(0xffffffffu, p.cossum, off);
     return o;
+}
+
+// Order-preserving keys of a float for unsigned atomicMax, 0 meaning "no
+// cell": key_max grows with v, key_min shrinks with v.
+__device__ __forceinline__ unsigned int float_order(float v) {
+    const unsigned int u = __float_as_uint(v);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float float_unorder(unsigned int o) {
+    return __uint_as_float((o & 0x80000000u) ? (o & 0x7fffffffu) : ~o);
+}
+__device__ __forceinline__ unsigned long long key_max(float v) {
+    return (unsigned long long)float_order(v) + 1ull;
+}
+__device__ __forceinline__ unsigned long long key_min(float v) {
+    return (unsigned long long)(0xffffffffu - float_order(v)) + 1ull;
+}
+
+// hi * 2^64 + lo += v (a two-word signed 128-bit integer)
+__device__ __forceinline__ void fix_add(long long &hi, unsigned long long &lo, long long v) {
+    const unsigned long long n = lo + (unsigned long long)v;
+    hi += (v < 0 ? -1 : 0) + (n < lo ? 1 : 0);
+    lo = n;
+}
+
+// Warp-wide exact sum of one signed 64-bit value per lane, as a double in
+// units of kMassUnit.
+__device__ __forceinline__ double warp_fix_sum(long long v) {
+    long long hi = 0;
+    unsigned long long lo = 0;
+    fix_add(hi, lo, v);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const long long ohi = __shfl_down_sync(0xffffffffu, hi, off);
+        const unsigned long long olo = __shfl_down_sync(0xffffffffu, lo, off);
+        const unsigned long long n = lo + olo;
+        hi += ohi + (n < lo ? 1 : 0);
+        lo = n;
+    }
+    return ((double)hi * 0x1p64 + (double)lo) * kMassUnit;
 }
 
 // Block-wide reduction; the result is valid in thread 0.  red: NT/32 slots.
@@ -545,14 +571,15 @@ struct MarchSmem {
     RedPart redd[NT / 32];
 };
 
-// Block partial measures of iteration t into its parity slot.
-template <int NT, class P>
-__device__ __forceinline__ void write_partials(const StepArgs &a, const P &part, long long t,
-                                               int blin, P *red) {
-    const P tot = block_reduce<NT>(part, red);
+// Block partial measures of iteration t.  Float64 states: into the block's
+// parity slot of the partials array.
+template <int NT, class R>
+__device__ __forceinline__ void write_partials(const StepArgs &a, const PartT<R> &part,
+                                               long long t, int blin, PartT<R> *red) {
+    const PartT<R> tot = block_reduce<NT>(part, red);
     if (threadIdx.x == 0) {
         double *pp = a.partials + ((size_t)(t & 1) * (size_t)a.part_stride + (size_t)blin) * kNPart;
-        pp[0] = part_mass_slot(tot);
+        pp[0] = (double)tot.mhi + (double)tot.mlo;
         pp[1] = (double)tot.wet;
         pp[2] = (double)tot.hmax;
         pp[3] = (double)tot.hmin;
@@ -561,38 +588,106 @@ __device__ __forceinline__ void write_partials(const StepArgs &a, const P &part,
     }
 }
 
-// Lattice-wide measures of iteration s (its partials are complete: they were
-// written by an earlier launch), in a fixed order, so deterministic; the mass
-// of FP32 states exactly (a 128-bit fixed-point sum of the blocks' exact
-// 64-bit sums), so independent of the blocks as well.  Writes the per-step
-// record and, for the FP32/FP16 mass correction, the correction of
-// iteration s + 2.  M(s) is the mass of the populations
+// FP32-arithmetic states: added by integer atomics into lane blin % 32 of the
+// iteration's accumulators (exact and order-free; fire-and-forget reductions
+// in L2, so no CTA waits).
+template <int NT>
+__device__ __forceinline__ void write_partials(const StepArgs &a, const PartQ &part, long long t,
+                                               int blin, PartQ *red) {
+    const PartQ tot = block_reduce<NT>(part, red);
+    if (threadIdx.x == 0) {
+        unsigned long long(*acc)[kAccLanes] = a.ctl->acc[t & 1];
+        const int l = blin & (kAccLanes - 1);
+        atomicAdd(&acc[kAccMass][l], (unsigned long long)tot.mq);
+        atomicAdd(&acc[kAccWet][l], (unsigned long long)tot.wet);
+        atomicMax(&acc[kAccHmax][l], key_max(tot.hmax));
+        atomicMax(&acc[kAccHmin][l], key_min(tot.hmin));
+        if (a.meas_mask & SWB_MEAS_AREA) {
+            atomicAdd(&acc[kAccArea][l], (unsigned long long)tot.area);
+            atomicAdd(&acc[kAccCos][l], (unsigned long long)tot.cossum);
+        }
+    }
+}
+
+// The record of iteration s and, with the mass correction on, the
+// correction of iteration s + 2.  M(s) is the mass of the populations
 // iteration s pulled; the corrections c(s) and c(s+1) were applied after that
 // and are not in it, so
 //   c(s+2) = (M_target - M(s) - N (c(s) + c(s+1))) / N
-// makes M(s+3) = M_target up to three steps of rounding noise.
+// makes M(s+3) = M_target up to three steps of rounding noise.  One thread.
+__device__ __forceinline__ void finish_step(const StepArgs &a, long long s, double mass,
+                                            double wet, double hmax, double hmin, double area,
+                                            double cossum) {
+    Control *c = a.ctl;
+    if (a.meas_mask) {
+        Record &r = a.records[(s - 1) % a.rec_cap];
+        r.t = s;
+        r.mass = mass;
+        r.wetted = wet;
+        r.hmax = hmax;
+        r.hmin = hmin;
+        r.area = area;
+        r.cos_sum = a.theta_mode == THETA_SCALAR ? wet * a.cos_theta : cossum;
+        c->rec_head = __ldcg(&c->rec_head) + 1;
+    }
+    if (a.mass_corr) {
+        if (s == __ldcg(&c->fresh_step)) c->mass_target = mass;
+        const double N = (double)a.Lx * (double)a.Ly;
+        const double in_flight = __ldcg(&c->corr[s & 1]) + __ldcg(&c->corr[(s + 1) & 1]);
+        c->corr[s & 1] = (__ldcg(&c->mass_target) - mass - N * in_flight) / N;
+    }
+}
+
+// Lattice-wide measures of iteration s (complete: an earlier launch, or the
+// previous phase of a multi-step launch, produced them).
+//  * FP32-arithmetic states: one warp reads the kAccLanes lanes of the
+//    integer accumulators, clears them for iteration s + 2 and sums them
+//    exactly (128-bit), so the result does not depend on the CTAs at all.
+//  * Float64 states: plain Float64 sums over the block partials (each already
+//    a compensated sum, ~1e-15 relative for a few thousand blocks) in a fixed
+//    order, so deterministic.  Unrolled so that many partials are in flight
+//    at once: this CTA runs beside the strips and must not become the
+//    launch's straggler.
+// No __syncthreads in the FP32 path: the other warps return at once.
 template <int NT>
 __device__ void reduce_step(const StepArgs &a, long long s, RedPart *redd) {
+    if (a.mass_fixed) {
+        if (threadIdx.x >= 32) return;
+        const int l = threadIdx.x;
+        unsigned long long(*acc)[kAccLanes] = a.ctl->acc[s & 1];
+        const unsigned long long m = __ldcg(&acc[kAccMass][l]), w = __ldcg(&acc[kAccWet][l]);
+        unsigned long long kx = __ldcg(&acc[kAccHmax][l]), kn = __ldcg(&acc[kAccHmin][l]);
+        const unsigned long long ar = __ldcg(&acc[kAccArea][l]), cs = __ldcg(&acc[kAccCos][l]);
+#pragma unroll
+        for (int f = 0; f < kAccFields; ++f) acc[f][l] = 0ull;
+        const double mass = warp_fix_sum((long long)m);
+        const double area = warp_fix_sum((long long)ar);
+        const double cossum = warp_fix_sum((long long)cs);
+        unsigned long long wt = w;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            wt += __shfl_down_sync(0xffffffffu, wt, off);
+            kx = max(kx, __shfl_down_sync(0xffffffffu, kx, off));
+            kn = max(kn, __shfl_down_sync(0xffffffffu, kn, off));
+        }
+        if (l == 0) {
+            const double hmax = kx ? (double)float_unorder((unsigned int)(kx - 1ull)) : -INFINITY;
+            const double hmin =
+                kn ? (double)float_unorder(0xffffffffu - (unsigned int)(kn - 1ull)) : INFINITY;
+            finish_step(a, s, mass, (double)wt, hmax, hmin, area, cossum);
+        }
+        return;
+    }
     const int nblocks = a.tiles_x * a.tiles_y;
     const double *base = a.partials + (size_t)(s & 1) * (size_t)a.part_stride * kNPart;
-    // Float64 states: plain sums over the block partials (each already a
-    // compensated sum): ~1e-15 relative for a few thousand blocks.  Unrolled so that many
-    // partials are in flight at once: this CTA runs beside the strips and must
-    // not become the launch's straggler.
     // a partial is 48 bytes, 16-byte aligned: three 16-byte loads each
     static_assert(kNPart == 6, "partials of six doubles");
-    const bool fixed = a.mass_fixed != 0;
     double m = 0.0, wt = 0.0, ar = 0.0, cs = 0.0, mx = -INFINITY, mn = INFINITY;
-    long long qhi = 0;
-    unsigned long long qlo = 0;
 #pragma unroll 8
     for (int b = threadIdx.x; b < nblocks; b += NT) {
         const double2 *pp = reinterpret_cast<const double2 *>(base + (size_t)b * kNPart);
         const double2 v0 = __ldcg(pp), v1 = __ldcg(pp + 1), v2 = __ldcg(pp + 2);
-        if (fixed)
-            fix_add(qhi, qlo, __double_as_longlong(v0.x));
-        else
-            m += v0.x;
+        m += v0.x;
         wt += v0.y;
         mx = fmax(mx, v1.x);
         mn = fmin(mn, v1.y);
@@ -601,36 +696,14 @@ __device__ void reduce_step(const StepArgs &a, long long s, RedPart *redd) {
     }
     RedPart acc;
     acc.m = m;
-    acc.qhi = qhi;
-    acc.qlo = qlo;
     acc.wet = (int)wt;
     acc.hmax = mx;
     acc.hmin = mn;
     acc.area = ar;
     acc.cossum = cs;
     acc = block_reduce<NT>(acc, redd);
-    if (threadIdx.x == 0) {
-        Control *c = a.ctl;
-        const double mass =
-            fixed ? ((double)acc.qhi * 0x1p64 + (double)acc.qlo) * kMassUnit : acc.m;
-        if (a.meas_mask) {
-            Record &r = a.records[(s - 1) % a.rec_cap];
-            r.t = s;
-            r.mass = mass;
-            r.wetted = (double)acc.wet;
-            r.hmax = acc.hmax;
-            r.hmin = acc.hmin;
-            r.area = acc.area;
-            r.cos_sum = a.theta_mode == THETA_SCALAR ? (double)acc.wet * a.cos_theta : acc.cossum;
-            c->rec_head = __ldcg(&c->rec_head) + 1;
-        }
-        if (a.mass_corr) {
-            if (s == __ldcg(&c->fresh_step)) c->mass_target = mass;
-            const double N = (double)a.Lx * (double)a.Ly;
-            const double in_flight = __ldcg(&c->corr[s & 1]) + __ldcg(&c->corr[(s + 1) & 1]);
-            c->corr[s & 1] = (__ldcg(&c->mass_target) - mass - N * in_flight) / N;
-        }
-    }
+    if (threadIdx.x == 0)
+        finish_step(a, s, acc.m, (double)acc.wet, acc.hmax, acc.hmin, acc.area, acc.cossum);
 }
 
 // ------------------------------------------------------------ thermal noise
@@ -1031,11 +1104,11 @@ __device__ __forceinline__ void march_run(const StepArgs &a, int bx, int by, lon
                 R gx2, gy2;
                 grad9<R>(hrow[t - 1], hm[t], hrow[t + 1], hp[t], hm[t - 1], hm[t + 1], hp[t + 1],
                          hp[t - 1], gx2, gy2);
-                part.area += sqrt(gx2 * gx2 + gy2 * gy2 + R(1));
+                area_add(part, R(sqrt(gx2 * gx2 + gy2 * gy2 + R(1))));
                 if (mode == THETA_FIELD)
-                    part.cossum += reinterpret_cast<const R *>(a.cosF)[frow(gy) * Lx + gxf];
+                    cos_add(part, reinterpret_cast<const R *>(a.cosF)[frow(gy) * Lx + gxf]);
                 else if (mode == THETA_WAVE)
-                    part.cossum += cos_col;
+                    cos_add(part, cos_col);
             }
         }
         }
@@ -1220,13 +1293,13 @@ __device__ __forceinline__ void tile2d_run(const StepArgs &a, int bx, int by, lo
                 const R *hm = hc - kT2HX, *hp = hc + kT2HX;
                 R gx2, gy2;
                 grad9<R>(hc[-1], hm[0], hc[1], hp[0], hm[-1], hm[1], hp[1], hp[-1], gx2, gy2);
-                part.area += sqrt(gx2 * gx2 + gy2 * gy2 + R(1));
+                area_add(part, R(sqrt(gx2 * gx2 + gy2 * gy2 + R(1))));
                 if (mode == THETA_FIELD) {
-                    part.cossum += reinterpret_cast<const R *>(
-                        a.cosF)[wrapc(gy - fsy, Ly) * Lx + wrapc(gx - fsx, Lx)];
+                    cos_add(part, reinterpret_cast<const R *>(
+                                      a.cosF)[wrapc(gy - fsy, Ly) * Lx + wrapc(gx - fsx, Lx)]);
                 } else if (mode == THETA_WAVE) {
                     const R th = R(a.theta0) + R(a.dtheta) * sinpi_r(R(2) * (R(gx) - R(a.wave_v) * R(tt)) / R(Lx));
-                    part.cossum += cospi_r(th);
+                    cos_add(part, cospi_r(th));
                 }
             }
         }
