@@ -156,9 +156,28 @@ __device__ __forceinline__ void pull9(const void *src, int pitch, int Lx, int gx
 }
 
 // Sum of the eight moving populations (pairwise).
+// Packed FP32 pairs: Blackwell's FADD2 / FMUL2 / FFMA2 issue two FP32
+// operations as one instruction, each lane rounded like the scalar
+// operation, so pairing changes no result bit.  A - B is written
+// fma(-1, B, A) (exact).
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
+    return __ffma2_rn(make_float2(-1.0f, -1.0f), b, a);
+}
+
 template <class R>
 __device__ __forceinline__ R small8(const R f[9]) {
     return ((f[1] + f[3]) + (f[2] + f[4])) + ((f[5] + f[7]) + (f[6] + f[8]));
+}
+// FP32: ((f1+f3) + (f5+f7)) + ((f2+f4) + (f6+f8)), two lanes at a time
+__device__ __forceinline__ float small8(const float f[9]) {
+    const float2 s1 = add2(f2(f[1], f[2]), f2(f[3], f[4]));  // f1+f3, f2+f4
+    const float2 s2 = add2(f2(f[5], f[6]), f2(f[7], f[8]));  // f5+f7, f6+f8
+    const float2 ss = add2(s1, s2);
+    return ss.x + ss.y;
 }
 
 // moments! (src/moments.jl:43-51): h and the momentum numerators.
@@ -172,9 +191,14 @@ __device__ __forceinline__ void moments9(const R f[9], R &h, R &jx, R &jy) {
         jx = f[1] - f[3] + f[5] - f[6] - f[7] + f[8];
         jy = f[2] - f[4] + f[5] + f[6] - f[7] - f[8];
     } else {
+        // differences of opposite pairs, two lanes at a time:
+        // jx = ((f1-f3) + (f5-f7)) + (f8-f6), jy = ((f2-f4) + (f5-f7)) + (f6-f8)
         h = f[0] + small8(f);
-        jx = (f[1] - f[3]) + (f[5] - f[7]) + (f[8] - f[6]);
-        jy = (f[2] - f[4]) + (f[5] - f[7]) + (f[6] - f[8]);
+        const float2 d1 = sub2(f2(f[1], f[2]), f2(f[3], f[4]));
+        const float2 d2 = sub2(f2(f[5], f[6]), f2(f[7], f[8]));
+        const float2 jj = add2(d1, f2(d2.x, d2.x));
+        jx = jj.x - d2.y;
+        jy = jj.y + d2.y;
     }
 }
 
@@ -852,8 +876,10 @@ __device__ __forceinline__ void collide_cell(const StepArgs &a,
         }
     } else {
         const R c = qdiv(cc.mu6 * h, __fmaf_rn(__fmaf_rn(R(2), h, cc.delta6), h, cc.delta3sq));
-        Fx = __fmaf_rn(-h, gpx, -(c * ux));
-        Fy = __fmaf_rn(-h, gpy, -(c * uy));
+        // (Fx, Fy) = -h ∇p - c u, both components in one packed pair
+        const float2 F = fma2(f2(-h, -h), f2(gpx, gpy), mul2(f2(-c, -c), f2(ux, uy)));
+        Fx = F.x;
+        Fy = F.y;
         if (GEN && a.thermal) {
             R kx, ky;
             thermal_force<false, R>(a.seed, (long long)cell, tt, R(a.k6), h, R(a.delta), &kx, &ky);
@@ -910,24 +936,35 @@ __device__ __forceinline__ void collide_cell(const StepArgs &a,
         const R vsq = __fmaf_rn(ux, ux, uy * uy);
         const R base = __fmaf_rn(R(1.5) * cc.g, h, R(-1.5) * vsq);
         const R w1h = h * R(1.0 / 9.0), w5h = h * R(1.0 / 36.0);
-        const R da = ux + uy, db = uy - ux;
-        const R cu[4] = {ux, uy, da, db};
-        const R wq[4] = {w1h, w1h, w5h, w5h};
-        const R sq[4] = {R(1.0 / 3.0) * Fx, R(1.0 / 3.0) * Fy, R(1.0 / 24.0) * (Fx + Fy),
-                         R(1.0 / 24.0) * (Fy - Fx)};
-        constexpr int qp[4] = {1, 2, 5, 6}, qm[4] = {3, 4, 7, 8};
+        // the k = (1, 2) and (5, 6) directions as packed pairs: velocities
+        // cu = (ux, uy) and (ux + uy, uy - ux), weights w1 h and w5 h, sources
+        // (Fx, Fy) / 3 and (Fx + Fy, Fy - Fx) / 24
+        const float2 U = f2(ux, uy), F2 = f2(Fx, Fy);
+        const float2 CU[2] = {U, add2(U, f2(uy, -ux))};
+        const float2 SQ[2] = {mul2(f2(1.0f / 3.0f, 1.0f / 3.0f), F2),
+                              mul2(f2(1.0f / 24.0f, 1.0f / 24.0f), add2(F2, f2(Fy, -Fx)))};
+        const R wq[2] = {w1h, w5h};
+        const float2 BASE = f2(base, base);
+        constexpr int qp[2] = {1, 5}, qm[2] = {3, 7};  // and qp + 1, qm + 1
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const R A = wq[k] * __fmaf_rn(R(4.5) * cu[k], cu[k], base);
+        for (int j = 0; j < 2; ++j) {
+            const float2 WQ = f2(wq[j], wq[j]);
+            const float2 A = mul2(WQ, fma2(mul2(f2(4.5f, 4.5f), CU[j]), CU[j], BASE));
+            float2 P, M;
             if constexpr (TAU1) {
-                const R BS = __fmaf_rn(R(3) * wq[k], cu[k], sq[k]);
-                fo[qp[k]] = S::rt(qp[k], A + BS);
-                fo[qm[k]] = S::rt(qm[k], A - BS);
+                const float2 BS = fma2(mul2(f2(3.0f, 3.0f), WQ), CU[j], SQ[j]);
+                P = add2(A, BS);
+                M = sub2(A, BS);
             } else {
-                const R B = (R(3) * wq[k]) * cu[k];
-                fo[qp[k]] = S::rt(qp[k], __fmaf_rn(cc.omeg, fq[qp[k]], cc.invtau * (A + B)) + sq[k]);
-                fo[qm[k]] = S::rt(qm[k], __fmaf_rn(cc.omeg, fq[qm[k]], cc.invtau * (A - B)) - sq[k]);
+                const float2 B = mul2(mul2(f2(3.0f, 3.0f), WQ), CU[j]);
+                const float2 OM = f2(cc.omeg, cc.omeg), IT = f2(cc.invtau, cc.invtau);
+                P = add2(fma2(OM, f2(fq[qp[j]], fq[qp[j] + 1]), mul2(IT, add2(A, B))), SQ[j]);
+                M = sub2(fma2(OM, f2(fq[qm[j]], fq[qm[j] + 1]), mul2(IT, sub2(A, B))), SQ[j]);
             }
+            fo[qp[j]] = S::rt(qp[j], P.x);
+            fo[qp[j] + 1] = S::rt(qp[j] + 1, P.y);
+            fo[qm[j]] = S::rt(qm[j], M.x);
+            fo[qm[j] + 1] = S::rt(qm[j] + 1, M.y);
         }
         R hlo = R(0);
         if constexpr (!FRESH) hlo = *hlo_p;
