@@ -174,10 +174,10 @@ static std::atomic<unsigned long long> g_launches{0};
 void count_launches(unsigned long long n) { g_launches += n; }
 unsigned long long launches_so_far() { return g_launches.load(); }
 
-cudaError_t launch_fused_step(int precision, const StepArgs &a, int k, cudaStream_t st) {
+cudaError_t launch_fused_step(int precision, const StepArgs &a, int k, bool steady, cudaStream_t st) {
     count_launches(1);
     return precision == SWB_F64 ? launch_fused_step_f64(a, k, st)
-                                : launch_fused_step_f32(precision, a, k, st);
+                                : launch_fused_step_f32(precision, a, k, steady, st);
 }
 cudaError_t launch_moments(int precision, const StepArgs &a, cudaStream_t st) {
     count_launches(1);
@@ -504,10 +504,13 @@ bool persist_default(const swb_state *s) {
 }
 
 // n step launches (k = 0..n-1) and the advance kernel that closes them.
+// Launch 0 is the first iteration after the fields were set when the state
+// is fresh; fused_steps runs that one alone, so that every launch of a
+// captured sequence is steady and the graph can be replayed at any time.
 cudaError_t launch_sequence(swb_state *s, int n) {
     cudaError_t e = cudaSuccess;
     for (int k = 0; k < n && e == cudaSuccess; ++k)
-        e = swb::launch_fused_step(s->precision, s->a, k, s->stream);
+        e = swb::launch_fused_step(s->precision, s->a, k, !(s->host_fresh && k == 0), s->stream);
     if (e == cudaSuccess) e = swb::launch_advance(s->a, n, s->stream);
     return e;
 }
@@ -634,7 +637,16 @@ int autotune_geometry(swb_state *s, long long &left) {
 int fused_steps(swb_state *s, long long nsteps) {
     long long left = nsteps;
     const long long steps0 = s->steps;
-    if (!s->tuned && s->autotune && left >= kTuneMinSteps) {
+    const bool tune_now = !s->tuned && s->autotune && nsteps >= kTuneMinSteps;
+    if (s->host_fresh && left > 0) {
+        // the first iteration after the fields were set, alone (see launch_sequence)
+        CUDA_TRY(&s->err, launch_sequence(s, 1));
+        s->steps += 1;
+        left -= 1;
+        s->host_fresh = false;
+        s->fields_current = false;
+    }
+    if (tune_now) {
         int rc = autotune_geometry(s, left);
         if (rc) return rc;
     }

@@ -165,7 +165,7 @@ unsigned long long launches_so_far();
 // precision: SWB_F64 (swb_step_f64.cu) / SWB_F32, SWB_F16 (swb_step_f32.cu)
 // Step kernel number k of a sequence, and the sequence's closing advance
 // kernel (precision independent, defined in swb_step_f64.cu).
-cudaError_t launch_fused_step(int precision, const StepArgs &a, int k, cudaStream_t st);
+cudaError_t launch_fused_step(int precision, const StepArgs &a, int k, bool steady, cudaStream_t st);
 cudaError_t launch_advance(const StepArgs &a, int n, cudaStream_t st);
 cudaError_t launch_batch_advance(const StepArgs *d_args, int count, int n, cudaStream_t st);
 // CTAs of step launch k of a single lattice: its strips, plus the reducer.
@@ -205,7 +205,10 @@ cudaError_t launch_fout_f64(const StepArgs &a, double *out, cudaStream_t st);
 cudaError_t launch_pressure_now_f64(const StepArgs &a, double *out, cudaStream_t st);
 cudaError_t launch_batch_step_f64(int nt, bool gen, const StepArgs *d_args, const TileRef *d_tiles,
                                   int ntiles, int grid, int k, cudaStream_t st);
-cudaError_t launch_fused_step_f32(int precision, const StepArgs &a, int k, cudaStream_t st);
+// steady: the iteration is not the first after the fields were set (the
+// steady kernel forms may run it)
+cudaError_t launch_fused_step_f32(int precision, const StepArgs &a, int k, bool steady,
+                                  cudaStream_t st);
 cudaError_t launch_moments_f32(int precision, const StepArgs &a, cudaStream_t st);
 cudaError_t launch_fout_f32(int precision, const StepArgs &a, double *out, cudaStream_t st);
 cudaError_t launch_pressure_now_f32(int precision, const StepArgs &a, double *out,

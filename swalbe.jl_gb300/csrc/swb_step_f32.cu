@@ -40,15 +40,33 @@ int grid_for(long long n, int threads) {
         }                                          \
     } while (0)
 
-cudaError_t launch_fused_step_f32(int precision, const StepArgs &a, int k, cudaStream_t st) {
+// Strips of 64 or 128 threads (the widths the tuner and the size rule pick
+// for single lattices) also exist in the steady forms.
+#define DISPATCH_NT_NARROW(nt, ...)                \
+    do {                                           \
+        if ((nt) == 64) {                          \
+            constexpr int NT = 64;                 \
+            __VA_ARGS__;                           \
+        } else {                                   \
+            constexpr int NT = 128;                \
+            __VA_ARGS__;                           \
+        }                                          \
+    } while (0)
+
+cudaError_t launch_fused_step_f32(int precision, const StepArgs &a, int k, bool steady,
+                                  cudaStream_t st) {
     const int grid = step_grid(a, k);
     if (a.march_nt == kTileGeom) {
         DISPATCH_STORE(precision, (fused_tile_kernel<S><<<grid, kT2NT, 0, st>>>(a, k)));
-    } else {
-        if (step_general(a))
-            DISPATCH_STORE(precision, DISPATCH_NT(a.march_nt, (fused_step_kernel<S, NT, true><<<grid, NT, 0, st>>>(a, k))));
+    } else if (step_general(a)) {
+        DISPATCH_STORE(precision, DISPATCH_NT(a.march_nt, (fused_step_kernel<S, NT, true><<<grid, NT, 0, st>>>(a, k))));
+    } else if (steady && (a.march_nt == 64 || a.march_nt == 128)) {
+        if (a.tau_is_one)
+            DISPATCH_STORE(precision, DISPATCH_NT_NARROW(a.march_nt, (fused_step_kernel<S, NT, false, kFormSteadyTau1><<<grid, NT, 0, st>>>(a, k))));
         else
-            DISPATCH_STORE(precision, DISPATCH_NT(a.march_nt, (fused_step_kernel<S, NT, false><<<grid, NT, 0, st>>>(a, k))));
+            DISPATCH_STORE(precision, DISPATCH_NT_NARROW(a.march_nt, (fused_step_kernel<S, NT, false, kFormSteady><<<grid, NT, 0, st>>>(a, k))));
+    } else {
+        DISPATCH_STORE(precision, DISPATCH_NT(a.march_nt, (fused_step_kernel<S, NT, false><<<grid, NT, 0, st>>>(a, k))));
     }
     return cudaGetLastError();
 }

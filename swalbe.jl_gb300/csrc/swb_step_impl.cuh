@@ -1476,9 +1476,19 @@ __global__ void __launch_bounds__(NT, T2D ? 2 : 1) fused_run_kernel(const StepAr
     }
 }
 
+// Iterations a single-lattice step kernel is compiled for.  kFormAny
+// decides at run time (the first iteration after the fields were set, τ = 1
+// or not); the steady forms leave the first-iteration code out, and the τ
+// code they do not need, so that the common step (steady, τ = 1, no rare
+// forces) is allocated the registers of its own path (64 instead of 80 for
+// FP32 strips of 64 threads: 16 CTAs per SM instead of 12).  The host runs
+// the first iteration after the fields were set as a one-step sequence of
+// kFormAny.
+enum StepForm { kFormAny = 0, kFormSteadyTau1 = 1, kFormSteady = 2 };
+
 // Single lattice: one CTA per strip, plus (when measures are kept and k > 0)
 // a reducer CTA, block 0, for the previous iteration's measures.
-template <class S, int NT, bool GEN>
+template <class S, int NT, bool GEN, int FORM = kFormAny>
 __global__ void __launch_bounds__(NT) fused_step_kernel(const StepArgs a, int k) {
     __shared__ MarchSmem<S, NT> sm;
     int b = blockIdx.x;
@@ -1489,7 +1499,13 @@ __global__ void __launch_bounds__(NT) fused_step_kernel(const StepArgs a, int k)
         }
         b -= 1;
     }
-    march_tile<S, NT, GEN>(a, b % a.tiles_x, b / a.tiles_x, a.ctl->step_base + k, sm);
+    const long long done = a.ctl->step_base + k;
+    if constexpr (FORM == kFormSteadyTau1)
+        march_run<S, NT, false, true, GEN>(a, b % a.tiles_x, b / a.tiles_x, done, sm);
+    else if constexpr (FORM == kFormSteady)
+        march_run<S, NT, false, false, GEN>(a, b % a.tiles_x, b / a.tiles_x, done, sm);
+    else
+        march_tile<S, NT, GEN>(a, b % a.tiles_x, b / a.tiles_x, done, sm);
 }
 
 // Closes a sequence of n step launches: the last iteration's measures, then
