@@ -160,6 +160,7 @@ struct swb_batch {
     int grid = 0;
     int nt = swb::kBatchNT, rows = swb::kBatchRows;  // strip geometry of every lattice
     bool tuned = false, args_dirty = true, gvalid = false;
+    bool fresh_pending = true;  // a lattice's next iteration takes h, u from its fields
     long long steps = 0;
     std::string err;
 
@@ -214,13 +215,20 @@ int upload_args(swb_batch *b) {
 }
 
 // n batched step launches (k = 0..n-1) and the advance kernel closing them.
+// While a lattice is at its first iteration after its height was set
+// (fresh_pending), swb_batch_step runs that iteration alone, so that the
+// launches of a captured sequence are steady and the graph can be replayed
+// at any time.
 cudaError_t batch_sequence(swb_batch *b, int n, int grid) {
     cudaError_t e = cudaSuccess;
-    bool gen = false;  // the general kernel if any lattice needs it
-    for (const StepArgs &a : b->args) gen = gen || swb::step_general(a);
+    bool gen = false, tau1 = true;  // the general kernel if any lattice needs it
+    for (const StepArgs &a : b->args) {
+        gen = gen || swb::step_general(a);
+        tau1 = tau1 && a.tau_is_one;
+    }
     for (int k = 0; k < n && e == cudaSuccess; ++k)
-        e = swb::launch_batch_step(b->precision, b->nt, gen, b->d_args, b->d_tiles, b->ntiles,
-                                   grid, k, b->stream);
+        e = swb::launch_batch_step(b->precision, b->nt, gen, tau1 && !(b->fresh_pending && k == 0),
+                                   b->d_args, b->d_tiles, b->ntiles, grid, k, b->stream);
     if (e == cudaSuccess && n > 0) e = swb::launch_batch_advance(b->d_args, b->count, n, b->stream);
     return e;
 }
@@ -357,6 +365,7 @@ int swb_batch_set_height(swb_batch *b, int idx, const double *host) {
     B_TRY(b, swb::lattice_upload_height(a, b->precision, host, b->staging, b->stream));
     B_TRY(b, cudaStreamSynchronize(b->stream));
     b->fields_current[idx] = 1;
+    b->fresh_pending = true;
     return SWB_OK;
 }
 
@@ -380,7 +389,13 @@ int swb_batch_step(swb_batch *b, int64_t nsteps) {
     int rc = upload_args(b);
     if (rc) return rc;
     long long left = nsteps;
-    if (!b->tuned) {
+    if (b->fresh_pending) {
+        rc = launch_n(b, 1, b->grid > 0 ? b->grid : b->ntiles);
+        if (rc) return rc;
+        b->fresh_pending = false;
+        left -= 1;
+    }
+    if (!b->tuned && left > 0) {
         rc = autotune(b, left);
         if (rc) return rc;
     }

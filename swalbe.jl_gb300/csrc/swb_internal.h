@@ -195,9 +195,11 @@ cudaError_t launch_thermal_field_f64(const StepArgs &a, long long t, double *fx,
 cudaError_t launch_thermal_field_f32(int precision, const StepArgs &a, long long t, double *fx,
                                      double *fy, cudaStream_t st);
 // gen: some lattice of the batch needs the general kernel (step_general).
-cudaError_t launch_batch_step(int precision, int nt, bool gen, const StepArgs *d_args,
-                              const TileRef *d_tiles, int ntiles, int grid, int k,
-                              cudaStream_t st);
+// steady_tau1: no lattice is at its first iteration after its fields were
+// set and every lattice has τ = 1 (the steady batch form may run it)
+cudaError_t launch_batch_step(int precision, int nt, bool gen, bool steady_tau1,
+                              const StepArgs *d_args, const TileRef *d_tiles, int ntiles,
+                              int grid, int k, cudaStream_t st);
 int batch_blocks_per_sm(int precision, int nt);
 cudaError_t launch_fused_step_f64(const StepArgs &a, int k, cudaStream_t st);
 cudaError_t launch_moments_f64(const StepArgs &a, cudaStream_t st);
@@ -213,9 +215,9 @@ cudaError_t launch_moments_f32(int precision, const StepArgs &a, cudaStream_t st
 cudaError_t launch_fout_f32(int precision, const StepArgs &a, double *out, cudaStream_t st);
 cudaError_t launch_pressure_now_f32(int precision, const StepArgs &a, double *out,
                                     cudaStream_t st);
-cudaError_t launch_batch_step_f32(int precision, int nt, bool gen, const StepArgs *d_args,
-                                  const TileRef *d_tiles, int ntiles, int grid, int k,
-                                  cudaStream_t st);
+cudaError_t launch_batch_step_f32(int precision, int nt, bool gen, bool steady_tau1,
+                                  const StepArgs *d_args, const TileRef *d_tiles, int ntiles,
+                                  int grid, int k, cudaStream_t st);
 int batch_blocks_per_sm_f64(int nt);
 int batch_blocks_per_sm_f32(int precision, int nt);
 

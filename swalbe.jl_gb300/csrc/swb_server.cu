@@ -230,11 +230,13 @@ void worker_main(swb_server *sv) {
                 sv->st.admitted++;
             }
         }
+        bool fresh_new = false;  // admitted lattices are at their first iteration
         for (Req *r : admitted) {
             if (admit_device(sv, r)) {
                 std::lock_guard<std::mutex> g(sv->mu);
                 sv->active.push_back(r);
                 changed = true;
+                fresh_new = true;
             } else {
                 std::lock_guard<std::mutex> g(sv->mu);
                 r->status = SWB_ERR_OOM;
@@ -256,10 +258,14 @@ void worker_main(swb_server *sv) {
         const int grid = std::min(ntiles, sms * occ);
         const double tb = sv->now();
         cudaError_t e = cudaSuccess;
-        bool gen = false;  // the general kernel if any resident request needs it
-        for (Req *r : sv->active) gen = gen || swb::step_general(r->a);
+        bool gen = false, tau1 = true;  // the general kernel if any resident request needs it
+        for (Req *r : sv->active) {
+            gen = gen || swb::step_general(r->a);
+            tau1 = tau1 && r->a.tau_is_one;
+        }
         for (int64_t k = 0; k < tick && e == cudaSuccess; ++k)
-            e = swb::launch_batch_step(sv->precision, swb::kBatchNT, gen, sv->d_args, sv->d_tiles,
+            e = swb::launch_batch_step(sv->precision, swb::kBatchNT, gen,
+                                       tau1 && !(fresh_new && k == 0), sv->d_args, sv->d_tiles,
                                        ntiles, grid, (int)k, sv->stream);
         if (e == cudaSuccess)
             e = swb::launch_batch_advance(sv->d_args, (int)sv->active.size(), (int)tick, sv->stream);

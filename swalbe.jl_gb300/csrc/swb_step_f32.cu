@@ -97,19 +97,27 @@ cudaError_t launch_pressure_now_f32(int precision, const StepArgs &a, double *ou
     return cudaGetLastError();
 }
 
-cudaError_t launch_batch_step_f32(int precision, int nt, bool gen, const StepArgs *d_args,
-                                  const TileRef *d_tiles, int ntiles, int grid, int k,
-                                  cudaStream_t st) {
+cudaError_t launch_batch_step_f32(int precision, int nt, bool gen, bool steady_tau1,
+                                  const StepArgs *d_args, const TileRef *d_tiles, int ntiles,
+                                  int grid, int k, cudaStream_t st) {
     if (gen)
         DISPATCH_STORE(precision, DISPATCH_NT(nt, (batch_step_kernel<S, NT, true><<<grid, NT, 0, st>>>(d_args, d_tiles, ntiles, k))));
+    else if (steady_tau1 && nt == kBatchNT)
+        DISPATCH_STORE(precision, (batch_step_kernel<S, kBatchNT, false, kFormSteadyTau1><<<grid, kBatchNT, 0, st>>>(d_args, d_tiles, ntiles, k)));
     else
         DISPATCH_STORE(precision, DISPATCH_NT(nt, (batch_step_kernel<S, NT, false><<<grid, NT, 0, st>>>(d_args, d_tiles, ntiles, k))));
     return cudaGetLastError();
 }
 
+// Resident CTAs per SM of the batch kernel most launches use (the steady
+// form at the default width: fewer registers, so more CTAs).  The table walk
+// needs no co-residency, so a grid sized for it is valid for every form.
 int batch_blocks_per_sm_f32(int precision, int nt) {
     int n = 0;
-    DISPATCH_STORE(precision, DISPATCH_NT(nt, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_step_kernel<S, NT, false>, NT, 0)));
+    if (nt == kBatchNT)
+        DISPATCH_STORE(precision, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_step_kernel<S, kBatchNT, false, kFormSteadyTau1>, kBatchNT, 0));
+    else
+        DISPATCH_STORE(precision, DISPATCH_NT(nt, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_step_kernel<S, NT, false>, NT, 0)));
     return n < 1 ? 1 : n;
 }
 

@@ -1521,7 +1521,9 @@ __global__ void __launch_bounds__(NT) advance_kernel(const StepArgs a, int n) {
 
 // Batch: persistent CTAs walk a packed table of strips of many lattices;
 // entries with tx = -1 reduce their lattice's previous iteration.
-template <class S, int NT, bool GEN>
+// FORM = kFormSteadyTau1 when no lattice is at its first iteration after
+// its fields were set and every lattice has τ = 1 (the host knows both).
+template <class S, int NT, bool GEN, int FORM = kFormAny>
 __global__ void __launch_bounds__(NT) batch_step_kernel(const StepArgs *__restrict__ args,
                                                         const TileRef *__restrict__ tiles,
                                                         int ntiles, int k) {
@@ -1531,9 +1533,12 @@ __global__ void __launch_bounds__(NT) batch_step_kernel(const StepArgs *__restri
         const TileRef tr = tiles[e];
         if (threadIdx.x == 0) sa = args[tr.lattice];
         __syncthreads();
-        if (tr.tx >= 0)
-            march_tile<S, NT, GEN>(sa, tr.tx, tr.ty, sa.ctl->step_base + k, sm);
-        else if (k > 0)
+        if (tr.tx >= 0) {
+            if constexpr (FORM == kFormSteadyTau1)
+                march_run<S, NT, false, true, GEN>(sa, tr.tx, tr.ty, sa.ctl->step_base + k, sm);
+            else
+                march_tile<S, NT, GEN>(sa, tr.tx, tr.ty, sa.ctl->step_base + k, sm);
+        } else if (k > 0)
             reduce_step<NT>(sa, sa.ctl->step_base + k, sm.redd);
         __syncthreads();
     }
