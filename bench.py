@@ -53,7 +53,8 @@ def parse():
     ap.add_argument("--no-extras", action="store_true", help="skip the 2048² and FP64 side runs")
     ap.add_argument("--profile-case", choices=["rt512", "film2048"],
                     help="run a few steps of one case, untimed (for ncu captures)")
-    ap.add_argument("--geometry", default="", help="strip geometry NT,H for --profile-case")
+    ap.add_argument("--geometry", default="",
+                    help="strip geometry NT,H (default: the autotuner's choice)")
     ap.add_argument("--step-mode", default="per_iteration", choices=["per_iteration", "multi"],
                     help="launch form for --profile-case")
     ap.add_argument("--case-steps", type=int, default=12)
@@ -167,9 +168,18 @@ def cpu_baseline(h0, sysc, chunk_steps=1000, chunks=4):
         oracle.FusedState(P, h0).run(chunk_steps, record_dh=True, nthreads=threads)
     dt = time.perf_counter() - t0
     lu = sysc.Lx * sysc.Ly * chunk_steps * chunks
+    # the reference's own op sequence (one pass per op, one core): the closest
+    # stand-in for its single-threaded Julia broadcasts
+    lit_steps = 20
+    t1 = time.perf_counter()
+    oracle.time_loop_literal(P, h0, lit_steps, record_dh=True)
+    dt1 = time.perf_counter() - t1
     return {"value": lu / dt / 1e6, "unit": "MLUPS", "cores": threads, "kind": "port",
             "sample": f"{chunks} x {chunk_steps} time steps of the {sysc.Lx}x{sysc.Ly} workload "
-                      f"from h0, Float64, {dt:.1f} s"}
+                      f"from h0, Float64, {dt:.1f} s",
+            "literal_single_thread": {
+                "value": sysc.Lx * sysc.Ly * lit_steps / dt1 / 1e6, "unit": "MLUPS", "cores": 1,
+                "sample": f"{lit_steps} time steps, the literal per-op oracle, {dt1:.2f} s"}}
 
 
 def run_reference(args):
@@ -259,6 +269,8 @@ def run_ours(args):
     st.set_stream(stream.cuda_stream)
     st.set_theta(sysc.param.theta)
     st.set_measures(L.MEAS_MASS | L.MEAS_MAXMIN)
+    if args.geometry:  # a fixed geometry instead of the autotuner (e.g. for ncu captures)
+        st.set_geometry(*(int(v) for v in args.geometry.split(",")))
     d_h0 = torch.from_numpy(np.ascontiguousarray(h0.ravel(order="F"))).to(f"cuda:{dev}")
     d_zero = torch.zeros(N, dtype=torch.float64, device=f"cuda:{dev}")
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{dev}")
@@ -357,7 +369,8 @@ def run_ours(args):
                   "L2-resident within a step",
             "parallelism": "replicas" if world > 1 else "single GPU",
             "geometry": {"nt": geo[0], "rows": geo[1], "form": form,
-                         "chosen_by": "autotuner (timed on the first 2000-step chunk)"},
+                         "chosen_by": "--geometry" if args.geometry else
+                                       "autotuner (timed on the first 2000-step chunk)"},
         },
         "e2e": {"value": e2e_value, "unit": "MLUPS",
                 "h2d_bytes_per_step": 3 * N * rb,
