@@ -548,7 +548,7 @@ def serving_run(sw, np, duration=12.0, rate=200.0, budget=24 << 30, steps_per_ti
 
 
 def spinodal_run(sw, np, L_, steps=100000):
-    """Spinodal dewetting of a 2048² film (h = 1 + U[-0.1, 0.1], seed 3,
+    """The spinodal-comparison film, 2048² (h = 1 + U[-0.1, 0.1], seed 3,
     γ = 0.01, θ = 1/9): FP32 and FP16-storage runs against the Float64 run
     of the same film, after `steps` iterations: relative L2 of h, mass drift
     (FP64 sums of the per-iteration mass), droplets (h > 0.055, periodic

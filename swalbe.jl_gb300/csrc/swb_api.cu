@@ -213,9 +213,10 @@ int batch_blocks_per_sm(int precision, int nt) {
 }
 
 // Default strip geometry by lattice size (from sweeps on GB300): narrow
-// strips (64 threads) and as many rows per strip as still leave ~1000 CTAs;
-// FP16 small lattices prefer 128-thread strips.  (*nt == kTileGeom keeps
-// the 2D tiles.)
+// strips (64 threads) and as many rows per strip as still leave ~1000 CTAs
+// (FP16: at most 16 rows); FP16 small lattices prefer 128-thread strips.
+// E.g. FP32 2048^2: 60x32 strips, 61.9 us per iteration against 64.0 at
+// 60x16; 1024^2: 60x16.  (*nt == kTileGeom keeps the 2D tiles.)
 void default_geometry(int Lx, int Ly, int precision, int *nt, int *h) {
     int n = *nt;
     if (n == kTileGeom) {
@@ -227,7 +228,7 @@ void default_geometry(int Lx, int Ly, int precision, int *nt, int *h) {
     const long long want = precision == SWB_F64 ? 600 : 1000;
     int hh = kMinRows;
     for (int cand : {32, 16, 8}) {
-        if (precision != SWB_F64 && cand > 16) continue;
+        if (precision == SWB_F16 && cand > 16) continue;
         if (strips * ((Ly + cand - 1) / cand) >= want) {
             hh = cand;
             break;

@@ -925,8 +925,9 @@ __device__ __forceinline__ void collide_cell(const StepArgs &a,
         // iterations) without a systematic transport.  Folding all of c into
         // a moving pair instead moves the residue to the neighbours every
         // iteration, which biases slow dynamics: 2-3e-4 relative L2 in h
-        // against Float64 after 100,000 iterations of spinodal dewetting on
-        // 2048², against 6e-7 this way (measured on GB300).  FP16
+        // against Float64 after 100,000 iterations of a 2048² film h = 1 ± 0.1
+        // (which levels over that time), against 6e-7 this way (measured
+        // on GB300).  FP16
         // populations cannot hold the left-out part; their mass is kept by
         // the FP64-measured correction.
         // Opposite populations (q+, q-) share their equilibrium's even part

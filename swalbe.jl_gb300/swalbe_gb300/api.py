@@ -281,6 +281,13 @@ class GB300State:
         self._chk(lib().swb_get_measures(self._h, buf, cap, C.byref(n)))
         return [buf[k] for k in range(n.value)]
 
+    def measures_array(self, cap: int = 1 << 16) -> np.ndarray:
+        """The records as a numpy structured array (fields of ``Measure``)."""
+        buf = (L.Measure * cap)()
+        n = C.c_int64()
+        self._chk(lib().swb_get_measures(self._h, buf, cap, C.byref(n)))
+        return np.ctypeslib.as_array(buf)[: n.value].copy()
+
     def measure_now(self, hthresh: float = 0.055) -> L.Measure:
         m = L.Measure()
         self._chk(lib().swb_measure_now(self._h, hthresh, C.byref(m)))
@@ -426,15 +433,14 @@ def time_loop(sysc: SysConst, state: GB300State, *args, verbose: bool = False):
             _plain_iteration_with_callback(sysc, state, callback, measure)
     else:
         state.step(Tmax)
-    recs = state.measures(cap=max(Tmax, 1))
-    for r in recs:
-        t = r.t
-        if P.tdump > 0 and t % P.tdump == 0 and verbose:
-            print(f"Time step {t} mass is {round(r.mass, 3)}")
-        if dh is not None:
-            dh.append(r.hmax - r.hmin)
-        if callback is wetted_:
-            measure.append(int(r.wetted))
+    recs = state.measures_array(cap=max(Tmax, 1))
+    if verbose and P.tdump > 0:
+        for r in recs[recs["t"] % P.tdump == 0]:
+            print(f"Time step {int(r['t'])} mass is {round(float(r['mass']), 3)}")
+    if dh is not None:
+        dh.extend((recs["hmax"] - recs["hmin"]).tolist())
+    if callback is wetted_:
+        measure.extend(recs["wetted"].tolist())
     if callback is inclination_:
         state.set_inclination((0.0, 0.0))
     state.sync()
