@@ -155,6 +155,24 @@ __device__ __forceinline__ void pull9(const void *src, int pitch, int Lx, int gx
     ft[8] = S::ld(src, pitch, 8, rp + gxm);
 }
 
+// pull9 for a cell whose neighbours need no periodic wrap: one base pointer
+// at (gx, gy) and offsets that are the same for every thread of the launch
+// (q pitch, ±1 column, ±Lx row), so that each load needs no index arithmetic
+// of its own.
+template <class S>
+__device__ __forceinline__ void pull9_interior(const void *src, int pitch, int Lx, int cell,
+                                               typename S::real ft[9]) {
+    ft[0] = S::ld(src, pitch, 0, cell);
+    ft[1] = S::ld(src, pitch, 1, cell - 1);
+    ft[2] = S::ld(src, pitch, 2, cell - Lx);
+    ft[3] = S::ld(src, pitch, 3, cell + 1);
+    ft[4] = S::ld(src, pitch, 4, cell + Lx);
+    ft[5] = S::ld(src, pitch, 5, cell - Lx - 1);
+    ft[6] = S::ld(src, pitch, 6, cell - Lx + 1);
+    ft[7] = S::ld(src, pitch, 7, cell + Lx + 1);
+    ft[8] = S::ld(src, pitch, 8, cell + Lx - 1);
+}
+
 // Sum of the eight moving populations (pairwise).
 // Packed FP32 pairs: Blackwell's FADD2 / FMUL2 / FFMA2 issue two FP32
 // operations as one instruction, each lane rounded like the scalar
@@ -1042,13 +1060,22 @@ __device__ __forceinline__ void march_run(const StepArgs &a, int bx, int by, lon
 
     // pulled populations of the next leading row (prefetch; two in flight in the prologue)
     R fa_[9], fb_[9];
+    // strips whose pulls never cross the periodic boundary (rows y0-3 ..
+    // y0+rows+2, columns x0-3 .. x0+NT-2): the interior pull (FP32
+    // populations; for FP16 planes it costs more registers than it saves)
+    const bool no_wrap = !FRESH && !LIT && !S::kHalf && y0 >= 3 && y0 + rows + 2 < Ly &&
+                         x0 >= 3 && x0 + NT - 2 < Lx;
     auto issue = [&](R(&ft)[9], int yy) {
-        const int gy = wrow(yy);
         if constexpr (FRESH) {
-            ft[0] = reinterpret_cast<const R *>(a.hF)[gy * Lx + gx];
+            ft[0] = reinterpret_cast<const R *>(a.hF)[wrow(yy) * Lx + gx];
         } else {
-            const int gym = gy == 0 ? Ly - 1 : gy - 1, gyp = gy == Ly - 1 ? 0 : gy + 1;
-            pull9<S>(src, pitch, Lx, gx, gy, gxm, gxp, gym, gyp, ft);
+            if (no_wrap) {
+                pull9_interior<S>(src, pitch, Lx, yy * Lx + gx, ft);
+            } else {
+                const int gy = wrow(yy);
+                const int gym = gy == 0 ? Ly - 1 : gy - 1, gyp = gy == Ly - 1 ? 0 : gy + 1;
+                pull9<S>(src, pitch, Lx, gx, gy, gxm, gxp, gym, gyp, ft);
+            }
         }
     };
     auto consume = [&](const R(&ft)[9], int yy) {
