@@ -190,7 +190,7 @@ def test_fused_fout_roundtrip():
     assert np.array_equal(st.height, lit.field("height"))
 
 
-def test_config1_droplet_256_bit_exact():
+def test_droplet_relax_256_bit_exact():
     """The reference's CPU-runnable case: 256², R=60 cap of height 20, 10k steps,
     with its mass and wetted-area series."""
     from swalbe_gb300 import configs
