@@ -427,3 +427,65 @@ def test_nan_detected():
     with pytest.raises(sw.SwbError) as e:
         st.sync()
     assert e.value.status == L.SWB_ERR_NAN
+
+
+# ------------------------------------------------------------------ first iterations
+# The first iteration after the height is set runs alone (it takes h, u from
+# the fields); every other iteration runs the steady kernel forms, replayed
+# from CUDA graphs.  Re-setting the height after graphs exist must give what
+# the same iterations give when they are issued in small chunks, without
+# graphs (the stochastic rounding of FP32/FP16 depends on the iteration
+# number, so both runs go through the same iterations).
+@pytest.mark.parametrize("T", [np.float64, np.float32, np.float16])
+@pytest.mark.parametrize("tau", [1.0, 0.8])
+def test_height_reset_after_graphs(T, tau):
+    s = sysc(96, 80, tau=tau, g=-1e-4)
+    h_a, h_b = rough(96, 80, 11), rough(96, 80, 12)
+
+    def run(before, after):
+        st = sw.Sys(s, "GB300", T=T)
+        st.set_geometry(64, 8)
+        st.height = h_a
+        for n in before:
+            st.step(n)
+        st.height = h_b  # the velocities carry on
+        for n in after:
+            st.step(n)
+        return st.height
+
+    graphs = run([200], [150])  # 64-iteration graphs before and after the reset
+    chunks = run([1] * 5 + [13] * 15, [7] * 21 + [3])
+    assert np.array_equal(graphs, chunks)
+    if T == np.float64 and tau == 1.0:
+        # and the literal oracle through the same sequence (τ = 1: the
+        # populations before the reset drop out of the collision, so a
+        # fresh oracle state with the same h and u is the same state)
+        P = oparams(s)
+        first = oracle.time_loop_literal(P, h_a, 200)
+        ref = oracle.time_loop_literal(P, h_b, 150, ux0=first.velx, uy0=first.vely)
+        assert np.array_equal(graphs, ref.height)
+
+
+def test_batch_height_reset_matches_single():
+    """One lattice of a batch starts over while the other carries on: both
+    match single states that went through the same sequence."""
+    shapes = [(64, 64), (96, 48)]
+    systems = [sysc(Lx, Ly, g=-1e-4) for Lx, Ly in shapes]
+    b = sw.Batch(systems, T=np.float32)
+    for i, (Lx, Ly) in enumerate(shapes):
+        b.set_height(i, rough(Lx, Ly, 20 + i))
+    b.step(100)  # graphs of the steady batch form
+    h_new = rough(96, 48, 31)
+    b.set_height(1, h_new)
+    b.step(70)
+    single0 = sw.Sys(systems[0], "GB300", T=np.float32)
+    single0.height = rough(64, 64, 20)
+    single0.step(170)
+    single1 = sw.Sys(systems[1], "GB300", T=np.float32)
+    single1.height = rough(96, 48, 21)
+    single1.step(100)
+    single1.height = h_new
+    single1.step(70)
+    assert np.array_equal(b.get_height(0), single0.height)
+    assert np.array_equal(b.get_height(1), single1.height)
+    b.close()
