@@ -327,29 +327,41 @@ int ensure_tmp(swb_state *s, size_t bytes) {
 }
 
 // Host Float64 column-major -> device field of the compute type.
+__global__ void f2d_kernel(const float *src, double *dst, long long n);
+__global__ void d2f_kernel(const double *src, float *dst, long long n);
+
+// Host Float64 field -> device field of the compute type.  FP32 states copy
+// the doubles into the staging buffer (one DMA; asynchronous from pinned host
+// memory) and round them on the device.  Synchronous: the host buffer is only
+// read during the call.
 int upload_field(swb_state *s, void *dst, const double *host, long long n) {
     if (s->rb() == 8) {
         CUDA_TRY(&s->err, cudaMemcpyAsync(dst, host, n * 8, cudaMemcpyHostToDevice, s->stream));
-        CUDA_TRY(&s->err, cudaStreamSynchronize(s->stream));
     } else {
-        std::vector<float> tmp(n);
-        for (long long i = 0; i < n; ++i) tmp[i] = (float)host[i];
-        CUDA_TRY(&s->err, cudaMemcpyAsync(dst, tmp.data(), n * 4, cudaMemcpyHostToDevice, s->stream));
-        CUDA_TRY(&s->err, cudaStreamSynchronize(s->stream));
+        int rc = ensure_tmp(s, (size_t)n * 8);
+        if (rc) return rc;
+        CUDA_TRY(&s->err, cudaMemcpyAsync(s->dtmp, host, n * 8, cudaMemcpyHostToDevice, s->stream));
+        swb::count_launches(1);
+        d2f_kernel<<<blocks_for(n), 256, 0, s->stream>>>(s->dtmp, (float *)dst, n);
+        CUDA_TRY(&s->err, cudaGetLastError());
     }
+    CUDA_TRY(&s->err, cudaStreamSynchronize(s->stream));
     return SWB_OK;
 }
 
+// Device field -> host Float64 field (widened on the device for FP32 states).
 int download_field(swb_state *s, const void *src, double *host, long long n, int bytes) {
     if (bytes == 8) {
         CUDA_TRY(&s->err, cudaMemcpyAsync(host, src, n * 8, cudaMemcpyDeviceToHost, s->stream));
-        CUDA_TRY(&s->err, cudaStreamSynchronize(s->stream));
     } else {
-        std::vector<float> tmp(n);
-        CUDA_TRY(&s->err, cudaMemcpyAsync(tmp.data(), src, n * 4, cudaMemcpyDeviceToHost, s->stream));
-        CUDA_TRY(&s->err, cudaStreamSynchronize(s->stream));
-        for (long long i = 0; i < n; ++i) host[i] = (double)tmp[i];
+        int rc = ensure_tmp(s, (size_t)n * 8);
+        if (rc) return rc;
+        swb::count_launches(1);
+        f2d_kernel<<<blocks_for(n), 256, 0, s->stream>>>((const float *)src, s->dtmp, n);
+        CUDA_TRY(&s->err, cudaGetLastError());
+        CUDA_TRY(&s->err, cudaMemcpyAsync(host, s->dtmp, n * 8, cudaMemcpyDeviceToHost, s->stream));
     }
+    CUDA_TRY(&s->err, cudaStreamSynchronize(s->stream));
     return SWB_OK;
 }
 

@@ -140,9 +140,14 @@ class GB300State:
         return check(st, self._h)
 
     # ---- fields
-    def get(self, name: str) -> np.ndarray:
+    def get(self, name: str, out: Optional[np.ndarray] = None) -> np.ndarray:
+        """Copy field `name` to the host: a new array, or into `out` (Float64,
+        column-major, the field's shape; e.g. pinned host memory)."""
         shape = self.shape + ((9,) if name in ("fout", "feq") else ())
-        out = np.empty(shape, dtype=np.float64, order="F")
+        if out is None:
+            out = np.empty(shape, dtype=np.float64, order="F")
+        elif out.shape != shape or out.dtype != np.float64 or not out.flags.f_contiguous:
+            raise ValueError(f"out must be a column-major Float64 array of shape {shape}")
         self._chk(lib().swb_get_field(self._h, L.FIELD[name], out.ctypes.data))
         return out
 
