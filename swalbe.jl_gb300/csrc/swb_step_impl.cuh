@@ -56,7 +56,6 @@ struct StoreF64T {
     __device__ __forceinline__ static void st(void *b, int pitch, int q, int i, double v) {
         reinterpret_cast<double *>(b)[q * pitch + i] = v;
     }
-    __device__ __forceinline__ static double rt(int, double v) { return v; }
 };
 
 template <class L>
@@ -70,7 +69,6 @@ struct StoreF32T {
     __device__ __forceinline__ static void st(void *b, int pitch, int q, int i, float v) {
         reinterpret_cast<float *>(b)[q * pitch + i] = v;
     }
-    __device__ __forceinline__ static float rt(int, float v) { return v; }
 };
 
 // f0 as an FP32 plane, f1..f8 as FP16 planes holding 2^10 f_q (the scale
@@ -96,9 +94,6 @@ struct StoreF16T {
             __half *h = const_cast<__half *>(hp(b, pitch));
             h[(q - 1) * pitch + i] = __float2half_rn(v * kScale);
         }
-    }
-    __device__ __forceinline__ static float rt(int q, float v) {
-        return q == 0 ? v : __half2float(__float2half_rn(v * kScale)) * kInv;
     }
 };
 
@@ -965,6 +960,9 @@ __device__ __forceinline__ void collide_cell(const StepArgs &a,
         const R wq[2] = {w1h, w5h};
         const float2 BASE = f2(base, base);
         constexpr int qp[2] = {1, 5}, qm[2] = {3, 7};  // and qp + 1, qm + 1
+        // FP16 planes: the stored bits of (f1, f2), (f3, f4), (f5, f6), (f7, f8),
+        // rounded once per pair; fo holds the values they represent
+        [[maybe_unused]] __half2 hb[4];
 #pragma unroll
         for (int j = 0; j < 2; ++j) {
             const float2 WQ = f2(wq[j], wq[j]);
@@ -980,10 +978,22 @@ __device__ __forceinline__ void collide_cell(const StepArgs &a,
                 P = add2(fma2(OM, f2(fq[qp[j]], fq[qp[j] + 1]), mul2(IT, add2(A, B))), SQ[j]);
                 M = sub2(fma2(OM, f2(fq[qm[j]], fq[qm[j] + 1]), mul2(IT, sub2(A, B))), SQ[j]);
             }
-            fo[qp[j]] = S::rt(qp[j], P.x);
-            fo[qp[j] + 1] = S::rt(qp[j] + 1, P.y);
-            fo[qm[j]] = S::rt(qm[j], M.x);
-            fo[qm[j] + 1] = S::rt(qm[j] + 1, M.y);
+            if constexpr (S::kHalf) {
+                const float2 sc = f2(S::kScale, S::kScale), inv = f2(S::kInv, S::kInv);
+                hb[2 * j] = __float22half2_rn(mul2(P, sc));
+                hb[2 * j + 1] = __float22half2_rn(mul2(M, sc));
+                const float2 rp = mul2(__half22float2(hb[2 * j]), inv);
+                const float2 rm = mul2(__half22float2(hb[2 * j + 1]), inv);
+                fo[qp[j]] = rp.x;
+                fo[qp[j] + 1] = rp.y;
+                fo[qm[j]] = rm.x;
+                fo[qm[j] + 1] = rm.y;
+            } else {
+                fo[qp[j]] = P.x;
+                fo[qp[j] + 1] = P.y;
+                fo[qm[j]] = M.x;
+                fo[qm[j] + 1] = M.y;
+            }
         }
         R hlo = R(0);
         if constexpr (!FRESH) hlo = *hlo_p;
@@ -1003,8 +1013,19 @@ __device__ __forceinline__ void collide_cell(const StepArgs &a,
             fo[5] = fo[5] + d;
             fo[7] = fo[7] + d;
         }
+        if constexpr (S::kHalf) {
+            reinterpret_cast<float *>(dst)[cell] = fo[0];
+            __half *hpl = const_cast<__half *>(S::hp(dst, pitch)) + cell;
+            // planes 1..8 in the order of hb: (1, 2), (3, 4), (5, 6), (7, 8)
 #pragma unroll
-        for (int q = 0; q < 9; ++q) S::st(dst, pitch, q, cell, fo[q]);
+            for (int k = 0; k < 4; ++k) {
+                hpl[(2 * k) * pitch] = __low2half(hb[k]);
+                hpl[(2 * k + 1) * pitch] = __high2half(hb[k]);
+            }
+        } else {
+#pragma unroll
+            for (int q = 0; q < 9; ++q) S::st(dst, pitch, q, cell, fo[q]);
+        }
     }
 }
 
