@@ -164,7 +164,7 @@ int swb_set_inclination(swb_state *s, double ax, double ay, int loop_time, int64
                         int64_t tstart, int64_t tsmooth);
 
 /* Geometry of the fused step: CTAs of nt threads (64, 128, 256) own strips
- * of nt-4 columns and h rows (4..512) that they march row by row; or, with
+ * of nt-4 columns and h rows (2..512) that they march row by row; or, with
  * nt = 32 (SWB_F32 / SWB_F16 only; h is ignored), CTAs of 256 threads own
  * 2D tiles of 32 x 16 cells whose loads are all issued at once.  By default
  * states autotune it on their first swb_step of >= 512 steps (timing a few
@@ -295,7 +295,7 @@ int swb_batch_step(swb_batch *b, int64_t nsteps);
  * lattice saw a non-finite height. */
 int swb_batch_sync(swb_batch *b);
 /* Strips of every lattice: nt threads (64, 128, 256; nt - 4 columns) and
- * `rows` rows (4..512, capped at each lattice's height).  Default 64 x 32:
+ * `rows` rows (2..512, capped at each lattice's height).  Default 64 x 32:
  * the batch's parallelism comes from its many lattices, so strips are tall. */
 int swb_batch_set_geometry(swb_batch *b, int nt, int rows);
 int swb_batch_tile(swb_batch *b, int *tile_x, int *tile_y, int *steps_per_graph);

@@ -226,7 +226,7 @@ void default_geometry(int Lx, int Ly, int precision, int *nt, int *h) {
     if (!n) n = (precision == SWB_F16 && (long long)Lx * Ly <= 512LL * 512) ? 128 : 64;
     const long long strips = (Lx + n - 5) / (n - 4);
     const long long want = precision == SWB_F64 ? 600 : 1000;
-    int hh = kMinRows;
+    int hh = 4;  // 2-row strips only through the tuner (faster at 256², slower at 512²)
     for (int cand : {32, 16, 8}) {
         if (precision == SWB_F16 && cand > 16) continue;
         if (strips * ((Ly + cand - 1) / cand) >= want) {
@@ -596,7 +596,7 @@ int autotune_geometry(swb_state *s, long long &left) {
     }
     // {nt, h, multi-step}
     const int K = swb::kTileGeom;
-    const int all[][3] = {{64, 4, 0},  {64, 8, 0},  {64, 16, 0}, {64, 32, 0}, {128, 4, 0},
+    const int all[][3] = {{64, 2, 0},  {64, 4, 0},  {64, 8, 0},  {64, 16, 0}, {64, 32, 0}, {128, 4, 0},
                           {128, 16, 0}, {256, 16, 0}, {K, 16, 0},  {64, 8, 1},  {64, 16, 1},
                           {128, 8, 1},  {K, 16, 1}};
     std::vector<std::array<int, 3>> cands;

@@ -11,7 +11,7 @@ namespace swb {
 // Fused step geometry: a CTA of NT threads (64, 128 or 256) owns a strip of
 // NT - 4 columns and H rows (kMinRows..kMaxRows).  Partial-measure buffers
 // are sized for the finest decomposition (NT = 64, H = kMinRows).
-constexpr int kMinRows = 4;
+constexpr int kMinRows = 2;
 constexpr int kMaxRows = 512;
 inline long long max_tiles(int Lx, int Ly) {  // per parity slot: strips or 2D tiles
     const long long strips = (long long)((Lx + 59) / 60) * ((Ly + kMinRows - 1) / kMinRows);

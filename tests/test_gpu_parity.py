@@ -212,7 +212,7 @@ def test_geometry_does_not_change_results(T):
     s = sysc(Lx, Ly, tau=0.9, delta=2.0)
     h0 = droplet(Lx, Ly, 30)
     out = []
-    geos = [(64, 4), (128, 16), (256, 64), (128, 512)]
+    geos = [(64, 2), (64, 4), (128, 16), (256, 64), (128, 512)]
     if T != np.float64:
         geos.append((32, 16))  # 2D tiles (FP32 arithmetic only)
     for nt, hh in geos:
