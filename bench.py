@@ -51,7 +51,7 @@ def parse():
     ap.add_argument("--precision", default="f32", choices=["f32", "f16", "f64"])
     ap.add_argument("--chunk", type=int, default=CHUNK)
     ap.add_argument("--no-extras", action="store_true", help="skip the 2048² and FP64 side runs")
-    ap.add_argument("--profile-case", choices=["rt512", "film2048"],
+    ap.add_argument("--profile-case", choices=["rt512", "film2048", "ensemble64"],
                     help="run a few steps of one case, untimed (for ncu captures)")
     ap.add_argument("--geometry", default="",
                     help="strip geometry NT,H (default: the autotuner's choice)")
@@ -623,6 +623,20 @@ def profile_case(args):
     from swalbe_gb300 import configs
     sw.build()
     T = {"f32": np.float32, "f16": np.float16, "f64": np.float64}[args.precision]
+    if args.profile_case == "ensemble64":
+        # the first 64 members of the coalescence ensemble, batched (~0.7 GB)
+        members, _ = configs.ensemble(64)
+        b = sw.Batch([m.sysc for m in members], T=T)
+        for i, m in enumerate(members):
+            b.set_height(i, m.h0)
+        b.step(args.case_steps)
+        b.sync()
+        tx, ty, spg = b.tile()
+        print(json.dumps({"case": args.profile_case, "precision": args.precision,
+                          "lattices": len(members), "cells": sum(m.sysc.Lx * m.sysc.Ly for m in members),
+                          "strip": [tx, ty], "steps": args.case_steps}))
+        b.close()
+        return
     if args.profile_case == "rt512":
         sysc, h0, _ = configs.rayleigh_taylor_512()
         meas = L.MEAS_MASS | L.MEAS_MAXMIN
