@@ -227,9 +227,22 @@ int swb_sync(swb_state *s);
 /* Number of iterations completed since swb_create. */
 int swb_steps_done(swb_state *s, int64_t *t);
 /* Drains the per-step measures recorded since the last call (oldest
- * first); at most `cap` records (capacity of the device ring: 65536). */
+ * first); at most `cap` records.  The device ring holds SWB_RECORD_CAPACITY
+ * records: a caller that steps further than that between two drains loses
+ * the oldest ones, and swb_measures_dropped counts them.  The reference
+ * pushes Δh and wetted! every step (src/simulate.jl:56, src/measures.jl:13-17),
+ * so time_loop drains at least every SWB_RECORD_CAPACITY steps. */
+#define SWB_RECORD_CAPACITY 65536
 int swb_get_measures(swb_state *s, swb_measure *out, int64_t cap, int64_t *count);
-/* Measures of the current height now (mass, wetted, max/min, area). */
+/* Records overwritten in the device ring before swb_get_measures read them,
+ * since the state was created (0 when the host drained in time). */
+int swb_measures_dropped(swb_state *s, int64_t *dropped);
+/* Measures of the current height now (mass, wetted, max/min, area,
+ * surfacearea!'s energy; src/measures.jl:126-168).  The energy's cos θ is
+ * that of the iteration which starts from this height (steps done + 1): the
+ * scalar θ, the θ field at that iteration's offset (a moving substrate), or
+ * the θ wave at that time -- so it equals the step's own record of that
+ * iteration. */
 int swb_measure_now(swb_state *s, double hthresh, swb_measure *out);
 /* The same measures of a caller's Float64 column-major DEVICE height field,
  * without any device allocation by the library.  No counterpart in the
@@ -237,7 +250,9 @@ int swb_measure_now(swb_state *s, double hthresh, swb_measure *out);
  * committed its whole HBM budget, or whose own memory pool owns the device).
  * Scratch is a fixed 48 KiB array compiled into the library; lattices up to
  * 2^28 cells (larger: SWB_ERR_ARG).  d_cos_theta: per-cell cospi(θ) on the
- * device or NULL (then cos_theta is used for the energy).  Runs on `stream`
+ * device or NULL (then cos_theta is used for the energy).  Both fields must
+ * be device memory of the CURRENT device (cudaSetDevice), which owns the
+ * scratch copy the call uses; other pointers give SWB_ERR_ARG.  Runs on `stream`
  * (NULL: the default stream) and synchronises it.  The first call on each
  * device looks up the array's address, so make it before any stream capture.
  * All calls share the array: calls that overlap on the GPU race. */
@@ -276,7 +291,7 @@ int swb_op_thermal(swb_state *s, int64_t t);    /* Fx .-= kbtx, Fy .-= kbty: the
 int swb_op_inclination(swb_state *s, double ax, double ay, int64_t t, int64_t tstart,
                        int64_t tsmooth);        /* src/forcing.jl:363-368 */
 int swb_op_equilibrium(swb_state *s);           /* src/equilibrium.jl:63-119 */
-int swb_op_bgk_stream(swb_state *s);            /* src/collide.jl:261-296, 342-343 */
+int swb_op_bgk_stream(swb_state *s);            /* src/collide.jl:70-105, 151-152 */
 int swb_op_moments(swb_state *s);               /* src/moments.jl:43-64 */
 
 /* ---------------------------------------------------------------------- */

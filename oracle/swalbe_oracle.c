@@ -250,11 +250,11 @@ void orc_equilibrium(double *feq, const double *h, const double *ux, const doubl
     }
 }
 
-/* D2Q9 lattice velocities in the reference's order (src/collide.jl:283-291) */
+/* D2Q9 lattice velocities in the reference's order (src/collide.jl:92-100) */
 static const int CX[9] = {0, 1, 0, -1, 0, 1, -1, -1, 1};
 static const int CY[9] = {0, 0, 1, 0, -1, 1, 1, -1, -1};
 
-/* One cell of the BGK collision with the force source (src/collide.jl:267-280). */
+/* One cell of the BGK collision with the force source (src/collide.jl:76-89). */
 static inline void collide_cell(const double ft[9], const double fe[9], double Fx, double Fy,
                                 double omeg, double invtau, double fo[9]) {
     fo[0] = omeg * ft[0] + invtau * fe[0];
@@ -268,7 +268,7 @@ static inline void collide_cell(const double ft[9], const double fe[9], double F
     fo[8] = omeg * ft[8] + invtau * fe[8] + (1.0 / 24.0) * (Fx - Fy);
 }
 
-/* BGKandStream!(fout, feq, ftemp, Fx, Fy, τ) (src/collide.jl:261-296):
+/* BGKandStream!(fout, feq, ftemp, Fx, Fy, τ) (src/collide.jl:70-105):
  * collide into fout, stream fout into ftemp by circshift!, copy back. */
 void orc_bgk_stream(double *fout, const double *feq, double *ftemp, const double *Fx,
                     const double *Fy, int Lx, int Ly, double tau) {

@@ -252,12 +252,14 @@ struct swb_state {
     StepArgs a{};
     PlainState ps{};
     double *plain_kapF = nullptr;
+    double *plain_cosF = nullptr;  // cospi(θ) of a θ field (the plain path's measures)
     // measures
     Record *rec = nullptr;     // ring of kRecCap
     Record *mrec = nullptr;    // slot for swb_measure_now
     double *mscratch = nullptr;
     unsigned int *mticket = nullptr;
     long long rec_read = 0;    // records consumed by the host
+    long long rec_dropped = 0; // records overwritten before the host read them
     long long plain_rec_head = 0;
     int plain_meas_mask = 0;
     // host mirrors
@@ -421,14 +423,31 @@ int check_nan(swb_state *s) {
     return SWB_OK;
 }
 
+// The θ source of surfacearea!'s energy term for the height that iteration
+// t starts from: the scalar θ, the θ field at its offset of iteration t (a
+// moving substrate), or the θ wave at t -- what the fused step's own measures
+// of iteration t use.
+swb::CosSrc cos_source(const swb_state *s, long long t) {
+    swb::CosSrc cs{};
+    cs.mode = s->a.theta_mode;
+    cs.cos_theta = s->a.cos_theta;
+    cs.cosF = s->plain() ? (const void *)s->plain_cosF : s->a.cosF;
+    if (cs.mode == swb::THETA_FIELD) swb::substrate_shift(s->a, t, &cs.sx, &cs.sy);
+    cs.theta0 = s->a.theta0;
+    cs.dtheta = s->a.dtheta;
+    cs.wave_v = s->a.wave_v;
+    cs.t = t;
+    return cs;
+}
+
 // One plain iteration: the reference's op sequence, one kernel per op.
 int plain_iteration(swb_state *s) {
     const long long t = s->steps + 1;
     const swb_params &p = s->p;
     PlainState &ps = s->ps;
     if (s->plain_meas_mask) {
-        CUDA_TRY(&s->err, swb::launch_measure(ps.h, 1, p.Lx, p.Ly, s->a.hthresh, nullptr,
-                                              s->a.cos_theta, s->mscratch, s->mticket,
+        CUDA_TRY(&s->err, swb::launch_measure(ps.h, 1, p.Lx, p.Ly, s->a.hthresh, cos_source(s, t),
+                                              s->mscratch, s->mticket,
                                               s->rec + (t - 1) % swb::kRecCap, t, s->stream));
         s->plain_rec_head++;
     }
@@ -994,7 +1013,9 @@ int swb_set_theta_field(swb_state *s, const double *theta) {
     StepArgs &a = s->a;
     if (s->plain()) {
         if (!s->plain_kapF) CUDA_TRY(&s->err, s->alloc((void **)&s->plain_kapF, (size_t)N * 8));
+        if (!s->plain_cosF) CUDA_TRY(&s->err, s->alloc((void **)&s->plain_cosF, (size_t)N * 8));
         CUDA_TRY(&s->err, cudaMemcpyAsync(s->plain_kapF, kap.data(), N * 8, cudaMemcpyHostToDevice, s->stream));
+        CUDA_TRY(&s->err, cudaMemcpyAsync(s->plain_cosF, cs.data(), N * 8, cudaMemcpyHostToDevice, s->stream));
         CUDA_TRY(&s->err, cudaStreamSynchronize(s->stream));
     } else {
         if (!a.kapF) {
@@ -1271,7 +1292,11 @@ int swb_get_measures(swb_state *s, swb_measure *out, int64_t cap, int64_t *count
     }
     CUDA_TRY(&s->err, cudaStreamSynchronize(s->stream));
     long long first = s->rec_read;
-    if (head - first > swb::kRecCap) first = head - swb::kRecCap;  // older ones overwritten
+    if (head - first > swb::kRecCap) {  // older ones overwritten
+        s->rec_dropped += head - swb::kRecCap - first;
+        first = head - swb::kRecCap;
+        s->rec_read = first;
+    }
     long long n = head - first;
     if (n > cap) n = cap;
     std::vector<Record> tmp(n);
@@ -1289,14 +1314,31 @@ int swb_get_measures(swb_state *s, swb_measure *out, int64_t cap, int64_t *count
     return check_nan(s);
 }
 
+int swb_measures_dropped(swb_state *s, int64_t *dropped) {
+    if (!s || !dropped) return fail(s ? &s->err : nullptr, SWB_ERR_ARG, "NULL argument");
+    long long head = 0;
+    if (s->plain()) {
+        head = s->plain_rec_head;
+    } else {
+        CUDA_TRY(&s->err, cudaMemcpyAsync(&head, &s->a.ctl->rec_head, sizeof(long long),
+                                          cudaMemcpyDeviceToHost, s->stream));
+        CUDA_TRY(&s->err, cudaStreamSynchronize(s->stream));
+    }
+    const long long lost = head - s->rec_read - swb::kRecCap;
+    *dropped = s->rec_dropped + (lost > 0 ? lost : 0);
+    return SWB_OK;
+}
+
 int swb_measure_now(swb_state *s, double hthresh, swb_measure *out) {
     if (!s || !out) return fail(s ? &s->err : nullptr, SWB_ERR_ARG, "NULL argument");
     int rc = materialize(s);
     if (rc) return rc;
-    const void *cosF = (!s->plain() && s->a.theta_mode == swb::THETA_FIELD) ? s->a.cosF : nullptr;
-    CUDA_TRY(&s->err, swb::launch_measure(s->a.hF, s->rb() == 8, s->p.Lx, s->p.Ly, hthresh, cosF,
-                                          s->a.cos_theta, s->mscratch, s->mticket, s->mrec,
-                                          s->steps, s->stream));
+    // the current height is what iteration steps + 1 starts from: the θ of
+    // a moving field or wave at that iteration, as in its own record
+    const void *h = s->plain() ? (const void *)s->ps.h : s->a.hF;
+    CUDA_TRY(&s->err, swb::launch_measure(h, s->rb() == 8, s->p.Lx, s->p.Ly, hthresh,
+                                          cos_source(s, s->steps + 1), s->mscratch, s->mticket,
+                                          s->mrec, s->steps, s->stream));
     Record r{};
     CUDA_TRY(&s->err, cudaMemcpyAsync(&r, s->mrec, sizeof(Record), cudaMemcpyDeviceToHost, s->stream));
     CUDA_TRY(&s->err, cudaStreamSynchronize(s->stream));

@@ -33,7 +33,7 @@ constexpr int kNPart = 6;
 enum { kAccMass, kAccWet, kAccHmax, kAccHmin, kAccArea, kAccCos, kAccFields };
 constexpr int kAccLanes = 32;
 // Capacity of the per-step measure ring of a single state (records).
-constexpr int kRecCap = 65536;
+constexpr int kRecCap = SWB_RECORD_CAPACITY;
 
 // Device-side control block of one lattice.  A launch sequence of n steps
 // is n step kernels (launch index k = 0..n-1, time_loop iteration
@@ -247,6 +247,22 @@ cudaError_t plain_moments(const PlainState &s, cudaStream_t st);
 // reduction into `rec` (device).  `scratch` holds blocks*kNPart doubles,
 // `ticket` one unsigned int (zero on entry, left zero).
 int measure_blocks(long long N);
+// Where cos θ of a wetted cell comes from (surfacearea!'s energy term): the
+// scalar cos_theta, a θ field's cospi values (cosF, the height's type) moved
+// by (sx, sy) cells, or the θ wave θ0 + Δθ sinpi(2 (x - v t) / Lx) at
+// iteration t, evaluated like the fused step does.
+struct CosSrc {
+    int mode;  // ThetaMode
+    const void *cosF;
+    int sx, sy;
+    double cos_theta;
+    double theta0, dtheta, wave_v;
+    long long t;
+};
+cudaError_t launch_measure(const void *h, int is_double, int Lx, int Ly, double hthresh,
+                           const CosSrc &cs, double *scratch, unsigned int *ticket, Record *rec,
+                           long long t, cudaStream_t st);
+// Scalar θ (cosF null) or a fixed θ field.
 cudaError_t launch_measure(const void *h, int is_double, int Lx, int Ly, double hthresh,
                            const void *cosF, double cos_theta, double *scratch,
                            unsigned int *ticket, Record *rec, long long t, cudaStream_t st);

@@ -59,6 +59,20 @@ int nfail(int code, const std::string &m) {
     return code;
 }
 
+// Whether p is device memory that the current device owns (the scratch
+// address is that device's): cudaPointerGetAttributes allocates nothing.
+bool on_current_device(const void *p) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return false;
+    cudaPointerAttributes pa{};
+    if (cudaPointerGetAttributes(&pa, p) != cudaSuccess) {
+        cudaGetLastError();  // clear the error the query recorded
+        return false;
+    }
+    return (pa.type == cudaMemoryTypeDevice || pa.type == cudaMemoryTypeManaged) &&
+           pa.device == dev;
+}
+
 }  // namespace
 
 extern "C" int swb_measure_field_noalloc(const double *d_height, int Lx, int Ly, double hthresh,
@@ -71,6 +85,9 @@ extern "C" int swb_measure_field_noalloc(const double *d_height, int Lx, int Ly,
                                   "limit of its fixed scratch");
     if (swb::measure_blocks((long long)Lx * Ly) > kMaxBlocks)
         return nfail(SWB_ERR_ARG, "swb_measure_field_noalloc: reduction grid exceeds the scratch");
+    if (!on_current_device(d_height) || (d_cos_theta && !on_current_device(d_cos_theta)))
+        return nfail(SWB_ERR_ARG, "swb_measure_field_noalloc: the height (and cos θ) field must "
+                                  "be device memory of the current device");
     double *scratch = nullptr;
     cudaError_t e = scratch_address(&scratch);
     if (e != cudaSuccess)

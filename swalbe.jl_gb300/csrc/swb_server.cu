@@ -100,10 +100,21 @@ void set_error(swb_server *sv, const std::string &m) {
     sv->err = m;
 }
 
+// A failed admission gives the request's pool memory back, so that the
+// budget accounting (which treats it as free again) stays true.
+void release_device(swb_server *sv, Req *r) {
+    if (r->dev) {
+        cudaFreeAsync(r->dev, sv->stream);
+        cudaStreamSynchronize(sv->stream);
+        r->dev = nullptr;
+    }
+}
+
 // Worker-side: allocate and initialise newly admitted requests.
 bool admit_device(swb_server *sv, Req *r) {
     cudaError_t e = cudaMallocFromPoolAsync((void **)&r->dev, r->bytes, sv->pool, sv->stream);
     if (e != cudaSuccess) {
+        r->dev = nullptr;
         set_error(sv, std::string("admit: ") + cudaGetErrorString(e));
         return false;
     }
@@ -116,7 +127,9 @@ bool admit_device(swb_server *sv, Req *r) {
         cudaFree(sv->staging);
         sv->staging = nullptr;
         if (cudaMalloc((void **)&sv->staging, (size_t)N * 8) != cudaSuccess) {
+            sv->staging = nullptr;
             sv->staging_elems = 0;
+            release_device(sv, r);
             set_error(sv, "admit: staging allocation failed");
             return false;
         }
@@ -126,6 +139,7 @@ bool admit_device(swb_server *sv, Req *r) {
     if (e == cudaSuccess) e = swb::lattice_upload_height(r->a, sv->precision, r->h0.data(), sv->staging, sv->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(sv->stream);
     if (e != cudaSuccess) {
+        release_device(sv, r);
         set_error(sv, std::string("admit: ") + cudaGetErrorString(e));
         return false;
     }

@@ -261,7 +261,7 @@ cudaError_t plain_stream(const PlainState &s, cudaStream_t st) {
     k_stream<<<grid_for(s.N, 256), 256, 0, st>>>(s);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    // fout .= ftemp (src/collide.jl:294)
+    // fout .= ftemp (src/collide.jl:103)
     return cudaMemcpyAsync(s.fout, s.ftemp, 9 * s.N * sizeof(double), cudaMemcpyDeviceToDevice,
                            st);
 }
@@ -269,44 +269,60 @@ cudaError_t plain_moments(const PlainState &s, cudaStream_t st) { PLAIN_LAUNCH(k
 
 // ------------------------------------------------------------ measures
 // Grid-stride partials per block, then the last block (ticket) reduces the
-// partials in a fixed order and writes one Record.
+// partials in a fixed order and writes one Record.  Per-cell values are
+// computed in the height's type R (as the fused step computes them); the
+// block sums are Float64 for every R.  cos θ of a wetted cell comes from the
+// θ source `cs`: a scalar, a (possibly moving) field, or the θ wave, with the
+// fused step's formulas for its iteration cs.t.
+template <class R>
+__device__ __forceinline__ R cos_of_cell(const CosSrc &cs, long long c, int Lx, int Ly) {
+    const int i = (int)(c % Lx), j = (int)(c / Lx);
+    if (cs.mode == THETA_FIELD) {
+        const int fi = cs.sx ? (i - cs.sx < 0 ? i - cs.sx + Lx : i - cs.sx) : i;
+        const int fj = cs.sy ? (j - cs.sy < 0 ? j - cs.sy + Ly : j - cs.sy) : j;
+        return reinterpret_cast<const R *>(cs.cosF)[(long long)fj * Lx + fi];
+    }
+    const R th = R(cs.theta0) + R(cs.dtheta) * sinpi_r(R(2) * (R(i) - R(cs.wave_v) * R(cs.t)) / R(Lx));
+    return cospi_r(th);
+}
+
 template <class R>
 __global__ void __launch_bounds__(256) measure_kernel(const R *h, int Lx, int Ly, R thr,
-                                                      const R *cosF, double cos_theta,
-                                                      double *scratch, unsigned int *ticket,
-                                                      Record *rec, long long t) {
-    __shared__ PartT<R> red[8];
-    __shared__ PartT<double> redd[8];
+                                                      const CosSrc cs, double *scratch,
+                                                      unsigned int *ticket, Record *rec,
+                                                      long long t) {
+    __shared__ PartT<double> red[8];
     __shared__ int last;
     const long long N = (long long)Lx * Ly;
-    PartT<R> p;
+    const bool percell = cs.mode != THETA_SCALAR;
+    PartT<double> p;
     part_init(p);
     for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < N;
          c += (long long)gridDim.x * blockDim.x) {
         const R v = h[c];
-        mass_add(p, v);
+        mass_add(p, (double)v);
         const bool wet = v > thr;
         p.wet += wet ? 1 : 0;
-        p.hmax = fmax(p.hmax, v);
-        p.hmin = fmin(p.hmin, v);
+        p.hmax = fmax(p.hmax, (double)v);
+        p.hmin = fmin(p.hmin, (double)v);
         if (wet) {
             const Nb b = neighbours(c, Lx, Ly);
             R gx, gy;
             grad9<R>(h[b.ip], h[b.jp], h[b.im], h[b.jm], h[b.ipjp], h[b.imjp], h[b.imjm],
                      h[b.ipjm], gx, gy);
-            p.area += sqrt(gx * gx + gy * gy + R(1));
-            if (cosF) p.cossum += cosF[c];
+            p.area += (double)R(sqrt(gx * gx + gy * gy + R(1)));
+            if (percell) p.cossum += (double)cos_of_cell<R>(cs, c, Lx, Ly);
         }
     }
-    PartT<R> tot = block_reduce<256>(p, red);
+    PartT<double> tot = block_reduce<256>(p, red);
     if (threadIdx.x == 0) {
         double *pp = scratch + (size_t)blockIdx.x * kNPart;
-        pp[0] = (double)tot.mhi + (double)tot.mlo;
+        pp[0] = tot.mhi + tot.mlo;
         pp[1] = (double)tot.wet;
-        pp[2] = (double)tot.hmax;
-        pp[3] = (double)tot.hmin;
-        pp[4] = (double)tot.area;
-        pp[5] = (double)tot.cossum;
+        pp[2] = tot.hmax;
+        pp[3] = tot.hmin;
+        pp[4] = tot.area;
+        pp[5] = tot.cossum;
         __threadfence();
         last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
     }
@@ -327,7 +343,7 @@ __global__ void __launch_bounds__(256) measure_kernel(const R *h, int Lx, int Ly
         q.cossum = __ldcg(pp + 5);
         part_merge(acc, q);
     }
-    acc = block_reduce<256>(acc, redd);
+    acc = block_reduce<256>(acc, red);
     if (threadIdx.x == 0) {
         rec->t = t;
         rec->mass = acc.mhi + acc.mlo;
@@ -335,7 +351,7 @@ __global__ void __launch_bounds__(256) measure_kernel(const R *h, int Lx, int Ly
         rec->hmax = acc.hmax;
         rec->hmin = acc.hmin;
         rec->area = acc.area;
-        rec->cos_sum = cosF ? acc.cossum : (double)acc.wet * cos_theta;
+        rec->cos_sum = percell ? acc.cossum : (double)acc.wet * cs.cos_theta;
         *ticket = 0u;
     }
 }
@@ -347,19 +363,27 @@ int measure_blocks(long long N) {
 }
 
 cudaError_t launch_measure(const void *h, int is_double, int Lx, int Ly, double hthresh,
-                           const void *cosF, double cos_theta, double *scratch, unsigned int *ticket,
-                           Record *rec, long long t, cudaStream_t st) {
+                           const CosSrc &cs, double *scratch, unsigned int *ticket, Record *rec,
+                           long long t, cudaStream_t st) {
     const int blocks = measure_blocks((long long)Lx * Ly);
     count_launches(1);
     if (is_double)
-        measure_kernel<double><<<blocks, 256, 0, st>>>((const double *)h, Lx, Ly, hthresh,
-                                                       (const double *)cosF, cos_theta, scratch, ticket,
-                                                       rec, t);
+        measure_kernel<double><<<blocks, 256, 0, st>>>((const double *)h, Lx, Ly, hthresh, cs,
+                                                       scratch, ticket, rec, t);
     else
         measure_kernel<float><<<blocks, 256, 0, st>>>((const float *)h, Lx, Ly, (float)hthresh,
-                                                      (const float *)cosF, cos_theta, scratch, ticket,
-                                                      rec, t);
+                                                      cs, scratch, ticket, rec, t);
     return cudaGetLastError();
+}
+
+cudaError_t launch_measure(const void *h, int is_double, int Lx, int Ly, double hthresh,
+                           const void *cosF, double cos_theta, double *scratch, unsigned int *ticket,
+                           Record *rec, long long t, cudaStream_t st) {
+    CosSrc cs{};
+    cs.mode = cosF ? THETA_FIELD : THETA_SCALAR;
+    cs.cosF = cosF;
+    cs.cos_theta = cos_theta;
+    return launch_measure(h, is_double, Lx, Ly, hthresh, cs, scratch, ticket, rec, t, st);
 }
 
 }  // namespace swb

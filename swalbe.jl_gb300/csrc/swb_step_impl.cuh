@@ -133,7 +133,7 @@ __device__ __forceinline__ R kappa_of(R theta, int n, int m, R hmin) {
 }
 
 // Pull the nine populations of cell (gx, gy) from the post-collision buffer:
-// f_q(x) = fpost_q(x - c_q), c_q as in src/collide.jl:283-291.
+// f_q(x) = fpost_q(x - c_q), c_q as in src/collide.jl:92-100.
 template <class S>
 __device__ __forceinline__ void pull9(const void *src, int pitch, int Lx, int gx, int gy,
                                       int gxm, int gxp, int gym, int gyp,
@@ -302,7 +302,7 @@ __device__ __forceinline__ void feq_literal(R h, R ux, R uy, R g, R fe[9]) {
     fe[8] = w5 * h * (g0 * h + R(3) * (ux - uy) + R(4.5) * ((ux - uy) * (ux - uy)) - R(1.5) * vsq);
 }
 
-// Force source of BGKandStream! (src/collide.jl:272-280).
+// Force source of BGKandStream! (src/collide.jl:80-89).
 template <class R>
 __device__ __forceinline__ R source(int q, R Fx, R Fy) {
     switch (q) {
@@ -850,7 +850,7 @@ __device__ __forceinline__ CellConst<R> cell_consts(const StepArgs &a, long long
 // Forces, equilibrium and collision of one cell and the store of its nine
 // post-collision populations: slippage! (src/forcing.jl:43-44), the force sum
 // (src/simulate.jl:18-19), inclination! (src/forcing.jl:364-365),
-// equilibrium! and BGKandStream! (src/collide.jl:267-280).  (gpx, gpy) is
+// equilibrium! and BGKandStream! (src/collide.jl:76-89).  (gpx, gpy) is
 // ∇p at the cell (h∇p!, src/forcing.jl:181-184); *hlo_p the rounding
 // residue of the pulled height (FP32 arithmetic; not read for a fresh step).
 // GEN = false compiles out the rare forces (thermal, inclination) for the
@@ -904,7 +904,7 @@ __device__ __forceinline__ void collide_cell(const StepArgs &a,
             Fy = __fmaf_rn(h * R(a.ay), cc.incl_fac, Fy);
         }
     }
-    // collision (src/collide.jl:267-280); ftemp only matters for τ != 1
+    // collision (src/collide.jl:76-89); ftemp only matters for τ != 1
     R fq[9];
     R hft = h;
     if constexpr (!TAU1) {
@@ -945,7 +945,7 @@ __device__ __forceinline__ void collide_cell(const StepArgs &a,
         // the FP64-measured correction.
         // Opposite populations (q+, q-) share their equilibrium's even part
         // A and odd part B (feq = A ± B, src/equilibrium.jl:67-114) and their
-        // force source ±S (src/collide.jl:272-280).
+        // force source ±S (src/collide.jl:80-89).
         R fo[9];
         const R vsq = __fmaf_rn(ux, ux, uy * uy);
         const R base = __fmaf_rn(R(1.5) * cc.g, h, R(-1.5) * vsq);

@@ -32,6 +32,7 @@ FIELD = {"height": 0, "velx": 1, "vely": 2, "pressure": 3, "fout": 4, "feq": 5, 
 FIELD_HEIGHT, FIELD_VELX, FIELD_VELY, FIELD_PRESSURE, FIELD_FOUT = 0, 1, 2, 3, 4
 
 MEAS_MASS, MEAS_WETTED, MEAS_MAXMIN, MEAS_AREA, MEAS_ALL = 1, 2, 4, 8, 15
+RECORD_CAPACITY = 65536  # SWB_RECORD_CAPACITY: per-step records the device ring holds
 STEP_AUTO, STEP_PER_ITERATION, STEP_MULTI = 0, 1, 2
 
 
@@ -108,6 +109,7 @@ def lib() -> C.CDLL:
             "swb_sync": (i, [p]),
             "swb_steps_done": (i, [p, C.POINTER(i64)]),
             "swb_get_measures": (i, [p, C.POINTER(Measure), i64, C.POINTER(i64)]),
+            "swb_measures_dropped": (i, [p, C.POINTER(i64)]),
             "swb_measure_now": (i, [p, d, C.POINTER(Measure)]),
             "swb_measure_field_noalloc": (i, [p, i, i, d, p, d, p, C.POINTER(Measure)]),
             "swb_op_filmpressure": (i, [p]),

@@ -293,6 +293,12 @@ class GB300State:
         self._chk(lib().swb_get_measures(self._h, buf, cap, C.byref(n)))
         return np.ctypeslib.as_array(buf)[: n.value].copy()
 
+    def measures_dropped(self) -> int:
+        """Per-step records overwritten on the device before they were read."""
+        n = C.c_int64()
+        self._chk(lib().swb_measures_dropped(self._h, C.byref(n)))
+        return n.value
+
     def measure_now(self, hthresh: float = 0.055) -> L.Measure:
         m = L.Measure()
         self._chk(lib().swb_measure_now(self._h, hthresh, C.byref(m)))
@@ -365,7 +371,7 @@ def equilibrium_(state: GB300State, sysc: SysConst) -> None:
 
 
 def BGKandStream_(state: GB300State, sysc: SysConst) -> None:
-    """BGKandStream!(state, sys) (src/collide.jl:342-343)."""
+    """BGKandStream!(state, sys) (src/collide.jl:151-152)."""
     state._chk(lib().swb_op_bgk_stream(state.handle))
 
 
@@ -436,9 +442,23 @@ def time_loop(sysc: SysConst, state: GB300State, *args, verbose: bool = False):
     if callback is not None and callback not in (wetted_, inclination_):
         for _ in range(Tmax):
             _plain_iteration_with_callback(sysc, state, callback, measure)
+        recs = state.measures_array(cap=max(Tmax, 1))
     else:
-        state.step(Tmax)
-    recs = state.measures_array(cap=max(Tmax, 1))
+        # the device ring holds RECORD_CAPACITY per-step records: step in
+        # chunks no longer than that and drain after each, so that every
+        # step's Δh / wetted! entry reaches the host (src/simulate.jl:56)
+        state.measures_array(cap=L.RECORD_CAPACITY)  # records of earlier calls
+        dropped0 = state.measures_dropped()
+        parts = []
+        left = Tmax
+        while left > 0:
+            n = min(left, L.RECORD_CAPACITY)
+            state.step(n)
+            parts.append(state.measures_array(cap=n))
+            left -= n
+        recs = np.concatenate(parts) if parts else state.measures_array(cap=1)
+        if state.measures_dropped() != dropped0:
+            raise RuntimeError("per-step records were overwritten before they were read")
     if verbose and P.tdump > 0:
         for r in recs[recs["t"] % P.tdump == 0]:
             print(f"Time step {int(r['t'])} mass is {round(float(r['mass']), 3)}")

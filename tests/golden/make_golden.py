@@ -14,8 +14,8 @@ import os
 
 G = {}
 
-# test/differences.jl:21-32 (also src/differences.jl:125-139, test/forcing.jl:279-288,
-# test/measures.jl:203-213): ∇f! of reshape(1:25,5,5); `==` comparison.
+# test/differences.jl:21-32 (also src/differences.jl:125-139, test/forcing.jl:119-128,
+# test/measures.jl:66-79): ∇f! of reshape(1:25,5,5); `==` comparison.
 G["grad_solx"] = {
     "src": "test/differences.jl:21-32",
     "rows": [[-1.5] * 5, [1.0] * 5, [1.0] * 5, [1.0] * 5, [-1.5] * 5],
@@ -55,9 +55,9 @@ G["power_broad"] = {
     "five": [125.0, 15625.0],
     "vec": {"args": [2.0, 3.0, 4.0], "rows": [[8.0, 27.0, 64.0], [64.0, 729.0, 4096.0]]},
 }
-# test/forcing.jl:173-229: slippage!, h = 1, μ = 1/6
+# test/forcing.jl:13-69: slippage!, h = 1, μ = 1/6
 G["slippage"] = {
-    "src": "test/forcing.jl:173-229",
+    "src": "test/forcing.jl:13-69",
     "cases": [
         {"ux": 0.0, "uy": 0.0, "delta": 1.0, "sx": 0.0, "sy": 0.0, "exact": True},
         {"ux": 0.1, "uy": 0.0, "delta": 1.0, "sx": 0.1 / 11, "sy": 0.0},
@@ -70,16 +70,16 @@ G["slippage"] = {
 # src/forcing.jl:147-157 doctest: 10x10, pressure = reshape(1:100,10,10), h = 1:
 # h∇px[1,:] == -4, h∇px[2,:] == 1 (exact).
 G["hgradp_doctest"] = {"src": "src/forcing.jl:147-157", "row1": -4.0, "row2": 1.0}
-# test/forcing.jl:326-344: inclination!([0.1,0.1], state, t, tstart=0, tsmooth=1), h = 1
+# test/forcing.jl:166-184: inclination!([0.1,0.1], state, t, tstart=0, tsmooth=1), h = 1
 G["inclination"] = {
-    "src": "test/forcing.jl:333-343",
+    "src": "test/forcing.jl:173-183",
     "alpha": [0.1, 0.1],
     "cases": [{"t": 0, "value": 0.05}, {"t": 1, "value_formula": "0.1*(0.5+0.5*tanh(1.0))"}],
 }
 # test/equilibrium.jl:6-83 (values given as formulas; see the test for exact/≈)
 G["equilibrium"] = {"src": "test/equilibrium.jl:6-83"}
 # test/collide.jl:27-123 (τ = 1 and τ = 0.75, forces ±0.1)
-G["collide"] = {"src": "test/collide.jl:163-276", "tau2": 0.75, "ftemp_fill": 1.2}
+G["collide"] = {"src": "test/collide.jl:27-138", "tau2": 0.75, "ftemp_fill": 1.2}
 # test/moments.jl:14-134
 G["moments"] = {
     "src": "test/moments.jl:14-134",
@@ -93,17 +93,17 @@ G["moments"] = {
     ],
 }
 # test/measures.jl:2-24 wetted!; test/measures.jl:55-115 surfacearea!
-G["wetted"] = {"src": "test/measures.jl:137-159", "block_2_3": 4, "diag_series": [1, 2, 3, 4, 5]}
+G["wetted"] = {"src": "test/measures.jl:2-24", "block_2_3": 4, "diag_series": [1, 2, 3, 4, 5]}
 # test/simulate.jl: integration tests (physics tolerances, not bit pins)
 G["simulate"] = {
-    "flat": {"src": "test/simulate.jl:268-274", "L": 25, "Tmax": 200, "tdump": 100},
-    "random": {"src": "test/simulate.jl:281-286", "L": 25, "Tmax": 10000, "eps": 0.1,
+    "flat": {"src": "test/simulate.jl:3-7", "L": 25, "Tmax": 200, "tdump": 100},
+    "random": {"src": "test/simulate.jl:16-21", "L": 25, "Tmax": 10000, "eps": 0.1,
                "bound": 0.1},
-    "rayleigh_taylor": {"src": "test/simulate.jl:297-300", "L": 100, "Tmax": 1000, "g": -0.002,
+    "rayleigh_taylor": {"src": "test/simulate.jl:32-35", "L": 100, "Tmax": 1000, "g": -0.002,
                         "kx": 4, "ky": 5, "eps": 0.01},
-    "droplet": {"src": "test/simulate.jl:307-325", "L": 150, "R": 35, "Tmax": 10000,
+    "droplet": {"src": "test/simulate.jl:42-60", "L": 150, "R": 35, "Tmax": 10000,
                 "delta": 3.0, "theta0": 1 / 6, "theta": 1 / 9, "rtol": 0.10},
-    "sliding": {"src": "test/simulate.jl:411-420", "L": 150, "R": 35, "Tmax": 5000,
+    "sliding": {"src": "test/simulate.jl:146-155", "L": 150, "R": 35, "Tmax": 5000,
                 "delta": 2.0, "fx": 1e-4},
 }
 

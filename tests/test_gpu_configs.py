@@ -1,0 +1,141 @@
+"""GPU parity at the benchmark workloads' own sizes, and per-step records
+past the device ring's capacity.
+
+* Rayleigh–Taylor film, 512² (g = -0.001, γ = 0.0005, θ = 1/9, h0 = 1 +
+  U[-0.01, 0.01], seed 2), 2000 steps with the Δh series: Float64 bit-exact
+  against the oracle; FP32 within 1e-4 relative L2 of h (the north-star
+  tolerance of the FP32 mode).
+* Coalescence ensemble: two members of each lattice size (128², 256², 512²,
+  1024x256) from the seeded ensemble, through one Batch: FP32 equal to the
+  same members run alone, Float64 bit-exact against the oracle.
+* time_loop(sys, state, Δh) with Tmax beyond the 65,536-record ring: every
+  step's Δh reaches the host, equal to the oracle's.
+"""
+import numpy as np
+import pytest
+
+import oracle
+import swalbe_gb300 as sw
+from swalbe_gb300 import _lib as L
+from swalbe_gb300 import configs
+
+pytestmark = pytest.mark.gpu
+
+
+def oparams(s: sw.SysConst):
+    p = s.param
+    return oracle.params(s.Lx, s.Ly, Tmax=p.Tmax, tdump=p.tdump, tau=p.tau, cs=p.cs, mu=p.mu,
+                         delta=p.delta, gamma=p.gamma, n=p.n, m=p.m, hmin=p.hmin, hcrit=p.hcrit,
+                         theta=p.theta, g=p.g)
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def run(s, h0, steps, T, meas=0):
+    st = sw.Sys(s, "GB300", T=T)
+    st.height = h0
+    if meas:
+        st.set_measures(meas)
+    st.step(steps)
+    st.sync()
+    return st
+
+
+@pytest.fixture(scope="module")
+def rt512():
+    s, h0, _ = configs.rayleigh_taylor_512()
+    steps = 2000
+    ref = oracle.FusedState(oparams(s), h0).run(steps, record_dh=True)
+    return s, h0, steps, ref
+
+
+def test_rayleigh_taylor_512_f64_bit_exact(rt512):
+    s, h0, steps, ref = rt512
+    st = run(s, h0, steps, np.float64, meas=L.MEAS_MASS | L.MEAS_MAXMIN)
+    assert np.array_equal(st.height, ref.height)
+    assert np.array_equal(st.velx, ref.velx) and np.array_equal(st.vely, ref.vely)
+    recs = st.measures_array(cap=steps)
+    assert np.array_equal(recs["t"], np.arange(1, steps + 1))
+    assert np.array_equal(recs["hmax"] - recs["hmin"], ref.dh)
+    sel = ~np.isnan(ref.mass)
+    assert np.allclose(recs["mass"][sel], ref.mass[sel], rtol=1e-13, atol=0)
+
+
+def test_rayleigh_taylor_512_fp32(rt512):
+    s, h0, steps, ref = rt512
+    st = run(s, h0, steps, np.float32, meas=L.MEAS_MASS | L.MEAS_MAXMIN)
+    assert rel_l2(st.height, ref.height) < 1e-4
+    m = st.measures_array(cap=steps)["mass"]
+    assert np.abs(m - m[0]).max() / m[0] < 1e-10
+
+
+def ensemble_sample(per_size=2):
+    """The first `per_size` members of each lattice size of the seeded
+    coalescence ensemble (its first 40 members are those of the 512-member
+    set: the generator draws member by member)."""
+    members, _ = configs.ensemble(count=40)
+    picked, seen = [], {}
+    for mb in members:
+        key = (mb.sysc.Lx, mb.sysc.Ly)
+        if seen.get(key, 0) < per_size:
+            seen[key] = seen.get(key, 0) + 1
+            picked.append(mb)
+    assert len(picked) == 4 * per_size
+    return picked
+
+
+def test_ensemble_members_fp32_batch_equals_single():
+    sample = ensemble_sample()
+    steps = 300
+    b = sw.Batch([mb.sysc for mb in sample], T=np.float32)
+    for i, mb in enumerate(sample):
+        b.set_height(i, mb.h0)
+    b.step(steps)
+    b.sync()
+    for i, mb in enumerate(sample):
+        st = run(mb.sysc, mb.h0, steps, np.float32)
+        assert np.array_equal(b.get_height(i), st.height), i
+    b.close()
+
+
+def test_ensemble_members_f64_batch_vs_oracle():
+    sample = ensemble_sample()
+    steps = 200
+    b = sw.Batch([mb.sysc for mb in sample], T=np.float64)
+    for i, mb in enumerate(sample):
+        b.set_height(i, mb.h0)
+    b.step(steps)
+    b.sync()
+    for i, mb in enumerate(sample):
+        ref = oracle.FusedState(oparams(mb.sysc), mb.h0).run(steps)
+        assert np.array_equal(b.get_height(i), ref.height), i
+    b.close()
+
+
+def test_time_loop_dh_past_ring_capacity():
+    n = L.RECORD_CAPACITY + 4464  # 70,000 steps
+    s = sw.SysConst(16, 16, sw.Taumucs(Tmax=n))
+    rng = np.random.default_rng(7)
+    h0 = np.asfortranarray(1.0 + 0.1 * rng.uniform(-1, 1, (16, 16)))
+    st = sw.Sys(s, "GB300", T=np.float64)
+    st.height = h0
+    dh = []
+    sw.time_loop(s, st, dh)
+    assert len(dh) == n
+    ref = oracle.time_loop_literal(oparams(s), h0, n, record_dh=True)
+    assert np.array_equal(np.asarray(dh), ref.dh)
+    assert np.array_equal(st.height, ref.height)
+    assert st.measures_dropped() == 0
+
+
+def test_dropped_records_are_counted():
+    s = sw.SysConst(8, 8, sw.Taumucs())
+    st = sw.Sys(s, "GB300", T=np.float64)
+    st.set_measures(L.MEAS_MASS)
+    st.step(L.RECORD_CAPACITY + 100)
+    assert st.measures_dropped() == 100
+    recs = st.measures_array(cap=L.RECORD_CAPACITY + 100)
+    assert len(recs) == L.RECORD_CAPACITY and recs["t"][0] == 101
+    assert st.measures_dropped() == 100

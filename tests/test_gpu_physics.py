@@ -20,7 +20,7 @@ def sysc(L, **kw):
 
 @pytest.mark.parametrize("T", MODES)
 def test_flat_interface(T):
-    # test/simulate.jl:268-274: all(h .== 1.0) and sum(h) == 625, bit for bit
+    # test/simulate.jl:3-7: all(h .== 1.0) and sum(h) == 625, bit for bit
     h = sw.run_flat(sysc(25, Tmax=200, tdump=100), "GB300", verbos=False, T=T)
     assert np.all(h == 1.0)
     assert np.sum(h) == 625
@@ -28,7 +28,7 @@ def test_flat_interface(T):
 
 @pytest.mark.parametrize("T", MODES)
 def test_random_interface(T):
-    # test/simulate.jl:281-286
+    # test/simulate.jl:16-21
     h = sw.run_random(sysc(25, Tmax=10000, tdump=5000), "GB300", ϵ=0.1, verbos=False, T=T,
                       rng=np.random.default_rng(11))
     assert h.max() - h.min() < 0.1
@@ -36,7 +36,7 @@ def test_random_interface(T):
 
 @pytest.mark.parametrize("T", MODES)
 def test_rayleigh_taylor(T):
-    # test/simulate.jl:297-300
+    # test/simulate.jl:32-35
     _, diff = sw.run_rayleightaylor(sysc(100, Tmax=1000, tdump=500, g=-0.002), "GB300", kx=4,
                                     ky=5, ϵ=0.01, verbos=False, T=T)
     assert len(diff) == 1000
@@ -58,7 +58,7 @@ def droplet_checks(h, R=35, th0=1 / 6, th=1 / 9):
 
 @pytest.mark.parametrize("T", MODES)
 def test_droplet_relax(T):
-    # test/simulate.jl:307-325
+    # test/simulate.jl:42-60
     h, A = sw.run_dropletrelax(sysc(150, Tmax=10000, delta=3.0), "GB300", radius=35,
                                verbos=False, T=T)
     droplet_checks(h)
@@ -67,7 +67,7 @@ def test_droplet_relax(T):
 
 @pytest.mark.parametrize("T", [np.float64, np.float32])
 def test_droplet_patterned(T):
-    # test/simulate.jl:361-377
+    # test/simulate.jl:96-112
     h = sw.run_dropletpatterned(sysc(150, Tmax=10000, delta=3.0), "GB300", radius=35,
                                 θₛ=np.full((150, 150), 1 / 9), verbos=False, T=T)
     droplet_checks(h)
@@ -75,7 +75,7 @@ def test_droplet_patterned(T):
 
 @pytest.mark.parametrize("T", [np.float64, np.float32])
 def test_droplet_forced(T):
-    # test/simulate.jl:411-420: the maximum moves in x, not in y; |u| < 0.1
+    # test/simulate.jl:146-155: the maximum moves in x, not in y; |u| < 0.1
     h, u, v = sw.run_dropletforced(sysc(150, Tmax=5000, delta=2.0), "GB300", radius=35, fx=1e-4,
                                    verbos=False, T=T)
     ix, iy = np.unravel_index(np.argmax(h), h.shape)

@@ -92,7 +92,7 @@ def test_power_broad(orc, golden):
 
 # ---------------------------------------------------------------- forcing
 def test_slippage(orc, golden):
-    # test/forcing.jl:173-229 (h = 1, μ = 1/6)
+    # test/forcing.jl:13-69 (h = 1, μ = 1/6)
     g = golden["slippage"]
     h = np.ones((5, 5))
     for c in g["cases"]:
@@ -106,7 +106,7 @@ def test_slippage(orc, golden):
 
 
 def test_hgradp_ramp(orc, golden, ramp):
-    # test/forcing.jl:264-299: h = 1 (Sys default), pressure = ramp; exact ==
+    # test/forcing.jl:104-139: h = 1 (Sys default), pressure = ramp; exact ==
     gx, gy = orc.hgradp(np.ones((5, 5)), ramp)
     assert np.array_equal(gx, M(golden["grad_solx"]["rows"]))
     assert np.array_equal(gy, M(golden["grad_soly"]["rows"]))
@@ -121,7 +121,7 @@ def test_hgradp_doctest(orc, golden):
 
 
 def test_inclination(orc, golden):
-    # test/forcing.jl:326-344: exact ==
+    # test/forcing.jl:166-184: exact ==
     g = golden["inclination"]
     h = np.ones((5, 5))
     for c in g["cases"]:
@@ -178,7 +178,7 @@ SHIFTS = [(0, 0), (1, 0), (0, 1), (-1, 0), (0, -1), (1, 1), (-1, 1), (-1, -1), (
 
 
 def test_bgk_tau1_no_forces(orc):
-    # test/collide.jl:180-196 and doctest src/collide.jl:227-250
+    # test/collide.jl:27-43 and doctest src/collide.jl:33-59
     feq = np.ones((5, 5, 9), order="F")
     feq[0, 0, :] = 2.0
     fout, _ = orc.bgk_stream(feq, np.ones((5, 5, 9)), np.zeros((5, 5)), np.zeros((5, 5)), 1.0)
@@ -188,7 +188,7 @@ def test_bgk_tau1_no_forces(orc):
 
 
 def test_bgk_tau1_forces(orc):
-    # test/collide.jl:197-224: ftemp = 1.2, feq = 1, Fx = 0.1, Fy = -0.1; exact ==
+    # test/collide.jl:44-71: ftemp = 1.2, feq = 1, Fx = 0.1, Fy = -0.1; exact ==
     feq = np.ones((5, 5, 9), order="F")
     fout, _ = orc.bgk_stream(feq, np.full((5, 5, 9), 1.2), np.full((5, 5), 0.1),
                              np.full((5, 5), -0.1), 1.0)
@@ -201,7 +201,7 @@ def test_bgk_tau1_forces(orc):
 
 @pytest.mark.parametrize("forces", [False, True])
 def test_bgk_tau075(orc, forces):
-    # test/collide.jl:225-276: ftemp = 1 (set_dist!), feq = 1 with feq[1,1,:] = 2
+    # test/collide.jl:72-138: ftemp = 1 (set_dist!), feq = 1 with feq[1,1,:] = 2
     feq = np.ones((5, 5, 9), order="F")
     feq[0, 0, :] = 2.0
     ftemp = np.ones((5, 5, 9), order="F")
@@ -216,7 +216,7 @@ def test_bgk_tau075(orc, forces):
     assert np.array_equal(fout[:, :, 0], base)
     for q in range(1, 9):
         w = _shift(base + add[q], SHIFTS[q])
-        if q == 1:  # the reference compares population 2 with ≈ (test/collide.jl:241)
+        if q == 1:  # the reference compares population 2 with ≈ (test/collide.jl:88)
             assert np.allclose(fout[:, :, q], w)
         else:
             assert np.array_equal(fout[:, :, q], w), q
@@ -298,7 +298,7 @@ def test_singledroplet(orc):
 
 # ---------------------------------------------------------------- time loops
 def test_flat_interface_bit_exact(orc, golden):
-    # test/simulate.jl:268-274: all(h .== 1.0), sum(h) == 625
+    # test/simulate.jl:3-7: all(h .== 1.0), sum(h) == 625
     g = golden["simulate"]["flat"]
     P = orc.params(g["L"], g["L"], Tmax=g["Tmax"], tdump=g["tdump"])
     r = orc.time_loop_literal(P, np.ones((g["L"], g["L"])), g["Tmax"])

@@ -27,7 +27,7 @@ def droplet_shape(h, row):
 
 
 def test_random_interface_flattens(orc, golden):
-    # test/simulate.jl:281-286: max - min < 0.1 after 10k steps, θ = 1/9
+    # test/simulate.jl:16-21: max - min < 0.1 after 10k steps, θ = 1/9
     g = golden["simulate"]["random"]
     L = g["L"]
     P = orc.params(L, L, Tmax=g["Tmax"], tdump=5000)
@@ -38,7 +38,7 @@ def test_random_interface_flattens(orc, golden):
 
 
 def test_rayleigh_taylor_grows(orc, golden):
-    # test/simulate.jl:297-300: diff[1] < diff[end]
+    # test/simulate.jl:32-35: diff[1] < diff[end]
     g = golden["simulate"]["rayleigh_taylor"]
     L = g["L"]
     P = orc.params(L, L, Tmax=g["Tmax"], tdump=500, g=g["g"])
@@ -51,7 +51,7 @@ def test_rayleigh_taylor_grows(orc, golden):
 
 
 def test_droplet_relaxes(orc, golden):
-    # test/simulate.jl:307-325: volume and radius within 10 %, wetted area grows
+    # test/simulate.jl:42-60: volume and radius within 10 %, wetted area grows
     g = golden["simulate"]["droplet"]
     L, R = g["L"], g["R"]
     P = orc.params(L, L, Tmax=g["Tmax"], delta=g["delta"])
@@ -65,7 +65,7 @@ def test_droplet_relaxes(orc, golden):
 
 
 def test_sliding_droplet(orc, golden):
-    # test/simulate.jl:411-420: maximum moves in x only, |u| < 0.1
+    # test/simulate.jl:146-155: maximum moves in x only, |u| < 0.1
     g = golden["simulate"]["sliding"]
     L, R = g["L"], g["R"]
     P = orc.params(L, L, Tmax=g["Tmax"], delta=g["delta"])
