@@ -58,8 +58,9 @@ def parse():
     ap.add_argument("--step-mode", default="per_iteration", choices=["per_iteration", "multi"],
                     help="launch form for --profile-case")
     ap.add_argument("--case-steps", type=int, default=12)
-    ap.add_argument("--workload", choices=["ensemble", "serving", "spinodal"],
-                    help="print the ensemble, serving or spinodal-comparison line only")
+    ap.add_argument("--workload", choices=["ensemble", "serving", "spinodal", "lattice2048"],
+                    help="print the ensemble, serving, spinodal-comparison or 2048² FP32/FP16 "
+                         "line only")
     return ap.parse_args()
 
 
@@ -403,15 +404,20 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
-def side_runs(sw, L, np, torch, hbm):
-    """HBM-bound 2048² runs (state larger than L2) and the Float64 paths."""
+def lattice_2048_run(sw, np, torch, hbm, precs=("f32", "f16", "f64"), geometry=""):
+    """HBM-bound 2048² runs (the state is larger than L2), event-timed on the
+    state's stream; `geometry` "NT,H" overrides the size rule's strips."""
     out = {}
     rng = np.random.default_rng(3)
     n = 2048
     h0 = np.asfortranarray(1.0 + rng.uniform(-0.1, 0.1, (n, n)))
     s2 = sw.SysConst(n, n, sw.Taumucs())
     for prec, T, steps in (("f32", np.float32, 300), ("f16", np.float16, 300), ("f64", np.float64, 30)):
+        if prec not in precs:
+            continue
         st = sw.Sys(s2, "GB300", T=T)
+        if geometry:
+            st.set_geometry(*(int(v) for v in geometry.split(",")))
         stream = torch.cuda.Stream()
         st.set_stream(stream.cuda_stream)
         st.height = h0
@@ -424,8 +430,15 @@ def side_runs(sw, L, np, torch, hbm):
         t = e0.elapsed_time(e1) / 1e3 / steps
         ach = B_ALG[prec] * n * n / t / 1e9
         out.setdefault("lattice_2048", {})[prec] = {
-            "MLUPS": n * n / t / 1e6, "launch_us": t * 1e6, "achieved_GBs": ach, "frac": ach / hbm}
+            "MLUPS": n * n / t / 1e6, "launch_us": t * 1e6, "achieved_GBs": ach, "frac": ach / hbm,
+            "geometry": list(st.geometry())}
         del st
+    return out
+
+
+def side_runs(sw, L, np, torch, hbm):
+    """HBM-bound 2048² runs and the Float64 paths."""
+    out = lattice_2048_run(sw, np, torch, hbm)
     s5 = sw.SysConst(512, 512, sw.Taumucs(g=-0.001, gamma=0.0005))
     h5 = np.asfortranarray(1.0 + np.random.default_rng(2).uniform(-0.01, 0.01, (512, 512)))
     for dev_name, steps in (("GB300", 200), ("GB300-plain", 50)):
@@ -601,6 +614,12 @@ def run_workload(args):
     if args.workload == "spinodal":
         r = spinodal_run(sw, np, L_, steps=args.case_steps if args.case_steps != 12 else 100000)
         print(json.dumps({"workload": "spinodal_2048", **r}), flush=True)
+        return
+    if args.workload == "lattice2048":
+        import torch
+        r = lattice_2048_run(sw, np, torch, peaks()[0], precs=("f32", "f16"),
+                             geometry=args.geometry)
+        print(json.dumps({"workload": "lattice_2048", **r}), flush=True)
         return
     if args.workload == "ensemble":
         r = ensemble_run(sw, np)

@@ -9,6 +9,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -173,6 +174,14 @@ void set_global_error(const char *msg) { g_err = msg; }
 static std::atomic<unsigned long long> g_launches{0};
 void count_launches(unsigned long long n) { g_launches += n; }
 unsigned long long launches_so_far() { return g_launches.load(); }
+
+bool launch_overlap() {
+    static const bool on = [] {
+        const char *v = getenv("SWB_LAUNCH_OVERLAP");
+        return !(v && v[0] == '0');
+    }();
+    return on;
+}
 
 cudaError_t launch_fused_step(int precision, const StepArgs &a, int k, bool steady, cudaStream_t st) {
     count_launches(1);

@@ -154,6 +154,10 @@ inline bool step_general(const StepArgs &a) {
 // Whether the step kernels of a lattice produce per-step partial measures.
 __host__ __device__ inline bool needs_partials(const StepArgs &a) { return a.meas_mask != 0 || a.mass_corr != 0; }
 
+// Launch overlap of consecutive step kernels (programmatic dependent
+// launch): on unless the environment sets SWB_LAUNCH_OVERLAP=0.  Read once.
+bool launch_overlap();
+
 // Error text returned by swb_last_error(NULL) on the calling thread.
 void set_global_error(const char *msg);
 // Counts kernel launches issued by the library (swb_launch_count).

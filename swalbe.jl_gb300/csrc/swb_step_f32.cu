@@ -56,19 +56,20 @@ int grid_for(long long n, int threads) {
 cudaError_t launch_fused_step_f32(int precision, const StepArgs &a, int k, bool steady,
                                   cudaStream_t st) {
     const int grid = step_grid(a, k);
+    cudaError_t e = cudaSuccess;
     if (a.march_nt == kTileGeom) {
-        DISPATCH_STORE(precision, (fused_tile_kernel<S><<<grid, kT2NT, 0, st>>>(a, k)));
+        DISPATCH_STORE(precision, e = launch_step(fused_tile_kernel<S>, grid, kT2NT, st, a, k));
     } else if (step_general(a)) {
-        DISPATCH_STORE(precision, DISPATCH_NT(a.march_nt, (fused_step_kernel<S, NT, true><<<grid, NT, 0, st>>>(a, k))));
+        DISPATCH_STORE(precision, DISPATCH_NT(a.march_nt, e = launch_step(fused_step_kernel<S, NT, true>, grid, NT, st, a, k)));
     } else if (steady && (a.march_nt == 64 || a.march_nt == 128)) {
         if (a.tau_is_one)
-            DISPATCH_STORE(precision, DISPATCH_NT_NARROW(a.march_nt, (fused_step_kernel<S, NT, false, kFormSteadyTau1><<<grid, NT, 0, st>>>(a, k))));
+            DISPATCH_STORE(precision, DISPATCH_NT_NARROW(a.march_nt, e = launch_step(fused_step_kernel<S, NT, false, kFormSteadyTau1>, grid, NT, st, a, k)));
         else
-            DISPATCH_STORE(precision, DISPATCH_NT_NARROW(a.march_nt, (fused_step_kernel<S, NT, false, kFormSteady><<<grid, NT, 0, st>>>(a, k))));
+            DISPATCH_STORE(precision, DISPATCH_NT_NARROW(a.march_nt, e = launch_step(fused_step_kernel<S, NT, false, kFormSteady>, grid, NT, st, a, k)));
     } else {
-        DISPATCH_STORE(precision, DISPATCH_NT(a.march_nt, (fused_step_kernel<S, NT, false><<<grid, NT, 0, st>>>(a, k))));
+        DISPATCH_STORE(precision, DISPATCH_NT(a.march_nt, e = launch_step(fused_step_kernel<S, NT, false>, grid, NT, st, a, k)));
     }
-    return cudaGetLastError();
+    return e;
 }
 
 cudaError_t launch_moments_f32(int precision, const StepArgs &a, cudaStream_t st) {
@@ -100,13 +101,14 @@ cudaError_t launch_pressure_now_f32(int precision, const StepArgs &a, double *ou
 cudaError_t launch_batch_step_f32(int precision, int nt, bool gen, bool steady_tau1,
                                   const StepArgs *d_args, const TileRef *d_tiles, int ntiles,
                                   int grid, int k, cudaStream_t st) {
+    cudaError_t e = cudaSuccess;
     if (gen)
-        DISPATCH_STORE(precision, DISPATCH_NT(nt, (batch_step_kernel<S, NT, true><<<grid, NT, 0, st>>>(d_args, d_tiles, ntiles, k))));
+        DISPATCH_STORE(precision, DISPATCH_NT(nt, e = launch_step(batch_step_kernel<S, NT, true>, grid, NT, st, d_args, d_tiles, ntiles, k)));
     else if (steady_tau1 && nt == kBatchNT)
-        DISPATCH_STORE(precision, (batch_step_kernel<S, kBatchNT, false, kFormSteadyTau1><<<grid, kBatchNT, 0, st>>>(d_args, d_tiles, ntiles, k)));
+        DISPATCH_STORE(precision, e = launch_step(batch_step_kernel<S, kBatchNT, false, kFormSteadyTau1>, grid, kBatchNT, st, d_args, d_tiles, ntiles, k));
     else
-        DISPATCH_STORE(precision, DISPATCH_NT(nt, (batch_step_kernel<S, NT, false><<<grid, NT, 0, st>>>(d_args, d_tiles, ntiles, k))));
-    return cudaGetLastError();
+        DISPATCH_STORE(precision, DISPATCH_NT(nt, e = launch_step(batch_step_kernel<S, NT, false>, grid, NT, st, d_args, d_tiles, ntiles, k)));
+    return e;
 }
 
 // Resident CTAs per SM of the batch kernel most launches use (the steady

@@ -25,23 +25,22 @@ namespace swb {
 
 cudaError_t launch_fused_step_f64(const StepArgs &a, int k, cudaStream_t st) {
     const int grid = step_grid(a, k);
+    cudaError_t e = cudaSuccess;
     if (step_general(a))
-        DISPATCH_NT(a.march_nt, (fused_step_kernel<StoreF64, NT, true><<<grid, NT, 0, st>>>(a, k)));
+        DISPATCH_NT(a.march_nt, e = launch_step(fused_step_kernel<StoreF64, NT, true>, grid, NT, st, a, k));
     else
-        DISPATCH_NT(a.march_nt, (fused_step_kernel<StoreF64, NT, false><<<grid, NT, 0, st>>>(a, k)));
-    return cudaGetLastError();
+        DISPATCH_NT(a.march_nt, e = launch_step(fused_step_kernel<StoreF64, NT, false>, grid, NT, st, a, k));
+    return e;
 }
 
 cudaError_t launch_advance(const StepArgs &a, int n, cudaStream_t st) {
     count_launches(1);
-    advance_kernel<128><<<1, 128, 0, st>>>(a, n);
-    return cudaGetLastError();
+    return launch_step(advance_kernel<128>, 1, 128, st, a, n);
 }
 
 cudaError_t launch_batch_advance(const StepArgs *d_args, int count, int n, cudaStream_t st) {
     count_launches(1);
-    batch_advance_kernel<128><<<count, 128, 0, st>>>(d_args, n);
-    return cudaGetLastError();
+    return launch_step(batch_advance_kernel<128>, count, 128, st, d_args, n);
 }
 
 static int grid_for(long long n, int threads) {
@@ -73,11 +72,12 @@ cudaError_t launch_pressure_now_f64(const StepArgs &a, double *out, cudaStream_t
 
 cudaError_t launch_batch_step_f64(int nt, bool gen, const StepArgs *d_args, const TileRef *d_tiles,
                                   int ntiles, int grid, int k, cudaStream_t st) {
+    cudaError_t e = cudaSuccess;
     if (gen)
-        DISPATCH_NT(nt, (batch_step_kernel<StoreF64, NT, true><<<grid, NT, 0, st>>>(d_args, d_tiles, ntiles, k)));
+        DISPATCH_NT(nt, e = launch_step(batch_step_kernel<StoreF64, NT, true>, grid, NT, st, d_args, d_tiles, ntiles, k));
     else
-        DISPATCH_NT(nt, (batch_step_kernel<StoreF64, NT, false><<<grid, NT, 0, st>>>(d_args, d_tiles, ntiles, k)));
-    return cudaGetLastError();
+        DISPATCH_NT(nt, e = launch_step(batch_step_kernel<StoreF64, NT, false>, grid, NT, st, d_args, d_tiles, ntiles, k));
+    return e;
 }
 
 int batch_blocks_per_sm_f64(int nt) {

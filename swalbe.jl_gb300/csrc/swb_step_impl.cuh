@@ -101,6 +101,40 @@ using StoreF64 = StoreF64T<LdNC>;
 using StoreF32 = StoreF32T<LdNC>;
 using StoreF16 = StoreF16T<LdNC>;
 
+// ------------------------------------------------------------ launch overlap
+// Programmatic dependent launch.  The kernels of a step sequence (step,
+// advance; single lattice and batch) are launched with the programmatic
+// stream-serialization attribute, so that the next launch is scheduled
+// during the tail of the current one instead of after it.  Every such kernel
+// begins with grid_dep_wait(): griddepcontrol.wait returns once the previous
+// grid has completed and its writes are visible, so nothing is read early.
+// A CTA calls grid_dep_launch() when its main work is done (griddepcontrol.
+// launch_dependents; an exiting CTA counts as well): the next grid is
+// scheduled once every CTA of this one got there, so its CTAs do not hold
+// registers and shared memory (and so L1) while this grid's strips run.
+// Launched without the attribute, both are no-ops.
+__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void grid_dep_launch() {
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// Launch of a kernel that begins with grid_dep_wait(), with the
+// programmatic-serialization attribute when launch overlap is on.
+template <class... P, class... A>
+cudaError_t launch_step(void (*kern)(P...), int grid, int block, cudaStream_t st, A &&...args) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = launch_overlap() ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kern, static_cast<A &&>(args)...);
+}
+
 // ------------------------------------------------------------ helpers
 __device__ __forceinline__ int wrapc(int x, int L) {
     while (x < 0) x += L;
@@ -1198,6 +1232,7 @@ __device__ __forceinline__ void march_run(const StepArgs &a, int bx, int by, lon
             }
         }
         }
+    grid_dep_launch();
     any_nan = __syncthreads_or(any_nan);
     if (any_nan && t == 0) a.ctl->nan_flag = 1;
     if (measure) write_partials<NT>(a, part, tt, by * a.tiles_x + bx, sm.red);
@@ -1390,6 +1425,7 @@ __device__ __forceinline__ void tile2d_run(const StepArgs &a, int bx, int by, lo
             }
         }
     }
+    grid_dep_launch();
     any_nan = __syncthreads_or(any_nan);
     if (any_nan && t == 0) a.ctl->nan_flag = 1;
     if (measure) write_partials<kT2NT>(a, part, tt, by * a.tiles_x + bx, sm.red);
@@ -1416,9 +1452,11 @@ __device__ __forceinline__ void tile2d_tile(const StepArgs &a, int bx, int by, l
 template <class S>
 __global__ void __launch_bounds__(kT2NT, 4) fused_tile_kernel(const StepArgs a, int k) {
     __shared__ TileSmem<S> sm;
+    grid_dep_wait();
     int b = blockIdx.x;
     if (needs_partials(a) && k > 0) {
         if (b == 0) {
+            grid_dep_launch();
             reduce_step<kT2NT>(a, a.ctl->step_base + k, sm.redd);
             return;
         }
@@ -1540,9 +1578,11 @@ enum StepForm { kFormAny = 0, kFormSteadyTau1 = 1, kFormSteady = 2 };
 template <class S, int NT, bool GEN, int FORM = kFormAny>
 __global__ void __launch_bounds__(NT) fused_step_kernel(const StepArgs a, int k) {
     __shared__ MarchSmem<S, NT> sm;
+    grid_dep_wait();
     int b = blockIdx.x;
     if (needs_partials(a) && k > 0) {
         if (b == 0) {
+            grid_dep_launch();
             reduce_step<NT>(a, a.ctl->step_base + k, sm.redd);
             return;
         }
@@ -1562,6 +1602,8 @@ __global__ void __launch_bounds__(NT) fused_step_kernel(const StepArgs a, int k)
 template <int NT>
 __global__ void __launch_bounds__(NT) advance_kernel(const StepArgs a, int n) {
     __shared__ RedPart redd[NT / 32];
+    grid_dep_wait();
+    grid_dep_launch();
     const long long s = a.ctl->step_base + n;
     if (needs_partials(a) && n > 0) reduce_step<NT>(a, s, redd);
     __syncthreads();
@@ -1578,7 +1620,9 @@ __global__ void __launch_bounds__(NT) batch_step_kernel(const StepArgs *__restri
                                                         int ntiles, int k) {
     __shared__ MarchSmem<S, NT> sm;
     __shared__ StepArgs sa;
+    grid_dep_wait();
     for (int e = blockIdx.x; e < ntiles; e += gridDim.x) {
+        if (e + (int)gridDim.x >= ntiles) grid_dep_launch();  // this CTA's last entry
         const TileRef tr = tiles[e];
         if (threadIdx.x == 0) sa = args[tr.lattice];
         __syncthreads();
@@ -1599,6 +1643,8 @@ __global__ void __launch_bounds__(NT) batch_advance_kernel(const StepArgs *__res
                                                            int n) {
     __shared__ RedPart redd[NT / 32];
     __shared__ StepArgs sa;
+    grid_dep_wait();
+    grid_dep_launch();
     if (threadIdx.x == 0) sa = args[blockIdx.x];
     __syncthreads();
     const long long s = sa.ctl->step_base + n;
