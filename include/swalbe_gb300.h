@@ -164,7 +164,11 @@ int swb_set_inclination(swb_state *s, double ax, double ay, int loop_time, int64
                         int64_t tstart, int64_t tsmooth);
 
 /* Geometry of the fused step: CTAs of nt threads (64, 128, 256) own strips
- * of nt-4 columns and h rows (2..512) that they march row by row; or, with
+ * of nt-4 columns and h rows (2..512) that they march row by row; with
+ * nt = -32, -64 or -128 (SWB_F32 / SWB_F16, even Lx) CTAs of -nt threads own
+ * strips of 2|nt|-4 columns, two columns per thread with paired (vector)
+ * population loads and stores (the common steady τ = 1 step; other
+ * iterations run as 64-thread strips of the same rows); or, with
  * nt = 32 (SWB_F32 / SWB_F16 only; h is ignored), CTAs of 256 threads own
  * 2D tiles of 32 x 16 cells whose loads are all issued at once.  By default
  * states autotune it on their first swb_step of >= 512 steps (timing a few

@@ -624,13 +624,18 @@ int autotune_geometry(swb_state *s, long long &left) {
     }
     // {nt, h, multi-step}
     const int K = swb::kTileGeom;
-    const int all[][3] = {{64, 2, 0},  {64, 4, 0},  {64, 8, 0},  {64, 16, 0}, {64, 32, 0}, {128, 4, 0},
-                          {128, 16, 0}, {256, 16, 0}, {K, 16, 0},  {64, 8, 1},  {64, 16, 1},
-                          {128, 8, 1},  {K, 16, 1}};
+    const int all[][3] = {{64, 2, 0},   {64, 4, 0},   {64, 8, 0},   {64, 16, 0},  {64, 32, 0},
+                          {128, 4, 0},  {128, 16, 0}, {256, 16, 0}, {K, 16, 0},   {-32, 4, 0},
+                          {-32, 8, 0},  {-64, 4, 0},  {-64, 8, 0},  {-64, 16, 0}, {-64, 32, 0},
+                          {-128, 16, 0}, {64, 8, 1},  {64, 16, 1},  {128, 8, 1},  {K, 16, 1}};
     std::vector<std::array<int, 3>> cands;
     const bool multi_ok = s->precision == SWB_F32 || s->precision == SWB_F16;
+    // pair strips: FP32 arithmetic, even Lx, and only the common steady τ = 1
+    // step has that form (others would time the one-column fallback)
+    const bool pair_ok = multi_ok && s->p.Lx % 2 == 0 && s->a.tau_is_one && !swb::step_general(s->a);
     for (auto &c : all) {
         if (c[0] == K && !multi_ok) continue;
+        if (c[0] < 0 && !pair_ok) continue;
         // the multi-step form only when asked for: it never won on GB300
         // (sweeps at 512^2..2048^2), and a 16-iteration probe can misjudge it
         if (c[2] && (!multi_ok || s->mode != SWB_STEP_MULTI)) continue;
@@ -1108,12 +1113,20 @@ int swb_set_geometry(swb_state *s, int nt, int h) {
         if (s->precision == SWB_F64)
             return fail(&s->err, SWB_ERR_UNSUPPORTED, "2D tiles: FP32 and FP16 storage only");
         h = swb::kTileY;
+    } else if (swb::pair_geometry(nt)) {
+        if (s->precision == SWB_F64)
+            return fail(&s->err, SWB_ERR_UNSUPPORTED, "pair strips: FP32 and FP16 storage only");
+        if (s->p.Lx % 2)
+            return fail(&s->err, SWB_ERR_UNSUPPORTED, "pair strips: Lx must be even");
+        if (h < swb::kMinRows || h > swb::kMaxRows)
+            return fail(&s->err, SWB_ERR_ARG, "geometry: 2 <= h <= 512");
     } else if ((nt != 64 && nt != 128 && nt != 256) || h < swb::kMinRows || h > swb::kMaxRows) {
         return fail(&s->err, SWB_ERR_ARG,
-                    "geometry: nt must be 64, 128 or 256 and 4 <= h <= 512, or nt = 32 (2D tiles)");
+                    "geometry: nt must be 64, 128 or 256 and 2 <= h <= 512, nt = -32, -64 or "
+                    "-128 (pair strips), or nt = 32 (2D tiles)");
     }
-    if (s->mode == SWB_STEP_MULTI && nt == 256)
-        return fail(&s->err, SWB_ERR_UNSUPPORTED, "multi-step kernel: nt must be 64 or 128");
+    if (s->mode == SWB_STEP_MULTI && (nt == 256 || nt < 0))
+        return fail(&s->err, SWB_ERR_UNSUPPORTED, "multi-step kernel: nt must be 64, 128 or 32");
     s->autotune = false;  // an explicit geometry (or the default) is kept
     s->tuned = true;
     if (s->a.march_nt != nt || s->a.march_h != h) {
@@ -1137,7 +1150,7 @@ int swb_set_step_mode(swb_state *s, int mode) {
         return fail(&s->err, SWB_ERR_UNSUPPORTED, "multi-step kernel: FP32 and FP16 storage only");
     CUDA_TRY(&s->err, cudaStreamSynchronize(s->stream));
     s->mode = mode;
-    if (mode == SWB_STEP_MULTI && s->a.march_nt == 256) {
+    if (mode == SWB_STEP_MULTI && (s->a.march_nt == 256 || s->a.march_nt < 0)) {
         int nt = 128, h = 0;
         swb::default_geometry(s->p.Lx, s->p.Ly, s->precision, &nt, &h);
         swb::set_geometry(s->a, nt, h);

@@ -124,6 +124,13 @@ __host__ __device__ inline void substrate_shift(const StepArgs &a, long long t, 
 constexpr int kTileGeom = 32;
 constexpr int kTileX = 32, kTileY = 16, kTileThreads = 256;
 
+// Pair strips (FP32 arithmetic, even Lx): geometry value -NT, CTAs of NT
+// threads (32, 64 or 128) with two columns per thread own strips of
+// 2 NT - 4 columns.  Only the common steady τ = 1 step has this form; the
+// other iterations of such a state run as one-column strips of 64 threads
+// with the same rows (pair_fallback).
+inline bool pair_geometry(int nt) { return nt == -32 || nt == -64 || nt == -128; }
+
 inline void set_geometry(StepArgs &a, int nt, int h) {
     a.march_nt = nt;
     if (nt == kTileGeom) {
@@ -133,11 +140,18 @@ inline void set_geometry(StepArgs &a, int nt, int h) {
         return;
     }
     a.march_h = h;
-    a.tiles_x = (a.Lx + nt - 5) / (nt - 4);
+    const int w = nt < 0 ? -2 * nt - 4 : nt - 4;  // strip width in columns
+    a.tiles_x = (a.Lx + w - 1) / w;
     a.tiles_y = (a.Ly + h - 1) / h;
 }
 // Threads per CTA of a geometry.
-inline int geometry_threads(int nt) { return nt == kTileGeom ? kTileThreads : nt; }
+inline int geometry_threads(int nt) { return nt == kTileGeom ? kTileThreads : (nt < 0 ? -nt : nt); }
+// The one-column strips that run the iterations the pair form leaves out.
+inline StepArgs pair_fallback(const StepArgs &a) {
+    StepArgs b = a;
+    set_geometry(b, 64, a.march_h);
+    return b;
+}
 
 // Entry in the packed tile table of a batch (tx = -1: the lattice's reducer).
 struct TileRef {

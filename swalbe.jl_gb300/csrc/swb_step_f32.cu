@@ -55,6 +55,19 @@ int grid_for(long long n, int threads) {
 
 cudaError_t launch_fused_step_f32(int precision, const StepArgs &a, int k, bool steady,
                                   cudaStream_t st) {
+    if (a.march_nt < 0) {
+        if (!(steady && a.tau_is_one && !step_general(a)))
+            return launch_fused_step_f32(precision, pair_fallback(a), k, steady, st);
+        const int grid = step_grid(a, k);
+        cudaError_t e = cudaSuccess;
+        if (a.march_nt == -32)
+            DISPATCH_STORE(precision, e = launch_step(pair_step_kernel<S, 32>, grid, 32, st, a, k));
+        else if (a.march_nt == -128)
+            DISPATCH_STORE(precision, e = launch_step(pair_step_kernel<S, 128>, grid, 128, st, a, k));
+        else
+            DISPATCH_STORE(precision, e = launch_step(pair_step_kernel<S, 64>, grid, 64, st, a, k));
+        return e;
+    }
     const int grid = step_grid(a, k);
     cudaError_t e = cudaSuccess;
     if (a.march_nt == kTileGeom) {

@@ -881,6 +881,116 @@ __device__ __forceinline__ CellConst<R> cell_consts(const StepArgs &a, long long
     return c;
 }
 
+// slippage! (src/forcing.jl:43-44) and the force sum (src/simulate.jl:18-19)
+// in FP32 arithmetic: (Fx, Fy) = -h ∇p - c u with c = 6 μ h / (2h² + 6δh +
+// 3δ²), both components in one packed pair.
+__device__ __forceinline__ float2 force_fast(const CellConst<float> &cc, float h, float ux,
+                                             float uy, float gpx, float gpy) {
+    const float c = qdiv(cc.mu6 * h, __fmaf_rn(__fmaf_rn(2.0f, h, cc.delta6), h, cc.delta3sq));
+    return fma2(f2(-h, -h), f2(gpx, gpy), mul2(f2(-c, -c), f2(ux, uy)));
+}
+
+// The FP32-arithmetic collision of one cell: its nine post-collision
+// populations fo (for FP16 storage also the stored half bits hb of the pairs
+// (1, 2), (3, 4), (5, 6), (7, 8); fo then holds the values they represent).
+// (Fx, Fy): the force; hft, fq: the pulled mass and populations (τ != 1
+// only); *hlo_p: the rounding residue of the pulled height (not read for a
+// fresh step).  Shared by every FP32-arithmetic kernel, so that they all
+// round identically.
+template <class S, bool FRESH, bool TAU1>
+__device__ __forceinline__ void collide_fast(const CellConst<float> &cc, float h, float ux,
+                                             float uy, float Fx, float Fy, float hft,
+                                             const float *fq, int cell, long long tt,
+                                             const float *hlo_p, float fo[9],
+                                             __half2 hb[4]) {
+    using R = float;
+    // FP32 arithmetic.  f0 closes the mass balance with the values as
+    // stored: f0 = M - Σ_{q>0} f_q, where M (the pulled mass, hi + lo)
+    // is what the cell must hold.  The residue c (e, the exact rounding
+    // error of f0 (Fast2Sum), the lo part of M and the cell's share of
+    // the mass correction) is added to f0 by stochastic rounding, so it
+    // stays in the cell, at rest, in expectation: no bias, whatever the
+    // state.  FP32 populations also keep what that rounding left out:
+    // c - k ulp(f0) is zero-mean and resolved by ulp(f5), so folding it
+    // into f5 and f7 keeps the mass (~1e-12 relative over 100,000
+    // iterations) without a systematic transport.  Folding all of c into
+    // a moving pair instead moves the residue to the neighbours every
+    // iteration, which biases slow dynamics: 2-3e-4 relative L2 in h
+    // against Float64 after 100,000 iterations of a 2048² film h = 1 ± 0.1
+    // (which levels over that time), against 6e-7 this way (measured
+    // on GB300).  FP16
+    // populations cannot hold the left-out part; their mass is kept by
+    // the FP64-measured correction.
+    // Opposite populations (q+, q-) share their equilibrium's even part
+    // A and odd part B (feq = A ± B, src/equilibrium.jl:67-114) and their
+    // force source ±S (src/collide.jl:80-89).
+    const R vsq = __fmaf_rn(ux, ux, uy * uy);
+    const R base = __fmaf_rn(R(1.5) * cc.g, h, R(-1.5) * vsq);
+    const R w1h = h * R(1.0 / 9.0), w5h = h * R(1.0 / 36.0);
+    // the k = (1, 2) and (5, 6) directions as packed pairs: velocities
+    // cu = (ux, uy) and (ux + uy, uy - ux), weights w1 h and w5 h, sources
+    // (Fx, Fy) / 3 and (Fx + Fy, Fy - Fx) / 24
+    const float2 U = f2(ux, uy), F2 = f2(Fx, Fy);
+    const float2 CU[2] = {U, add2(U, f2(uy, -ux))};
+    const float2 SQ[2] = {mul2(f2(1.0f / 3.0f, 1.0f / 3.0f), F2),
+                          mul2(f2(1.0f / 24.0f, 1.0f / 24.0f), add2(F2, f2(Fy, -Fx)))};
+    const R wq[2] = {w1h, w5h};
+    const float2 BASE = f2(base, base);
+    constexpr int qp[2] = {1, 5}, qm[2] = {3, 7};  // and qp + 1, qm + 1
+    // FP16 planes: the stored bits of (f1, f2), (f3, f4), (f5, f6), (f7, f8),
+    // rounded once per pair; fo holds the values they represent
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+        const float2 WQ = f2(wq[j], wq[j]);
+        const float2 A = mul2(WQ, fma2(mul2(f2(4.5f, 4.5f), CU[j]), CU[j], BASE));
+        float2 P, M;
+        if constexpr (TAU1) {
+            const float2 BS = fma2(mul2(f2(3.0f, 3.0f), WQ), CU[j], SQ[j]);
+            P = add2(A, BS);
+            M = sub2(A, BS);
+        } else {
+            const float2 B = mul2(mul2(f2(3.0f, 3.0f), WQ), CU[j]);
+            const float2 OM = f2(cc.omeg, cc.omeg), IT = f2(cc.invtau, cc.invtau);
+            P = add2(fma2(OM, f2(fq[qp[j]], fq[qp[j] + 1]), mul2(IT, add2(A, B))), SQ[j]);
+            M = sub2(fma2(OM, f2(fq[qm[j]], fq[qm[j] + 1]), mul2(IT, sub2(A, B))), SQ[j]);
+        }
+        if constexpr (S::kHalf) {
+            const float2 sc = f2(S::kScale, S::kScale), inv = f2(S::kInv, S::kInv);
+            hb[2 * j] = __float22half2_rn(mul2(P, sc));
+            hb[2 * j + 1] = __float22half2_rn(mul2(M, sc));
+            const float2 rp = mul2(__half22float2(hb[2 * j]), inv);
+            const float2 rm = mul2(__half22float2(hb[2 * j + 1]), inv);
+            fo[qp[j]] = rp.x;
+            fo[qp[j] + 1] = rp.y;
+            fo[qm[j]] = rm.x;
+            fo[qm[j] + 1] = rm.y;
+        } else {
+            fo[qp[j]] = P.x;
+            fo[qp[j] + 1] = P.y;
+            fo[qm[j]] = M.x;
+            fo[qm[j] + 1] = M.y;
+        }
+    }
+    R hlo = R(0);
+    if constexpr (!FRESH) hlo = *hlo_p;
+    // Σ_q fpost_q = (1-1/τ) Σ ft + Σ feq/τ = h once h is the pulled mass
+    const R mc = (TAU1 || !FRESH) ? h : cc.omeg * hft + cc.invtau * h;
+    const R ssum = small8(fo);
+    const R f0 = mc - ssum;
+    const R e = (mc - f0) - ssum;
+    const R c = e + hlo + R(cc.corr);
+    fo[0] = add_stochastic((float)f0, (float)c, mix32((unsigned)cell, (unsigned)tt));
+    if constexpr (!S::kHalf) {
+        // What the rounding left out, c - k ulp(f0): zero-mean whatever
+        // the state, at most ~ulp(f0), and on a grid that ulp(f5) = ulp(f0)/16
+        // resolves, so folding it into the diagonal pair keeps the mass
+        // (momentum unchanged) without a systematic transport.
+        const R d = R(0.5) * (c - (fo[0] - f0));
+        fo[5] = fo[5] + d;
+        fo[7] = fo[7] + d;
+    }
+}
+
 // Forces, equilibrium and collision of one cell and the store of its nine
 // post-collision populations: slippage! (src/forcing.jl:43-44), the force sum
 // (src/simulate.jl:18-19), inclination! (src/forcing.jl:364-365),
@@ -922,9 +1032,7 @@ __device__ __forceinline__ void collide_cell(const StepArgs &a,
             Fy = Fy + (h * R(a.ay)) * cc.incl_fac;
         }
     } else {
-        const R c = qdiv(cc.mu6 * h, __fmaf_rn(__fmaf_rn(R(2), h, cc.delta6), h, cc.delta3sq));
-        // (Fx, Fy) = -h ∇p - c u, both components in one packed pair
-        const float2 F = fma2(f2(-h, -h), f2(gpx, gpy), mul2(f2(-c, -c), f2(ux, uy)));
+        const float2 F = force_fast(cc, h, ux, uy, gpx, gpy);
         Fx = F.x;
         Fy = F.y;
         if (GEN && a.thermal) {
@@ -960,93 +1068,9 @@ __device__ __forceinline__ void collide_cell(const StepArgs &a,
             S::st(dst, pitch, q, cell, v);
         }
     } else {
-        // FP32 arithmetic.  f0 closes the mass balance with the values as
-        // stored: f0 = M - Σ_{q>0} f_q, where M (the pulled mass, hi + lo)
-        // is what the cell must hold.  The residue c (e, the exact rounding
-        // error of f0 (Fast2Sum), the lo part of M and the cell's share of
-        // the mass correction) is added to f0 by stochastic rounding, so it
-        // stays in the cell, at rest, in expectation: no bias, whatever the
-        // state.  FP32 populations also keep what that rounding left out:
-        // c - k ulp(f0) is zero-mean and resolved by ulp(f5), so folding it
-        // into f5 and f7 keeps the mass (~1e-12 relative over 100,000
-        // iterations) without a systematic transport.  Folding all of c into
-        // a moving pair instead moves the residue to the neighbours every
-        // iteration, which biases slow dynamics: 2-3e-4 relative L2 in h
-        // against Float64 after 100,000 iterations of a 2048² film h = 1 ± 0.1
-        // (which levels over that time), against 6e-7 this way (measured
-        // on GB300).  FP16
-        // populations cannot hold the left-out part; their mass is kept by
-        // the FP64-measured correction.
-        // Opposite populations (q+, q-) share their equilibrium's even part
-        // A and odd part B (feq = A ± B, src/equilibrium.jl:67-114) and their
-        // force source ±S (src/collide.jl:80-89).
-        R fo[9];
-        const R vsq = __fmaf_rn(ux, ux, uy * uy);
-        const R base = __fmaf_rn(R(1.5) * cc.g, h, R(-1.5) * vsq);
-        const R w1h = h * R(1.0 / 9.0), w5h = h * R(1.0 / 36.0);
-        // the k = (1, 2) and (5, 6) directions as packed pairs: velocities
-        // cu = (ux, uy) and (ux + uy, uy - ux), weights w1 h and w5 h, sources
-        // (Fx, Fy) / 3 and (Fx + Fy, Fy - Fx) / 24
-        const float2 U = f2(ux, uy), F2 = f2(Fx, Fy);
-        const float2 CU[2] = {U, add2(U, f2(uy, -ux))};
-        const float2 SQ[2] = {mul2(f2(1.0f / 3.0f, 1.0f / 3.0f), F2),
-                              mul2(f2(1.0f / 24.0f, 1.0f / 24.0f), add2(F2, f2(Fy, -Fx)))};
-        const R wq[2] = {w1h, w5h};
-        const float2 BASE = f2(base, base);
-        constexpr int qp[2] = {1, 5}, qm[2] = {3, 7};  // and qp + 1, qm + 1
-        // FP16 planes: the stored bits of (f1, f2), (f3, f4), (f5, f6), (f7, f8),
-        // rounded once per pair; fo holds the values they represent
+        float fo[9];
         [[maybe_unused]] __half2 hb[4];
-#pragma unroll
-        for (int j = 0; j < 2; ++j) {
-            const float2 WQ = f2(wq[j], wq[j]);
-            const float2 A = mul2(WQ, fma2(mul2(f2(4.5f, 4.5f), CU[j]), CU[j], BASE));
-            float2 P, M;
-            if constexpr (TAU1) {
-                const float2 BS = fma2(mul2(f2(3.0f, 3.0f), WQ), CU[j], SQ[j]);
-                P = add2(A, BS);
-                M = sub2(A, BS);
-            } else {
-                const float2 B = mul2(mul2(f2(3.0f, 3.0f), WQ), CU[j]);
-                const float2 OM = f2(cc.omeg, cc.omeg), IT = f2(cc.invtau, cc.invtau);
-                P = add2(fma2(OM, f2(fq[qp[j]], fq[qp[j] + 1]), mul2(IT, add2(A, B))), SQ[j]);
-                M = sub2(fma2(OM, f2(fq[qm[j]], fq[qm[j] + 1]), mul2(IT, sub2(A, B))), SQ[j]);
-            }
-            if constexpr (S::kHalf) {
-                const float2 sc = f2(S::kScale, S::kScale), inv = f2(S::kInv, S::kInv);
-                hb[2 * j] = __float22half2_rn(mul2(P, sc));
-                hb[2 * j + 1] = __float22half2_rn(mul2(M, sc));
-                const float2 rp = mul2(__half22float2(hb[2 * j]), inv);
-                const float2 rm = mul2(__half22float2(hb[2 * j + 1]), inv);
-                fo[qp[j]] = rp.x;
-                fo[qp[j] + 1] = rp.y;
-                fo[qm[j]] = rm.x;
-                fo[qm[j] + 1] = rm.y;
-            } else {
-                fo[qp[j]] = P.x;
-                fo[qp[j] + 1] = P.y;
-                fo[qm[j]] = M.x;
-                fo[qm[j] + 1] = M.y;
-            }
-        }
-        R hlo = R(0);
-        if constexpr (!FRESH) hlo = *hlo_p;
-        // Σ_q fpost_q = (1-1/τ) Σ ft + Σ feq/τ = h once h is the pulled mass
-        const R mc = (TAU1 || !FRESH) ? h : cc.omeg * hft + cc.invtau * h;
-        const R ssum = small8(fo);
-        const R f0 = mc - ssum;
-        const R e = (mc - f0) - ssum;
-        const R c = e + hlo + R(cc.corr);
-        fo[0] = add_stochastic((float)f0, (float)c, mix32((unsigned)cell, (unsigned)tt));
-        if constexpr (!S::kHalf) {
-            // What the rounding left out, c - k ulp(f0): zero-mean whatever
-            // the state, at most ~ulp(f0), and on a grid that ulp(f5) = ulp(f0)/16
-            // resolves, so folding it into the diagonal pair keeps the mass
-            // (momentum unchanged) without a systematic transport.
-            const R d = R(0.5) * (c - (fo[0] - f0));
-            fo[5] = fo[5] + d;
-            fo[7] = fo[7] + d;
-        }
+        collide_fast<S, FRESH, TAU1>(cc, h, ux, uy, Fx, Fy, hft, fq, cell, tt, hlo_p, fo, hb);
         if constexpr (S::kHalf) {
             reinterpret_cast<float *>(dst)[cell] = fo[0];
             __half *hpl = const_cast<__half *>(S::hp(dst, pitch)) + cell;
@@ -1258,6 +1282,325 @@ __device__ __forceinline__ void march_tile(const StepArgs &a, int bx, int by, lo
         else
             march_run<S, NT, false, false, GEN>(a, bx, by, done, sm);
     }
+}
+
+// ------------------------------------------------------------ pair strips
+// The common steady step (FP32 arithmetic, τ = 1, scalar θ, no rare forces)
+// with two adjacent columns per thread.  A CTA of NT threads owns a strip of
+// W = 2 NT - 4 columns and H rows; thread t owns columns c = x0 - 2 + 2t and
+// c + 1 for the whole strip.  Lx is even, so c is even: the pair never
+// straddles the periodic boundary, and every plane's pair is one aligned
+// access, 8 bytes for FP32 populations (and f0 of FP16 storage), 4 bytes for
+// FP16 planes.  A row of pulls is nine such loads per thread: the planes
+// pulled across x (f1, f5, f8 from x - 1; f3, f6, f7 from x + 1) take the
+// neighbouring lane's half of its pair by a warp shuffle, and lanes 0 and 31
+// load the one value from outside their warp directly.  The stores are nine
+// pair stores.  Shared-memory rings hold pairs, so a pressure or gradient
+// stencil of two cells is three pair reads and six scalar reads, and the
+// row's index and address arithmetic is paid once per two cells.  The
+// per-cell arithmetic is march_run's (moments9, pressure_cell, grad9,
+// force_fast, collide_fast): results are bit-identical to the one-column
+// strips.
+template <int NT>
+struct PairSmem {
+    float2 h[8][NT];  // heights of the pairs, ring of 5 live rows
+    float2 p[4][NT];  // film pressure
+    float2 jx[4][NT];
+    float2 jy[4][NT];
+    float2 lo[4][NT];  // rounding residue of the pulled height
+    PartQ red[NT / 32];
+    RedPart redd[NT / 32];
+};
+
+// One row of pulls of a pair, as loaded: f0 and the planes 1..8 at the
+// pair's own two columns (FP32 pairs or FP16 pairs), and in lanes 0 / 31 the
+// three values from outside the warp (planes 1, 5, 8 at c - 1 / planes 3, 6,
+// 7 at c + 2).
+template <class S>
+struct PairPull {
+    using W = typename std::conditional<S::kHalf, __half2, float2>::type;
+    using E = typename std::conditional<S::kHalf, __half, float>::type;
+    float2 f0;
+    W q[8];
+    E e[3];
+};
+
+template <class S>
+__device__ __forceinline__ float2 pair_f0(const void *b, int i) {
+    return __ldg(reinterpret_cast<const float2 *>(reinterpret_cast<const float *>(b) + i));
+}
+
+// plane q (1..8) at element i (even): the pair as stored
+template <class S>
+__device__ __forceinline__ typename PairPull<S>::W pair_ld(const void *b, int pitch, int q, int i) {
+    if constexpr (S::kHalf)
+        return __ldg(reinterpret_cast<const __half2 *>(S::hp(b, pitch) + (q - 1) * pitch + i));
+    else
+        return __ldg(reinterpret_cast<const float2 *>(reinterpret_cast<const float *>(b) + q * pitch + i));
+}
+
+template <class S>
+__device__ __forceinline__ typename PairPull<S>::E one_ld(const void *b, int pitch, int q, int i) {
+    if constexpr (S::kHalf)
+        return __ldg(S::hp(b, pitch) + (q - 1) * pitch + i);
+    else
+        return __ldg(reinterpret_cast<const float *>(b) + q * pitch + i);
+}
+
+// The pulled values of a plane at the pair, (f_q(c), f_q(c + 1)), from the
+// pair as stored (planes not pulled across x), or from the value at c - 1
+// and the stored pair (planes pulled from x - 1), or from the stored pair
+// and the value at c + 2 (planes pulled from x + 1).  FP16 values are
+// widened and unscaled exactly as StoreF16T::ld does, one value at a time.
+__device__ __forceinline__ float2 pair_val(float2 w) { return w; }
+__device__ __forceinline__ float2 pair_val(__half2 w) {
+    return mul2(__half22float2(w), f2(StoreF16::kInv, StoreF16::kInv));
+}
+__device__ __forceinline__ float2 left_pull(float left, float2 own) { return f2(left, own.x); }
+__device__ __forceinline__ float2 right_pull(float2 own, float right) { return f2(own.y, right); }
+__device__ __forceinline__ float2 left_pull(__half left, __half2 own) {
+    return pair_val(__halves2half2(left, __low2half(own)));
+}
+__device__ __forceinline__ float2 right_pull(__half2 own, __half right) {
+    return pair_val(__halves2half2(__high2half(own), right));
+}
+// the upper value of the lane below's pair / the lower value of the lane above's
+__device__ __forceinline__ float shfl_hi_up(float2 w) { return __shfl_up_sync(0xffffffffu, w.y, 1); }
+__device__ __forceinline__ float shfl_lo_down(float2 w) { return __shfl_down_sync(0xffffffffu, w.x, 1); }
+__device__ __forceinline__ __half shfl_hi_up(__half2 w) {
+    return __high2half(__shfl_up_sync(0xffffffffu, w, 1));
+}
+__device__ __forceinline__ __half shfl_lo_down(__half2 w) {
+    return __low2half(__shfl_down_sync(0xffffffffu, w, 1));
+}
+
+template <class S, int NT>
+__device__ __forceinline__ void march2_run(const StepArgs &a, int bx, int by, long long done,
+                                           PairSmem<NT> &sm) {
+    static_assert(!S::kLiteral && NT % 32 == 0, "pair strips: FP32 arithmetic, whole warps");
+    using R = float;
+    using PP = PairPull<S>;
+    constexpr int W = 2 * NT - 4;
+    const int t = threadIdx.x, lane = t & 31;
+    const int Lx = a.Lx, Ly = a.Ly;
+    const int H = a.march_h;
+    const int pitch = (int)a.pitch;  // 9 * pitch < 2^31 (checked at creation)
+    const long long tt = done + 1;
+    const void *src = (done & 1) ? a.fb : a.fa;
+    void *dst = (done & 1) ? a.fa : a.fb;
+    const int x0 = bx * W, y0 = by * H;
+    const int rows = min(H, Ly - y0);
+    const R gamma = R(a.gamma), hmin = R(a.hmin), hcrit = R(a.hcrit), kap = R(a.kap);
+    const bool tiny_y = Ly < 3;
+    auto wrow = [&](int yy) {
+        return tiny_y ? wrapc(yy, Ly) : (yy < 0 ? yy + Ly : (yy >= Ly ? yy - Ly : yy));
+    };
+    // this thread's pair (c, c + 1); x0 and Lx are even
+    const int cx = wrapc(x0 - 2 + 2 * t, Lx);
+    const bool interior = t >= 1 && t < NT - 1 && x0 - 2 + 2 * t < Lx;
+    // lanes 0 / 31: the column and planes of the values from outside the warp
+    const bool edge = lane == 0 || lane == 31;
+    const int ecol = lane == 0 ? (cx == 0 ? Lx - 1 : cx - 1) : (cx + 2 >= Lx ? cx + 2 - Lx : cx + 2);
+    const int eq0 = lane == 0 ? 1 : 3, eq1 = lane == 0 ? 5 : 6, eq2 = lane == 0 ? 8 : 7;
+    // neighbours of the pair in a ring row of pairs, read as floats (clamped
+    // at the CTA's ends, whose values are not used)
+    const int tl = t > 0 ? 2 * t - 1 : 0, tr = t < NT - 1 ? 2 * t + 2 : 2 * NT - 1;
+
+    PP fa_, fb_;
+    auto issue = [&](PP &P, int yy) {
+        const int gy = wrow(yy);
+        const int gym = gy == 0 ? Ly - 1 : gy - 1, gyp = gy == Ly - 1 ? 0 : gy + 1;
+        const int rc = gy * Lx, rm = gym * Lx, rp = gyp * Lx;
+        P.f0 = pair_f0<S>(src, rc + cx);
+        P.q[0] = pair_ld<S>(src, pitch, 1, rc + cx);  // f1 from x - 1
+        P.q[1] = pair_ld<S>(src, pitch, 2, rm + cx);  // f2 from y - 1
+        P.q[2] = pair_ld<S>(src, pitch, 3, rc + cx);  // f3 from x + 1
+        P.q[3] = pair_ld<S>(src, pitch, 4, rp + cx);  // f4 from y + 1
+        P.q[4] = pair_ld<S>(src, pitch, 5, rm + cx);  // f5 from (x - 1, y - 1)
+        P.q[5] = pair_ld<S>(src, pitch, 6, rm + cx);  // f6 from (x + 1, y - 1)
+        P.q[6] = pair_ld<S>(src, pitch, 7, rp + cx);  // f7 from (x + 1, y + 1)
+        P.q[7] = pair_ld<S>(src, pitch, 8, rp + cx);  // f8 from (x - 1, y + 1)
+        if (edge) {
+            P.e[0] = one_ld<S>(src, pitch, eq0, rc + ecol);
+            P.e[1] = one_ld<S>(src, pitch, eq1, rm + ecol);
+            P.e[2] = one_ld<S>(src, pitch, eq2, rp + ecol);
+        }
+    };
+    auto consume = [&](const PP &P, int yy) {
+        const int r = yy - y0 + 2;  // >= 0
+        // the halves of the x-pulled planes that come from the neighbouring pairs
+        auto l1 = shfl_hi_up(P.q[0]), l5 = shfl_hi_up(P.q[4]), l8 = shfl_hi_up(P.q[7]);
+        auto r3 = shfl_lo_down(P.q[2]), r6 = shfl_lo_down(P.q[5]), r7 = shfl_lo_down(P.q[6]);
+        if (lane == 0) {
+            l1 = P.e[0];
+            l5 = P.e[1];
+            l8 = P.e[2];
+        }
+        if (lane == 31) {
+            r3 = P.e[0];
+            r6 = P.e[1];
+            r7 = P.e[2];
+        }
+        float2 F[9];
+        F[0] = P.f0;
+        F[1] = left_pull(l1, P.q[0]);
+        F[2] = pair_val(P.q[1]);
+        F[3] = right_pull(P.q[2], r3);
+        F[4] = pair_val(P.q[3]);
+        F[5] = left_pull(l5, P.q[4]);
+        F[6] = right_pull(P.q[5], r6);
+        F[7] = right_pull(P.q[6], r7);
+        F[8] = left_pull(l8, P.q[7]);
+        R fA[9], fB[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            fA[q] = F[q].x;
+            fB[q] = F[q].y;
+        }
+        R hA, jxA, jyA, hB, jxB, jyB;
+        moments9<false>(fA, hA, jxA, jyA);
+        moments9<false>(fB, hB, jxB, jyB);
+        sm.h[r & 7][t] = f2(hA, hB);
+        sm.jx[r & 3][t] = f2(jxA, jxB);
+        sm.jy[r & 3][t] = f2(jyA, jyB);
+        sm.lo[r & 3][t] = f2(moments_lo(fA, hA), moments_lo(fB, hB));
+    };
+    auto pressure_row = [&](int yy) {
+        const int r = yy - y0 + 2;  // >= 1
+        const float2 *hm = sm.h[(r + 7) & 7], *hc = sm.h[r & 7], *hp = sm.h[(r + 1) & 7];
+        const float2 m = hm[t], c = hc[t], pl = hp[t];
+        const float *m1 = reinterpret_cast<const float *>(hm), *c1 = reinterpret_cast<const float *>(hc),
+                    *p1 = reinterpret_cast<const float *>(hp);
+        // ip = h[i-1,j], jp = h[i,j-1], im = h[i+1,j], jm = h[i,j+1], ...
+        const R pA = pressure_cell<false, R>(c.x, c1[tl], m.x, c.y, pl.x, m1[tl], m.y, pl.y, p1[tl],
+                                             kap, gamma, hmin, hcrit, a.n, a.m);
+        const R pB = pressure_cell<false, R>(c.y, c.x, m.y, c1[tr], pl.y, m.x, m1[tr], p1[tr], pl.x,
+                                             kap, gamma, hmin, hcrit, a.n, a.m);
+        sm.p[r & 3][t] = f2(pA, pB);
+    };
+
+    issue(fa_, y0 - 2);
+    issue(fb_, y0 - 1);
+    consume(fa_, y0 - 2);
+    issue(fa_, y0);
+    consume(fb_, y0 - 1);
+    issue(fb_, y0 + 1);
+    consume(fa_, y0);
+    issue(fa_, y0 + 2);
+    consume(fb_, y0 + 1);
+    __syncthreads();
+    pressure_row(y0 - 1);
+    pressure_row(y0);
+
+    const CellConst<R> cc = cell_consts<R>(a, tt, a.mass_corr ? __ldcg(&a.ctl->corr[tt & 1]) : 0.0);
+    const R thr = R(a.hthresh);
+    const bool measure = a.meas_mask || a.mass_corr;
+    PartQ part;
+    part_init(part);
+    int any_nan = 0;
+
+#pragma unroll 1
+    for (int j = 0; j < rows; ++j) {
+        const int y = y0 + j;
+        consume(fa_, y + 2);
+        if (j + 1 < rows) issue(fa_, y + 3);  // one row ahead
+        __syncthreads();
+        pressure_row(y + 1);
+        __syncthreads();
+        if (!interior) continue;
+        // ---- output row y, columns cx, cx + 1 ----
+        const int r = y - y0 + 2;
+        const int cellA = wrow(y) * Lx + cx;
+        const float2 h2 = sm.h[r & 7][t], jx2 = sm.jx[r & 3][t], jy2 = sm.jy[r & 3][t];
+        const float2 lo2 = sm.lo[r & 3][t];
+        const float2 *pm = sm.p[(r + 3) & 3], *pc = sm.p[r & 3], *pp = sm.p[(r + 1) & 3];
+        const float2 m = pm[t], c = pc[t], pl = pp[t];
+        const float *m1 = reinterpret_cast<const float *>(pm), *c1 = reinterpret_cast<const float *>(pc),
+                    *p1 = reinterpret_cast<const float *>(pp);
+        float foA[9], foB[9];
+        [[maybe_unused]] __half2 hbA[4], hbB[4];
+        {
+            R ux, uy, gpx, gpy;
+            velocity<false>(h2.x, jx2.x, jy2.x, ux, uy);
+            grad9<R>(c1[tl], m.x, c.y, pl.x, m1[tl], m.y, pl.y, p1[tl], gpx, gpy);  // h∇p!
+            const float2 F = force_fast(cc, h2.x, ux, uy, gpx, gpy);
+            collide_fast<S, false, true>(cc, h2.x, ux, uy, F.x, F.y, h2.x, nullptr, cellA, tt,
+                                         &lo2.x, foA, hbA);
+        }
+        {
+            R ux, uy, gpx, gpy;
+            velocity<false>(h2.y, jx2.y, jy2.y, ux, uy);
+            grad9<R>(c.x, m.y, c1[tr], pl.y, m.x, m1[tr], p1[tr], pl.x, gpx, gpy);
+            const float2 F = force_fast(cc, h2.y, ux, uy, gpx, gpy);
+            collide_fast<S, false, true>(cc, h2.y, ux, uy, F.x, F.y, h2.y, nullptr, cellA + 1, tt,
+                                         &lo2.y, foB, hbB);
+        }
+        reinterpret_cast<float2 *>(reinterpret_cast<float *>(dst) + cellA)[0] = f2(foA[0], foB[0]);
+        if constexpr (S::kHalf) {
+            __half2 *hpl = reinterpret_cast<__half2 *>(const_cast<__half *>(S::hp(dst, pitch)) + cellA);
+            const int pitch2 = pitch >> 1;  // pitch in pairs (pitch is a multiple of 64)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                hpl[(2 * k) * pitch2] = __lows2half2(hbA[k], hbB[k]);
+                hpl[(2 * k + 1) * pitch2] = __highs2half2(hbA[k], hbB[k]);
+            }
+        } else {
+            float2 *d2 = reinterpret_cast<float2 *>(reinterpret_cast<float *>(dst) + cellA);
+            const int pitch2 = pitch >> 1;
+#pragma unroll
+            for (int q = 1; q < 9; ++q) d2[q * pitch2] = f2(foA[q], foB[q]);
+        }
+        // measures of the heights at the start of this iteration
+        if (!isfinite(h2.x) || !isfinite(h2.y)) any_nan = 1;
+        if (measure) {
+            mass_add(part, h2.x);
+            mass_add(part, h2.y);
+            mass_add_lo(part, lo2.x);
+            mass_add_lo(part, lo2.y);
+            const bool wA = h2.x > thr, wB = h2.y > thr;
+            part.wet += (wA ? 1 : 0) + (wB ? 1 : 0);
+            part.hmax = fmaxf(part.hmax, fmaxf(h2.x, h2.y));
+            part.hmin = fminf(part.hmin, fminf(h2.x, h2.y));
+            if ((a.meas_mask & SWB_MEAS_AREA) && (wA || wB)) {
+                const float2 *hm = sm.h[(r + 7) & 7], *hc = sm.h[r & 7], *hp = sm.h[(r + 1) & 7];
+                const float2 hm2 = hm[t], hp2 = hp[t];
+                const float *hm1 = reinterpret_cast<const float *>(hm),
+                            *hc1 = reinterpret_cast<const float *>(hc),
+                            *hp1 = reinterpret_cast<const float *>(hp);
+                R gx2, gy2;
+                if (wA) {
+                    grad9<R>(hc1[tl], hm2.x, h2.y, hp2.x, hm1[tl], hm2.y, hp2.y, hp1[tl], gx2, gy2);
+                    area_add(part, R(sqrt(gx2 * gx2 + gy2 * gy2 + R(1))));
+                }
+                if (wB) {
+                    grad9<R>(h2.x, hm2.y, hc1[tr], hp2.y, hm2.x, hm1[tr], hp1[tr], hp2.x, gx2, gy2);
+                    area_add(part, R(sqrt(gx2 * gx2 + gy2 * gy2 + R(1))));
+                }
+            }
+        }
+    }
+    grid_dep_launch();
+    any_nan = __syncthreads_or(any_nan);
+    if (any_nan && t == 0) a.ctl->nan_flag = 1;
+    if (measure) write_partials<NT>(a, part, tt, by * a.tiles_x + bx, sm.red);
+}
+
+// One iteration of the common steady step on pair strips, plus (when
+// measures are kept and k > 0) the reducer CTA, block 0.
+template <class S, int NT>
+__global__ void __launch_bounds__(NT) pair_step_kernel(const StepArgs a, int k) {
+    __shared__ __align__(16) PairSmem<NT> sm;
+    grid_dep_wait();
+    int b = blockIdx.x;
+    if (needs_partials(a) && k > 0) {
+        if (b == 0) {
+            grid_dep_launch();
+            reduce_step<NT>(a, a.ctl->step_base + k, sm.redd);
+            return;
+        }
+        b -= 1;
+    }
+    march2_run<S, NT>(a, b % a.tiles_x, b / a.tiles_x, a.ctl->step_base + k, sm);
 }
 
 // ------------------------------------------------------------ 2D tiles

@@ -215,6 +215,7 @@ def test_geometry_does_not_change_results(T):
     geos = [(64, 2), (64, 4), (128, 16), (256, 64), (128, 512)]
     if T != np.float64:
         geos.append((32, 16))  # 2D tiles (FP32 arithmetic only)
+        geos.append((-64, 8))  # pair strips; at τ = 0.9 their one-column fallback runs
     for nt, hh in geos:
         st = sw.Sys(s, "GB300", T=T)
         st.set_geometry(nt, hh)
@@ -226,6 +227,61 @@ def test_geometry_does_not_change_results(T):
     if T == np.float64:
         ref = oracle.time_loop_literal(oparams(s), h0, steps)
         assert np.array_equal(out[0], ref.height)
+
+
+def _run_geo(s, h0, steps, T, geo, theta_wave=None):
+    st = sw.Sys(s, "GB300", T=T)
+    st.set_geometry(*geo)
+    st.set_measures(L.MEAS_ALL)
+    if theta_wave:
+        st.set_theta_wave(*theta_wave)
+    st.height = h0
+    st.step(steps // 3)
+    st.step(steps - steps // 3)
+    st.sync()
+    return st.height, st.measures_array(cap=steps)
+
+
+@pytest.mark.parametrize("T", [np.float32, np.float16])
+def test_pair_strips_equal_one_column_strips(T):
+    """Pair strips (two columns per thread, paired loads and stores, warp
+    shuffles across x) give the bits of one-column strips: heights and every
+    per-step measure, on full, ragged, tiny and multi-strip lattices."""
+    cases = [(150, 97, droplet(150, 97, 30)), (64, 48, rough(64, 48, 3)),
+             (2, 24, rough(2, 24, 2)), (246, 130, droplet(246, 130, 40)),
+             (128, 3, rough(128, 3, 5)), (520, 40, rough(520, 40, 8))]
+    steps = 150
+    for Lx, Ly, h0 in cases:
+        s = sysc(Lx, Ly, delta=2.0)
+        h_ref, r_ref = _run_geo(s, h0, steps, T, (64, 8))
+        for geo in ((-32, 4), (-64, 2), (-64, 16), (-128, 64)):
+            h, r = _run_geo(s, h0, steps, T, geo)
+            assert np.array_equal(h, h_ref), (Lx, Ly, geo)
+            for f in ("t", "mass", "wetted", "hmax", "hmin", "area", "energy"):
+                assert np.array_equal(r[f], r_ref[f]), (Lx, Ly, geo, f)
+
+
+@pytest.mark.parametrize("T", [np.float32, np.float16])
+def test_pair_geometry_fallback_forms(T):
+    """A pair-strip state whose iterations need another form (τ != 1, a θ
+    wave) runs them as one-column strips of the same rows: same results."""
+    Lx, Ly = 96, 64
+    h0 = droplet(Lx, Ly, 20)
+    for kw, wave in (({"tau": 0.8}, None), ({}, (1 / 9, 1 / 36, 1 / 98))):
+        s = sysc(Lx, Ly, **kw)
+        h_ref, r_ref = _run_geo(s, h0, 120, T, (64, 16), theta_wave=wave)
+        h, r = _run_geo(s, h0, 120, T, (-64, 16), theta_wave=wave)
+        assert np.array_equal(h, h_ref)
+        assert np.array_equal(r["mass"], r_ref["mass"]) and np.array_equal(r["area"], r_ref["area"])
+
+
+def test_pair_geometry_rules():
+    st = sw.Sys(sysc(33, 16), "GB300", T=np.float32)
+    with pytest.raises(sw.SwbError):
+        st.set_geometry(-64, 8)  # odd Lx
+    st64 = sw.Sys(sysc(32, 16), "GB300", T=np.float64)
+    with pytest.raises(sw.SwbError):
+        st64.set_geometry(-64, 8)  # Float64
 
 
 # ------------------------------------------------------------------ FP32 / FP16
