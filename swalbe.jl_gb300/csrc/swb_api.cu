@@ -226,10 +226,40 @@ int batch_blocks_per_sm(int precision, int nt) {
 // (FP16: at most 16 rows); FP16 small lattices prefer 128-thread strips.
 // E.g. FP32 2048^2: 60x32 strips, 61.9 us per iteration against 64.0 at
 // 60x16; 1024^2: 60x16.  (*nt == kTileGeom keeps the 2D tiles.)
+int pair_rows(int Lx, int Ly, int precision, int nt) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1)
+        sms = 1;
+    const long long slots = (long long)pair_blocks_per_sm(precision, nt) * sms;
+    const long long w = -2LL * nt - 4, tx = (Lx + w - 1) / w;
+    long long best = -1;
+    int bh = 8;
+    for (int hh = 8; hh <= kMaxRows; ++hh) {
+        const long long ctas = tx * ((Ly + hh - 1) / hh);
+        const long long cost = (ctas + slots - 1) / slots * (hh + 4);
+        if (best < 0 || cost < best) {
+            best = cost;
+            bh = hh;
+        }
+    }
+    return bh < Ly ? bh : (Ly < kMinRows ? kMinRows : Ly);
+}
+
 void default_geometry(int Lx, int Ly, int precision, int *nt, int *h) {
     int n = *nt;
     if (n == kTileGeom) {
         *h = kTileY;
+        return;
+    }
+    // Lattices whose populations exceed L2 (the HBM-bound ones) in FP32
+    // arithmetic: pair strips of 64 threads, rows by the wave rule (FP32
+    // 2048²: 124 x 24 strips, 53.5 us per iteration against 59.7 for 60 x 32
+    // one-column strips, measured on GB300).
+    if ((n == 0 || n < 0) && (precision == SWB_F32 || precision == SWB_F16) && Lx % 2 == 0 &&
+        (long long)Lx * Ly >= (1LL << 21)) {
+        *nt = n < 0 ? n : -64;
+        *h = pair_rows(Lx, Ly, precision, *nt);
         return;
     }
     if (!n) n = (precision == SWB_F16 && (long long)Lx * Ly <= 512LL * 512) ? 128 : 64;
@@ -633,7 +663,12 @@ int autotune_geometry(swb_state *s, long long &left) {
     // pair strips: FP32 arithmetic, even Lx, and only the common steady τ = 1
     // step has that form (others would time the one-column fallback)
     const bool pair_ok = multi_ok && s->p.Lx % 2 == 0 && s->a.tau_is_one && !swb::step_general(s->a);
-    for (auto &c : all) {
+    std::vector<std::array<int, 3>> todo;
+    for (auto &c : all) todo.push_back({c[0], c[1], c[2]});
+    if (pair_ok && s->mode != SWB_STEP_MULTI) {  // and the wave rule's rows
+        for (int pn : {-64, -32}) todo.push_back({pn, swb::pair_rows(s->p.Lx, s->p.Ly, s->precision, pn), 0});
+    }
+    for (auto &c : todo) {
         if (c[0] == K && !multi_ok) continue;
         if (c[0] < 0 && !pair_ok) continue;
         // the multi-step form only when asked for: it never won on GB300

@@ -237,6 +237,12 @@ cudaError_t launch_batch_step_f32(int precision, int nt, bool gen, bool steady_t
                                   const StepArgs *d_args, const TileRef *d_tiles, int ntiles,
                                   int grid, int k, cudaStream_t st);
 int batch_blocks_per_sm_f64(int nt);
+// Resident CTAs per SM of the pair-strip kernel (FP32 / FP16 storage).
+int pair_blocks_per_sm(int precision, int nt);
+// Rows per pair strip for a lattice: the strip march takes about the same
+// time in every CTA, so a launch lasts (waves of resident CTAs) x (rows + 4
+// halo rows); the rule takes the height that minimises that product.
+int pair_rows(int Lx, int Ly, int precision, int nt);
 int batch_blocks_per_sm_f32(int precision, int nt);
 
 // plain FP64 per-op kernels (reference operation order)

@@ -124,6 +124,18 @@ cudaError_t launch_batch_step_f32(int precision, int nt, bool gen, bool steady_t
     return e;
 }
 
+// Resident CTAs per SM of the pair-strip kernel of geometry nt (-32, -64, -128).
+int pair_blocks_per_sm(int precision, int nt) {
+    int n = 0;
+    if (nt == -32)
+        DISPATCH_STORE(precision, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pair_step_kernel<S, 32>, 32, 0));
+    else if (nt == -128)
+        DISPATCH_STORE(precision, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pair_step_kernel<S, 128>, 128, 0));
+    else
+        DISPATCH_STORE(precision, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pair_step_kernel<S, 64>, 64, 0));
+    return n < 1 ? 1 : n;
+}
+
 // Resident CTAs per SM of the batch kernel most launches use (the steady
 // form at the default width: fewer registers, so more CTAs).  The table walk
 // needs no co-residency, so a grid sized for it is valid for every form.

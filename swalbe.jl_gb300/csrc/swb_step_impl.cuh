@@ -859,7 +859,7 @@ __device__ __noinline__ void thermal_force(unsigned long long seed, long long ce
 template <class R>
 struct CellConst {
     R delta6, delta3sq, mu6, omeg, invtau, g, incl_fac;
-    double corr;  // FP16 mass correction per cell of this iteration
+    R corr;  // mass correction per cell of this iteration, converted once per CTA
 };
 
 template <class R>
@@ -877,7 +877,7 @@ __device__ __forceinline__ CellConst<R> cell_consts(const StepArgs &a, long long
     c.omeg = R(a.omeg);
     c.invtau = R(a.invtau);
     c.g = R(a.g);
-    c.corr = corr;
+    c.corr = R(corr);
     return c;
 }
 
@@ -978,7 +978,7 @@ __device__ __forceinline__ void collide_fast(const CellConst<float> &cc, float h
     const R ssum = small8(fo);
     const R f0 = mc - ssum;
     const R e = (mc - f0) - ssum;
-    const R c = e + hlo + R(cc.corr);
+    const R c = e + hlo + cc.corr;
     fo[0] = add_stochastic((float)f0, (float)c, mix32((unsigned)cell, (unsigned)tt));
     if constexpr (!S::kHalf) {
         // What the rounding left out, c - k ulp(f0): zero-mean whatever
