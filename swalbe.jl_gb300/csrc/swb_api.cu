@@ -537,21 +537,49 @@ constexpr int kRunChunk = 1024;
 
 // CTAs of the multi-step kernel for the state's geometry: one per strip plus
 // the reducer, capped at what the GPU holds at once (0: not possible).
-int run_grid(swb_state *s) {
-    const int per_sm = swb::fused_run_blocks_per_sm(s->precision, s->a.march_nt);
-    if (per_sm <= 0) return 0;
+int sm_count() {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const long long want =
-        (long long)s->a.tiles_x * s->a.tiles_y + (swb::needs_partials(s->a) ? 1 : 0);
-    const long long cap = (long long)per_sm * sms;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1)
+        sms = 1;
+    return sms;
+}
+
+// Rows of resident tiles for a lattice: the shortest tiles (the most CTAs)
+// whose CTAs are all co-resident; 0 when even kResMaxTH rows do not fit.
+int resident_rows(int Lx, int Ly, int precision) {
+    const long long tx = (Lx + swb::kResTW - 1) / swb::kResTW, sms = sm_count();
+    for (int h = 1; h <= swb::kResMaxTH; ++h) {
+        const long long tiles = tx * ((Ly + h - 1) / h);
+        const int per_sm = swb::resident_blocks_per_sm(precision, h);
+        if (per_sm > 0 && tiles <= per_sm * sms) return h < Ly ? h : Ly;
+    }
+    return 0;
+}
+
+// CTAs of the multi-step kernel for the state's geometry: one per strip plus
+// the reducer, capped at what the GPU holds at once; resident tiles: one per
+// tile, all of which must be co-resident (0: not possible).
+int run_grid(swb_state *s) {
+    const long long tiles = (long long)s->a.tiles_x * s->a.tiles_y;
+    if (s->a.march_nt == swb::kResGeom) {
+        const int per_sm = swb::resident_blocks_per_sm(s->precision, s->a.march_h);
+        return (per_sm > 0 && tiles <= (long long)per_sm * sm_count()) ? (int)tiles : 0;
+    }
+    const int per_sm = swb::fused_run_blocks_per_sm(s->precision, s->a.march_nt);
+    if (per_sm <= 0) return 0;
+    const long long want = tiles + (swb::needs_partials(s->a) ? 1 : 0);
+    const long long cap = (long long)per_sm * sm_count();
     return (int)(want < cap ? want : cap);
 }
 
+// Whether the state's iterations can run in its multi-step form now:
+// strips / 2D tiles of FP32-arithmetic states, or resident tiles for the
+// common steady τ = 1 step.
 bool run_possible(const swb_state *s) {
-    return (s->precision == SWB_F32 || s->precision == SWB_F16) &&
-           (s->a.march_nt == 64 || s->a.march_nt == 128 || s->a.march_nt == swb::kTileGeom);
+    if (s->precision != SWB_F32 && s->precision != SWB_F16) return false;
+    if (s->a.march_nt == swb::kResGeom) return swb::resident_ok(s->a) && run_grid(const_cast<swb_state *>(s)) > 0;
+    return s->a.march_nt == 64 || s->a.march_nt == 128 || s->a.march_nt == swb::kTileGeom;
 }
 
 // n iterations as multi-step launches of at most kRunChunk iterations.
@@ -560,7 +588,9 @@ cudaError_t run_sequence(swb_state *s, long long n) {
     if (grid <= 0) return cudaErrorInvalidConfiguration;
     while (n > 0) {
         const int c = (int)(n < kRunChunk ? n : kRunChunk);
-        cudaError_t e = swb::launch_fused_run(s->precision, s->a, c, grid, s->stream);
+        cudaError_t e = s->a.march_nt == swb::kResGeom
+                            ? swb::launch_resident_run(s->precision, s->a, c, s->stream)
+                            : swb::launch_fused_run(s->precision, s->a, c, grid, s->stream);
         if (e != cudaSuccess) return e;
         swb::count_launches(1);
         n -= c;
@@ -570,9 +600,10 @@ cudaError_t run_sequence(swb_state *s, long long n) {
 
 // Launch form without the tuner: one launch per iteration unless the
 // multi-step kernel was asked for (on GB300 it measured 5-25 % slower than
-// graph-replayed launches at 512^2..2048^2; the tuner times both).
+// graph-replayed launches at 512^2..2048^2; the tuner times both) or the
+// geometry is resident tiles (a multi-step form only).
 bool persist_default(const swb_state *s) {
-    return s->mode == SWB_STEP_MULTI && run_possible(s);
+    return (s->mode == SWB_STEP_MULTI || s->a.march_nt == swb::kResGeom) && run_possible(s);
 }
 
 // n step launches (k = 0..n-1) and the advance kernel that closes them.
@@ -668,12 +699,16 @@ int autotune_geometry(swb_state *s, long long &left) {
     if (pair_ok && s->mode != SWB_STEP_MULTI) {  // and the wave rule's rows
         for (int pn : {-64, -32}) todo.push_back({pn, swb::pair_rows(s->p.Lx, s->p.Ly, s->precision, pn), 0});
     }
+    // resident tiles (a multi-step form) where the lattice fits in the CTAs'
+    // shared memory: the shortest co-resident tiles
+    const int res_h = (multi_ok && swb::resident_ok(s->a)) ? resident_rows(s->p.Lx, s->p.Ly, s->precision) : 0;
+    if (res_h > 0) todo.push_back({swb::kResGeom, res_h, 1});
     for (auto &c : todo) {
         if (c[0] == K && !multi_ok) continue;
         if (c[0] < 0 && !pair_ok) continue;
         // the multi-step form only when asked for: it never won on GB300
         // (sweeps at 512^2..2048^2), and a 16-iteration probe can misjudge it
-        if (c[2] && (!multi_ok || s->mode != SWB_STEP_MULTI)) continue;
+        if (c[2] && c[0] != swb::kResGeom && (!multi_ok || s->mode != SWB_STEP_MULTI)) continue;
         if (!c[2] && s->mode == SWB_STEP_MULTI) continue;
         cands.push_back({c[0], c[1], c[2]});
     }
@@ -732,7 +767,9 @@ int fused_steps(swb_state *s, long long nsteps) {
         int rc = autotune_geometry(s, left);
         if (rc) return rc;
     }
-    if (s->persist) {
+    // (a resident-tile state whose θ, forces or τ changed since the form was
+    // chosen runs one launch per iteration, on strips of the same rows)
+    if (s->persist && run_possible(s)) {
         if (left > 0) CUDA_TRY(&s->err, run_sequence(s, left));
         left = 0;
     }
@@ -1148,6 +1185,19 @@ int swb_set_geometry(swb_state *s, int nt, int h) {
         if (s->precision == SWB_F64)
             return fail(&s->err, SWB_ERR_UNSUPPORTED, "2D tiles: FP32 and FP16 storage only");
         h = swb::kTileY;
+    } else if (nt == swb::kResGeom) {
+        if (s->precision != SWB_F32 && s->precision != SWB_F16)
+            return fail(&s->err, SWB_ERR_UNSUPPORTED, "resident tiles: FP32 and FP16 storage only");
+        if (h == 0) h = resident_rows(s->p.Lx, s->p.Ly, s->precision);
+        if (h < 1 || h > swb::kResMaxTH)
+            return fail(&s->err, SWB_ERR_UNSUPPORTED,
+                        "resident tiles: the lattice does not fit in the GPU's shared memory "
+                        "(rows must be 1..40 with every tile co-resident)");
+        const long long tiles = (long long)((s->p.Lx + swb::kResTW - 1) / swb::kResTW) *
+                                ((s->p.Ly + h - 1) / h);
+        if (tiles > (long long)swb::resident_blocks_per_sm(s->precision, h) * sm_count())
+            return fail(&s->err, SWB_ERR_UNSUPPORTED,
+                        "resident tiles: more tiles than the GPU holds at once; use more rows");
     } else if (swb::pair_geometry(nt)) {
         if (s->precision == SWB_F64)
             return fail(&s->err, SWB_ERR_UNSUPPORTED, "pair strips: FP32 and FP16 storage only");
@@ -1161,7 +1211,7 @@ int swb_set_geometry(swb_state *s, int nt, int h) {
                     "-128 (pair strips), or nt = 32 (2D tiles)");
     }
     if (s->mode == SWB_STEP_MULTI && (nt == 256 || nt < 0))
-        return fail(&s->err, SWB_ERR_UNSUPPORTED, "multi-step kernel: nt must be 64, 128 or 32");
+        return fail(&s->err, SWB_ERR_UNSUPPORTED, "multi-step kernel: nt must be 64, 128, 32 or 33");
     s->autotune = false;  // an explicit geometry (or the default) is kept
     s->tuned = true;
     if (s->a.march_nt != nt || s->a.march_h != h) {
@@ -1187,6 +1237,11 @@ int swb_set_step_mode(swb_state *s, int mode) {
     s->mode = mode;
     if (mode == SWB_STEP_MULTI && (s->a.march_nt == 256 || s->a.march_nt < 0)) {
         int nt = 128, h = 0;
+        swb::default_geometry(s->p.Lx, s->p.Ly, s->precision, &nt, &h);
+        swb::set_geometry(s->a, nt, h);
+    }
+    if (mode == SWB_STEP_PER_ITERATION && s->a.march_nt == swb::kResGeom) {
+        int nt = 0, h = 0;  // resident tiles are a multi-step form
         swb::default_geometry(s->p.Lx, s->p.Ly, s->precision, &nt, &h);
         swb::set_geometry(s->a, nt, h);
     }

@@ -130,6 +130,13 @@ constexpr int kTileX = 32, kTileY = 16, kTileThreads = 256;
 // other iterations of such a state run as one-column strips of 64 threads
 // with the same rows (pair_fallback).
 inline bool pair_geometry(int nt) { return nt == -32 || nt == -64 || nt == -128; }
+// Resident tiles (a multi-step launch form, SWB_F32 / SWB_F16): geometry
+// value kResGeom, tiles of kResTW columns x h rows (1 <= h <= kResMaxTH), one
+// CTA of kResThreads threads per tile holding the tile's populations in
+// shared memory, all CTAs co-resident.  Only the common steady τ = 1 step
+// has this form; other iterations run on strips (strip_fallback).
+constexpr int kResGeom = 33;
+constexpr int kResTW = 64, kResMaxTH = 40, kResThreads = 512;
 
 inline void set_geometry(StepArgs &a, int nt, int h) {
     a.march_nt = nt;
@@ -139,19 +146,29 @@ inline void set_geometry(StepArgs &a, int nt, int h) {
         a.tiles_y = (a.Ly + kTileY - 1) / kTileY;
         return;
     }
+    if (nt == kResGeom) {
+        a.march_h = h;
+        a.tiles_x = (a.Lx + kResTW - 1) / kResTW;
+        a.tiles_y = (a.Ly + h - 1) / h;
+        return;
+    }
     a.march_h = h;
     const int w = nt < 0 ? -2 * nt - 4 : nt - 4;  // strip width in columns
     a.tiles_x = (a.Lx + w - 1) / w;
     a.tiles_y = (a.Ly + h - 1) / h;
 }
 // Threads per CTA of a geometry.
-inline int geometry_threads(int nt) { return nt == kTileGeom ? kTileThreads : (nt < 0 ? -nt : nt); }
-// The one-column strips that run the iterations the pair form leaves out.
-inline StepArgs pair_fallback(const StepArgs &a) {
+inline int geometry_threads(int nt) {
+    return nt == kTileGeom ? kTileThreads : (nt == kResGeom ? kResThreads : (nt < 0 ? -nt : nt));
+}
+// The one-column strips (64 threads, the same rows) that run the iterations
+// the pair-strip and resident-tile forms leave out.
+inline StepArgs strip_fallback(const StepArgs &a) {
     StepArgs b = a;
-    set_geometry(b, 64, a.march_h);
+    set_geometry(b, 64, a.march_h < kMinRows ? kMinRows : a.march_h);
     return b;
 }
+inline StepArgs pair_fallback(const StepArgs &a) { return strip_fallback(a); }
 
 // Entry in the packed tile table of a batch (tx = -1: the lattice's reducer).
 struct TileRef {
@@ -237,6 +254,15 @@ cudaError_t launch_batch_step_f32(int precision, int nt, bool gen, bool steady_t
                                   const StepArgs *d_args, const TileRef *d_tiles, int ntiles,
                                   int grid, int k, cudaStream_t st);
 int batch_blocks_per_sm_f64(int nt);
+// Resident tiles: dynamic shared memory of a tile of h rows, CTAs per SM
+// that hold it (0: not possible), and n iterations in one cooperative launch
+// of tiles_x * tiles_y CTAs (closes the sequence itself).
+size_t resident_smem_bytes(int h);
+int resident_blocks_per_sm(int precision, int h);
+cudaError_t launch_resident_run(int precision, const StepArgs &a, int n, cudaStream_t st);
+// Whether iterations of `a` may run as resident tiles (the common steady
+// τ = 1 step of an FP32-arithmetic lattice).
+inline bool resident_ok(const StepArgs &a) { return a.tau_is_one && !step_general(a); }
 // Resident CTAs per SM of the pair-strip kernel (FP32 / FP16 storage).
 int pair_blocks_per_sm(int precision, int nt);
 // Rows per pair strip for a lattice: the strip march takes about the same

@@ -25,6 +25,7 @@ UNITS = {
     # batch) must round identically for results to be independent of it
     "swb_step_f32.cu": ["--fmad=false"],
     "swb_run_f32.cu": ["--fmad=false"],
+    "swb_resident.cu": ["--fmad=false"],
     "swb_api.cu": [],
     "swb_batch.cu": [],
     "swb_server.cu": [],

@@ -138,3 +138,55 @@ def test_tiles_small_and_ragged(L):
     a = run(s, h0, "multi", (32, 16), (37,), np.float32)
     b = run(s, h0, "per_iteration", (64, 4), (37,), np.float32)
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+# ------------------------------------------------------------------ resident tiles
+def _run_form(s, h0, steps, T, geo, chunks=3, wave=None):
+    st = sw.Sys(s, "GB300", T=T)
+    st.set_geometry(*geo)
+    st.set_measures(L.MEAS_ALL)
+    if wave:
+        st.set_theta_wave(*wave)
+    st.height = h0
+    done = 0
+    for c in range(chunks):
+        n = (steps - done) if c == chunks - 1 else steps // chunks
+        st.step(n)
+        done += n
+    st.sync()
+    return st, st.height, st.measures_array(cap=steps)
+
+
+@pytest.mark.parametrize("T", [np.float32, np.float16])
+def test_resident_tiles_equal_strips(T):
+    """Resident tiles (populations kept in shared memory across iterations of
+    one cooperative launch, a 3-cell ring exchanged through L2) give the bits
+    of the strips: heights and every per-step measure, on lattices with full
+    and partial tiles, narrower than a tile, and more iterations than one
+    launch takes."""
+    cases = [(512, 512, 300), (96, 64, 200), (48, 40, 1500), (130, 34, 200), (256, 256, 120)]
+    for Lx, Ly, steps in cases:
+        s = sw.SysConst(Lx, Ly, sw.Taumucs(delta=2.0))
+        h0 = np.asfortranarray(1.0 + 0.1 * np.random.default_rng(Lx + Ly).uniform(-1, 1, (Lx, Ly)))
+        _, h_ref, r_ref = _run_form(s, h0, steps, T, (64, 8))
+        st, h, r = _run_form(s, h0, steps, T, (33, 0))
+        assert st.geometry()[0] == 33 and st.step_mode() == "multi", (Lx, Ly)
+        assert np.array_equal(h, h_ref), (Lx, Ly)
+        for f in ("t", "mass", "wetted", "hmax", "hmin", "area", "energy"):
+            assert np.array_equal(r[f], r_ref[f]), (Lx, Ly, f)
+
+
+def test_resident_tiles_fallback_and_rules():
+    """A resident-tile state whose iterations need another form (a θ wave)
+    runs them one launch each, on strips: same results; Float64 and lattices
+    too large for the GPU's shared memory are refused."""
+    s = sw.SysConst(96, 64, sw.Taumucs())
+    h0 = np.asfortranarray(1.0 + 0.1 * np.random.default_rng(1).uniform(-1, 1, (96, 64)))
+    wave = (1 / 9, 1 / 36, 1 / 98)
+    _, h_ref, _ = _run_form(s, h0, 100, np.float32, (64, 8), wave=wave)
+    _, h, _ = _run_form(s, h0, 100, np.float32, (33, 0), wave=wave)
+    assert np.array_equal(h, h_ref)
+    with pytest.raises(sw.SwbError):
+        sw.Sys(s, "GB300", T=np.float64).set_geometry(33, 0)
+    with pytest.raises(sw.SwbError):
+        sw.Sys(sw.SysConst(2048, 2048, sw.Taumucs()), "GB300", T=np.float32).set_geometry(33, 0)
