@@ -475,6 +475,7 @@ def ensemble_run(sw, np, count=512, steps=200, plain_sample=8):
     dt = time.perf_counter() - t0
     batch_mlups = cells * steps / dt / 1e6
     tile = b.tile()
+    bgeo = b.geometry()
     b.close()
     del b
     # one at a time: the plain Float64 per-op path and the fused FP32 step
@@ -499,7 +500,9 @@ def ensemble_run(sw, np, count=512, steps=200, plain_sample=8):
     return {
         "instances": count, "cells": cells, "time_steps_per_sim": full_steps,
         "batch_f32": {"MLUPS": batch_mlups, "sims_per_s": count * steps / (dt * full_steps),
-                      "timed_steps": steps, "strip": {"width": tile[0], "rows": tile[1]}},
+                      "timed_steps": steps, "strip": {"width": tile[0], "rows": tile[1],
+                                "threads": abs(bgeo[0]), "columns_per_thread": 2 if bgeo[0] < 0 else 1,
+                                "ctas": bgeo[2], "chosen_by": "batch autotuner (strip shapes x CTA counts)"}},
         **out,
         "speedup_vs_plain": batch_mlups / out["plain_f64_one_at_a_time"]["MLUPS"],
         "speedup_vs_fused_one_at_a_time": batch_mlups / out["fused_f32_one_at_a_time"]["MLUPS"],

@@ -313,10 +313,18 @@ int swb_batch_step(swb_batch *b, int64_t nsteps);
 /* Waits for the batch; SWB_ERR_NAN (lattice index in swb_last_error) if a
  * lattice saw a non-finite height. */
 int swb_batch_sync(swb_batch *b);
-/* Strips of every lattice: nt threads (64, 128, 256; nt - 4 columns) and
- * `rows` rows (2..512, capped at each lattice's height).  Default 64 x 32:
- * the batch's parallelism comes from its many lattices, so strips are tall. */
+/* Strips of every lattice: nt threads (64, 128, 256; nt - 4 columns), or
+ * pair strips of -nt threads (nt = -32, -64, -128; 2|nt| - 4 columns, two per
+ * thread; SWB_F32 / SWB_F16 with even Lx in every lattice; iterations the
+ * pair form has no kernel for run on 64-thread strips), and `rows` rows
+ * (2..512, capped at each lattice's height).  By default the first
+ * swb_batch_step with enough steps times a few geometries (one-column and,
+ * where possible, pair strips) and CTA counts on real steps and keeps the
+ * fastest; setting a geometry keeps it and tunes only the CTA count. */
 int swb_batch_set_geometry(swb_batch *b, int nt, int rows);
+/* The geometry in use (nt as above), and the CTAs per launch (0: not tuned yet). */
+int swb_batch_geometry(swb_batch *b, int *nt, int *rows, int *grid);
+/* Strip width in columns and rows, and iterations per captured graph (0 until tuned). */
 int swb_batch_tile(swb_batch *b, int *tile_x, int *tile_y, int *steps_per_graph);
 
 /* ---------------------------------------------------------------------- */

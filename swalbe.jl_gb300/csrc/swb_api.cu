@@ -625,6 +625,7 @@ cudaError_t launch_sequence(swb_state *s, int n) {
 // SWB_F64 / SWB_F32, whose results do not depend on the geometry.
 constexpr int kTuneMinSteps = 512;
 constexpr int kTuneProbe = 16;
+constexpr int kPersistProbe = 4;
 
 // One candidate's probe: a per-iteration sequence is captured into a graph
 // (as it runs outside the tuner), a multi-step one is a single launch.
@@ -650,6 +651,11 @@ float tune_probe(swb_state *s, cudaEvent_t e0, cudaEvent_t e1) {
         cudaGraphDestroy(g);
         if (ie != cudaSuccess) return -1.f;
     }
+    // a multi-step candidate runs kPersistProbe times the iterations in one
+    // launch and is scaled back: outside the tuner it runs launches of up to
+    // kRunChunk iterations, whose set-up (loading a resident tile's region,
+    // the cooperative launch) a 16-iteration launch would overweight
+    const int reps = gx ? 1 : kPersistProbe;
     float ms = -1.f;
     for (int rep = 0; rep < 2; ++rep) {
         cudaEventRecord(e0, s->stream);
@@ -658,7 +664,7 @@ float tune_probe(swb_state *s, cudaEvent_t e0, cudaEvent_t e1) {
             e = cudaGraphLaunch(gx, s->stream);
             swb::count_launches(nodes);
         } else {
-            e = run_sequence(s, kTuneProbe);
+            e = run_sequence(s, (long long)kTuneProbe * reps);
         }
         cudaEventRecord(e1, s->stream);
         if (e == cudaSuccess) e = cudaEventSynchronize(e1);
@@ -666,8 +672,9 @@ float tune_probe(swb_state *s, cudaEvent_t e0, cudaEvent_t e1) {
             ms = -1.f;
             break;
         }
-        s->steps += kTuneProbe;
+        s->steps += (long long)kTuneProbe * reps;
         cudaEventElapsedTime(&ms, e0, e1);
+        ms /= (float)reps;
     }
     if (gx) cudaGraphExecDestroy(gx);
     return ms;
@@ -725,12 +732,13 @@ int autotune_geometry(swb_state *s, long long &left) {
         swb::set_geometry(s->a, c[0], c[1]);
         s->persist = c[2] != 0;
         if (s->persist && run_grid(s) <= 0) continue;
+        if (s->persist && left < 2 * kTuneProbe * kPersistProbe) continue;
         const float ms = tune_probe(s, e0, e1);
         if (ms < 0.f) {
             rc = fail(&s->err, SWB_ERR_CUDA, "autotuner probe failed");
             break;
         }
-        left -= 2 * kTuneProbe;
+        left -= 2 * kTuneProbe * (s->persist ? kPersistProbe : 1);
         if (ms < best) {
             best = ms;
             bnt = c[0];

@@ -4,6 +4,7 @@
 // The CTA count per launch is picked by timing the candidates on the first
 // steps (the timed steps are real steps of the simulation).
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <string>
 #include <vector>
@@ -154,6 +155,12 @@ struct swb_batch {
     TileRef *d_tiles = nullptr;
     int *d_flags = nullptr;
     int ntiles = 0;
+    // pair strips (nt < 0): the one-column strips (64 threads, same rows) of
+    // the iterations the pair form leaves out, with their own table
+    StepArgs *d_args_fb = nullptr;
+    TileRef *d_tiles_fb = nullptr;
+    int ntiles_fb = 0;
+    size_t cap_tiles = 0, cap_tiles_fb = 0;
     cudaStream_t stream = nullptr;
     cudaGraphExec_t gexec = nullptr;
     int steps_per_graph = 32;
@@ -177,6 +184,8 @@ struct swb_batch {
         cudaFree(d_args);
         cudaFree(d_tiles);
         cudaFree(d_flags);
+        cudaFree(d_args_fb);
+        cudaFree(d_tiles_fb);
         if (stream) cudaStreamDestroy(stream);
     }
 };
@@ -204,14 +213,71 @@ std::vector<TileRef> build_tiles(const std::vector<StepArgs> &args) {
     return tiles;
 }
 
+// Copies of the lattices' arguments with the one-column fallback strips.
+std::vector<StepArgs> fallback_args(const swb_batch *b) {
+    std::vector<StepArgs> fb = b->args;
+    for (StepArgs &a : fb) a = swb::strip_fallback(a);
+    return fb;
+}
+
+// Device copy of a tile table, growing its buffer when needed.
+cudaError_t put_tiles(swb_batch *b, TileRef **d, size_t *cap, const std::vector<TileRef> &t) {
+    if (t.size() > *cap) {
+        cudaFree(*d);
+        *d = nullptr;
+        cudaError_t e = cudaMalloc((void **)d, sizeof(TileRef) * t.size());
+        if (e != cudaSuccess) return e;
+        *cap = t.size();
+    }
+    return cudaMemcpy(*d, t.data(), sizeof(TileRef) * t.size(), cudaMemcpyHostToDevice);
+}
+
 int upload_args(swb_batch *b) {
     if (!b->args_dirty) return SWB_OK;
     B_TRY(b, cudaMemcpyAsync(b->d_args, b->args.data(), b->args.size() * sizeof(StepArgs),
                              cudaMemcpyHostToDevice, b->stream));
+    std::vector<StepArgs> fb;
+    if (b->nt < 0) {
+        fb = fallback_args(b);
+        if (!b->d_args_fb) B_TRY(b, cudaMalloc((void **)&b->d_args_fb, sizeof(StepArgs) * b->count));
+        B_TRY(b, cudaMemcpyAsync(b->d_args_fb, fb.data(), fb.size() * sizeof(StepArgs),
+                                 cudaMemcpyHostToDevice, b->stream));
+    }
     B_TRY(b, cudaStreamSynchronize(b->stream));
     b->args_dirty = false;
     b->invalidate();
     return SWB_OK;
+}
+
+// Strip geometry of every lattice (nt < 0: pair strips, which need FP32
+// arithmetic and even Lx everywhere) and the tile tables.
+int apply_geometry(swb_batch *b, int nt, int rows) {
+    B_TRY(b, cudaStreamSynchronize(b->stream));
+    b->nt = nt;
+    b->rows = rows;
+    for (int i = 0; i < b->count; ++i) {
+        int h = rows < b->params[i].Ly ? rows : b->params[i].Ly;
+        if (h < swb::kMinRows) h = swb::kMinRows;
+        swb::set_geometry(b->args[i], nt, h);
+    }
+    const std::vector<TileRef> tiles = build_tiles(b->args);
+    B_TRY(b, put_tiles(b, &b->d_tiles, &b->cap_tiles, tiles));
+    b->ntiles = (int)tiles.size();
+    if (nt < 0) {
+        const std::vector<TileRef> fbt = build_tiles(fallback_args(b));
+        B_TRY(b, put_tiles(b, &b->d_tiles_fb, &b->cap_tiles_fb, fbt));
+        b->ntiles_fb = (int)fbt.size();
+    }
+    b->args_dirty = true;
+    b->invalidate();
+    return upload_args(b);
+}
+
+bool pair_possible(const swb_batch *b) {
+    if (b->precision != SWB_F32 && b->precision != SWB_F16) return false;
+    for (const swb_params &p : b->params)
+        if (p.Lx % 2) return false;
+    return true;
 }
 
 // n batched step launches (k = 0..n-1) and the advance kernel closing them.
@@ -226,9 +292,15 @@ cudaError_t batch_sequence(swb_batch *b, int n, int grid) {
         gen = gen || swb::step_general(a);
         tau1 = tau1 && a.tau_is_one;
     }
-    for (int k = 0; k < n && e == cudaSuccess; ++k)
-        e = swb::launch_batch_step(b->precision, b->nt, gen, tau1 && !(b->fresh_pending && k == 0),
-                                   b->d_args, b->d_tiles, b->ntiles, grid, k, b->stream);
+    for (int k = 0; k < n && e == cudaSuccess; ++k) {
+        const bool steady = tau1 && !(b->fresh_pending && k == 0);
+        if (b->nt < 0 && (gen || !steady))  // an iteration the pair form leaves out
+            e = swb::launch_batch_step(b->precision, 64, gen, steady, b->d_args_fb, b->d_tiles_fb,
+                                       b->ntiles_fb, grid, k, b->stream);
+        else
+            e = swb::launch_batch_step(b->precision, b->nt, gen, steady, b->d_args, b->d_tiles,
+                                       b->ntiles, grid, k, b->stream);
+    }
     if (e == cudaSuccess && n > 0) e = swb::launch_batch_advance(b->d_args, b->count, n, b->stream);
     return e;
 }
@@ -238,47 +310,79 @@ int launch_n(swb_batch *b, int n, int grid) {
     return SWB_OK;
 }
 
-// Picks the CTA count: one CTA per tile, or persistent CTAs (k per SM).
+// Autotuner: times real steps of a few strip geometries (one-column strips
+// of 64 or 128 threads, and pair strips where every lattice allows them),
+// each with a few CTA counts (persistent CTAs, k per SM, or one CTA per
+// tile), and keeps the fastest.  Results do not depend on the choice (the
+// per-cell arithmetic is the same and the measures are exact sums).
 int autotune(swb_batch *b, long long &left) {
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int occ = swb::batch_blocks_per_sm(b->precision, b->nt);
-    std::vector<int> cands = {b->ntiles};
-    for (int k = 1; k <= occ; ++k) cands.push_back(std::min(b->ntiles, sms * k));
-    std::sort(cands.begin(), cands.end());
-    cands.erase(std::unique(cands.begin(), cands.end()), cands.end());
-    const int probe = 4;
-    if (left < (long long)probe * (long long)cands.size() + probe) {
-        b->grid = std::min(b->ntiles, sms * occ);
-        b->tuned = true;
-        return SWB_OK;
+    bool gen = false, tau1 = true;
+    for (const StepArgs &a : b->args) {
+        gen = gen || swb::step_general(a);
+        tau1 = tau1 && a.tau_is_one;
     }
+    std::vector<std::array<int, 2>> geos = {{64, 32}, {64, 16}, {128, 16}};
+    if (pair_possible(b) && !gen && tau1) {
+        geos.push_back({-64, 16});
+        geos.push_back({-64, 32});
+        geos.push_back({-32, 16});
+    }
+    if (b->nt != swb::kBatchNT || b->rows != swb::kBatchRows)  // a geometry set by the caller
+        geos = {{b->nt, b->rows}};
+    const int probe = 2;
+    struct Best {
+        float ms = 1e30f;
+        int nt = 0, rows = 0, grid = 0;
+    } best;
     cudaEvent_t e0, e1;
     B_TRY(b, cudaEventCreate(&e0));
     B_TRY(b, cudaEventCreate(&e1));
-    float best = 1e30f;
-    int best_grid = cands.back();
-    int rc = launch_n(b, 1, cands.back());  // warm-up (a real step)
-    left -= 1;
-    for (int g : cands) {
+    int rc = SWB_OK;
+    for (auto &g : geos) {
         if (rc) break;
-        cudaEventRecord(e0, b->stream);
-        rc = launch_n(b, probe, g);
-        cudaEventRecord(e1, b->stream);
-        cudaEventSynchronize(e1);
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, e0, e1);
-        if (ms < best) {
-            best = ms;
-            best_grid = g;
+        if (g[0] != b->nt || g[1] != b->rows) {
+            rc = apply_geometry(b, g[0], g[1]);
+            if (rc) break;
         }
-        left -= probe;
+        const int occ = swb::batch_blocks_per_sm(b->precision, b->nt);
+        std::vector<int> grids = {b->ntiles, std::min(b->ntiles, sms * occ),
+                                  std::min(b->ntiles, sms * std::max(1, occ / 2))};
+        std::sort(grids.begin(), grids.end());
+        grids.erase(std::unique(grids.begin(), grids.end()), grids.end());
+        if (left < 1 + (long long)probe * (long long)grids.size()) break;
+        rc = launch_n(b, 1, grids.back());  // loads the kernel (a real step)
+        left -= 1;
+        for (int gr : grids) {
+            if (rc) break;
+            cudaEventRecord(e0, b->stream);
+            rc = launch_n(b, probe, gr);
+            cudaEventRecord(e1, b->stream);
+            cudaEventSynchronize(e1);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            left -= probe;
+            if (ms < best.ms) best = {ms, b->nt, b->rows, gr};
+        }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (rc) return rc;
-    b->grid = best_grid;
+    if (best.nt == 0) {  // too few steps to probe: the default strips, persistent CTAs
+        if (b->nt != swb::kBatchNT || b->rows != swb::kBatchRows) {
+            rc = apply_geometry(b, swb::kBatchNT, swb::kBatchRows);
+            if (rc) return rc;
+        }
+        b->grid = std::min(b->ntiles, sms * swb::batch_blocks_per_sm(b->precision, b->nt));
+    } else {
+        if (best.nt != b->nt || best.rows != b->rows) {
+            rc = apply_geometry(b, best.nt, best.rows);
+            if (rc) return rc;
+        }
+        b->grid = best.grid;
+    }
     b->tuned = true;
     return SWB_OK;
 }
@@ -346,6 +450,7 @@ int swb_batch_create(const swb_params *params, int count, int precision, swb_bat
     BC_TRY(cudaMalloc((void **)&b->d_flags, sizeof(int) * count));
     BC_TRY(cudaMalloc((void **)&b->d_tiles, sizeof(TileRef) * tiles.size()));
     BC_TRY(cudaMemcpy(b->d_tiles, tiles.data(), sizeof(TileRef) * tiles.size(), cudaMemcpyHostToDevice));
+    b->cap_tiles = tiles.size();
 #undef BC_TRY
     *out = b;
     return SWB_OK;
@@ -448,35 +553,31 @@ int swb_batch_sync(swb_batch *b) {
 }
 
 int swb_batch_set_geometry(swb_batch *b, int nt, int rows) {
-    if (!b || (nt != 64 && nt != 128 && nt != 256) || rows < swb::kMinRows || rows > swb::kMaxRows)
+    if (!b || rows < swb::kMinRows || rows > swb::kMaxRows ||
+        (nt != 64 && nt != 128 && nt != 256 && !swb::pair_geometry(nt)))
         return swb::bfail(b ? &b->err : nullptr, SWB_ERR_ARG,
-                          "batch geometry: nt must be 64, 128 or 256 and 4 <= rows <= 512");
-    B_TRY(b, cudaStreamSynchronize(b->stream));
-    b->nt = nt;
-    b->rows = rows;
-    for (int i = 0; i < b->count; ++i) {
-        int h = rows < b->params[i].Ly ? rows : b->params[i].Ly;
-        if (h < swb::kMinRows) h = swb::kMinRows;
-        swb::set_geometry(b->args[i], nt, h);
-    }
-    const std::vector<TileRef> tiles = build_tiles(b->args);
-    if ((int)tiles.size() > b->ntiles) {
-        cudaFree(b->d_tiles);
-        b->d_tiles = nullptr;
-        B_TRY(b, cudaMalloc((void **)&b->d_tiles, sizeof(TileRef) * tiles.size()));
-    }
-    B_TRY(b, cudaMemcpy(b->d_tiles, tiles.data(), sizeof(TileRef) * tiles.size(),
-                        cudaMemcpyHostToDevice));
-    b->ntiles = (int)tiles.size();
-    b->args_dirty = true;
-    b->tuned = false;  // re-pick the CTA count
-    b->invalidate();
+                          "batch geometry: nt must be 64, 128, 256 or -32, -64, -128 (pair "
+                          "strips) and 2 <= rows <= 512");
+    if (nt < 0 && !pair_possible(b))
+        return swb::bfail(&b->err, SWB_ERR_UNSUPPORTED,
+                          "batch pair strips: FP32 or FP16 storage and even Lx in every lattice");
+    const int rc = apply_geometry(b, nt, rows);
+    if (rc) return rc;
+    b->tuned = false;  // re-pick the CTA count (the tuner keeps this geometry)
+    return SWB_OK;
+}
+
+int swb_batch_geometry(swb_batch *b, int *nt, int *rows, int *grid) {
+    if (!b) return swb::bfail(nullptr, SWB_ERR_ARG, "batch is NULL");
+    if (nt) *nt = b->nt;
+    if (rows) *rows = b->rows;
+    if (grid) *grid = b->grid;
     return SWB_OK;
 }
 
 int swb_batch_tile(swb_batch *b, int *tile_x, int *tile_y, int *steps_per_graph) {
     if (!b) return swb::bfail(nullptr, SWB_ERR_ARG, "batch is NULL");
-    if (tile_x) *tile_x = b->tuned ? b->nt - 4 : 0;
+    if (tile_x) *tile_x = b->tuned ? (b->nt < 0 ? -2 * b->nt - 4 : b->nt - 4) : 0;
     if (tile_y) *tile_y = b->tuned ? b->rows : 0;
     if (steps_per_graph) *steps_per_graph = b->tuned ? b->steps_per_graph : 0;
     return SWB_OK;

@@ -176,10 +176,11 @@ struct TileRef {
     int tx, ty;
 };
 
-// Whether a lattice's step needs the general kernel (θ field or wave,
-// thermal noise, inclination) rather than the common one.
+// Whether a lattice's step needs the general kernel (θ field, thermal
+// noise, inclination) rather than the common one (scalar θ or the θ wave,
+// whose κ depends on the column only).
 inline bool step_general(const StepArgs &a) {
-    return a.thermal || a.incl || a.theta_mode != THETA_SCALAR;
+    return a.thermal || a.incl || a.theta_mode == THETA_FIELD;
 }
 
 // Whether the step kernels of a lattice produce per-step partial measures.
@@ -261,8 +262,10 @@ size_t resident_smem_bytes(int h);
 int resident_blocks_per_sm(int precision, int h);
 cudaError_t launch_resident_run(int precision, const StepArgs &a, int n, cudaStream_t st);
 // Whether iterations of `a` may run as resident tiles (the common steady
-// τ = 1 step of an FP32-arithmetic lattice).
-inline bool resident_ok(const StepArgs &a) { return a.tau_is_one && !step_general(a); }
+// τ = 1 step with scalar θ of an FP32-arithmetic lattice).
+inline bool resident_ok(const StepArgs &a) {
+    return a.tau_is_one && !step_general(a) && a.theta_mode == THETA_SCALAR;
+}
 // Resident CTAs per SM of the pair-strip kernel (FP32 / FP16 storage).
 int pair_blocks_per_sm(int precision, int nt);
 // Rows per pair strip for a lattice: the strip march takes about the same

@@ -117,6 +117,16 @@ cudaError_t launch_batch_step_f32(int precision, int nt, bool gen, bool steady_t
                                   const StepArgs *d_args, const TileRef *d_tiles, int ntiles,
                                   int grid, int k, cudaStream_t st) {
     cudaError_t e = cudaSuccess;
+    if (nt < 0) {  // pair strips: the caller passes their table only for steady common steps
+        if (gen || !steady_tau1) return cudaErrorInvalidValue;
+        if (nt == -32)
+            DISPATCH_STORE(precision, e = launch_step(batch_pair_kernel<S, 32>, grid, 32, st, d_args, d_tiles, ntiles, k));
+        else if (nt == -128)
+            DISPATCH_STORE(precision, e = launch_step(batch_pair_kernel<S, 128>, grid, 128, st, d_args, d_tiles, ntiles, k));
+        else
+            DISPATCH_STORE(precision, e = launch_step(batch_pair_kernel<S, 64>, grid, 64, st, d_args, d_tiles, ntiles, k));
+        return e;
+    }
     if (gen)
         DISPATCH_STORE(precision, DISPATCH_NT(nt, e = launch_step(batch_step_kernel<S, NT, true>, grid, NT, st, d_args, d_tiles, ntiles, k)));
     else if (steady_tau1 && nt == kBatchNT)
@@ -143,6 +153,15 @@ int pair_blocks_per_sm(int precision, int nt) {
 // needs no co-residency, so a grid sized for it is valid for every form.
 int batch_blocks_per_sm_f32(int precision, int nt) {
     int n = 0;
+    if (nt < 0) {
+        if (nt == -32)
+            DISPATCH_STORE(precision, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_pair_kernel<S, 32>, 32, 0));
+        else if (nt == -128)
+            DISPATCH_STORE(precision, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_pair_kernel<S, 128>, 128, 0));
+        else
+            DISPATCH_STORE(precision, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_pair_kernel<S, 64>, 64, 0));
+        return n < 1 ? 1 : n;
+    }
     if (nt == kBatchNT)
         DISPATCH_STORE(precision, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_step_kernel<S, kBatchNT, false, kFormSteadyTau1>, kBatchNT, 0));
     else

@@ -282,8 +282,7 @@ __device__ __forceinline__ R cos_of_cell(const CosSrc &cs, long long c, int Lx, 
         const int fj = cs.sy ? (j - cs.sy < 0 ? j - cs.sy + Ly : j - cs.sy) : j;
         return reinterpret_cast<const R *>(cs.cosF)[(long long)fj * Lx + fi];
     }
-    const R th = R(cs.theta0) + R(cs.dtheta) * sinpi_r(R(2) * (R(i) - R(cs.wave_v) * R(cs.t)) / R(Lx));
-    return cospi_r(th);
+    return wave_kap_cos<R>(R(cs.theta0), R(cs.dtheta), R(cs.wave_v), i, cs.t, Lx, 2, 1, R(1)).cs;
 }
 
 template <class R>

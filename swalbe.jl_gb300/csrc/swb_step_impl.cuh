@@ -166,6 +166,29 @@ __device__ __forceinline__ R kappa_of(R theta, int n, int m, R hmin) {
     return a / (R(n - m) * hmin);
 }
 
+// κ and cospi(θ) of column x at iteration t of the moving-wettability wave
+// θ(x, t) = θ0 + Δθ sinpi(2 (x - v t) / Lx).  Not inlined: the kernels
+// evaluate it once per column, and its sinpi / cospi code stays out of their
+// register budget.  Every kernel and the measure reduction use this one
+// function, so they all see the same values.
+template <class R>
+struct KapCos {
+    R kap, cs;
+};
+template <class R>
+__device__ __noinline__ KapCos<R> wave_kap_cos(R theta0, R dtheta, R v, int x, long long t, int Lx,
+                                               int n, int m, R hmin) {
+    const R th = theta0 + dtheta * sinpi_r(R(2) * (R(x) - v * R(t)) / R(Lx));
+    KapCos<R> r;
+    r.kap = kappa_of(th, n, m, hmin);
+    r.cs = cospi_r(th);
+    return r;
+}
+template <class R>
+__device__ __forceinline__ KapCos<R> wave_at(const StepArgs &a, int x, long long t) {
+    return wave_kap_cos<R>(R(a.theta0), R(a.dtheta), R(a.wave_v), x, t, a.Lx, a.n, a.m, R(a.hmin));
+}
+
 // Pull the nine populations of cell (gx, gy) from the post-collision buffer:
 // f_q(x) = fpost_q(x - c_q), c_q as in src/collide.jl:92-100.
 template <class S>
@@ -1124,7 +1147,8 @@ __device__ __forceinline__ void march_run(const StepArgs &a, int bx, int by, lon
     const double corr = (!LIT && !FRESH && a.mass_corr) ? __ldcg(&a.ctl->corr[tt & 1]) : 0.0;
     // kappa and cospi(θ) of this column: constant (scalar θ) or θ(x, t) of
     // the moving-wettability mode, which depends on x only
-    const int mode = GEN ? a.theta_mode : THETA_SCALAR;  // GEN = false: scalar θ
+    // GEN = false: scalar θ or the θ wave (a per-column κ, computed once)
+    const int mode = GEN ? a.theta_mode : (a.theta_mode == THETA_WAVE ? THETA_WAVE : THETA_SCALAR);
     // θ field: column of this thread and row offset in the (possibly moving) field
     int fsx = 0, fsy = 0;
     if (mode == THETA_FIELD) substrate_shift(a, tt, &fsx, &fsy);
@@ -1132,9 +1156,9 @@ __device__ __forceinline__ void march_run(const StepArgs &a, int bx, int by, lon
     auto frow = [&](int gyy) { return fsy ? (gyy - fsy < 0 ? gyy - fsy + Ly : gyy - fsy) : gyy; };
     R kap_col = R(a.kap), cos_col = R(a.cos_theta);
     if (mode == THETA_WAVE) {
-        const R th = R(a.theta0) + R(a.dtheta) * sinpi_r(R(2) * (R(gx) - R(a.wave_v) * R(tt)) / R(Lx));
-        kap_col = kappa_of(th, a.n, a.m, hmin);
-        cos_col = cospi_r(th);
+        const KapCos<R> w = wave_at<R>(a, gx, tt);
+        kap_col = w.kap;
+        cos_col = w.cs;
     }
 
     // pulled populations of the next leading row (prefetch; two in flight in the prologue)
@@ -1265,7 +1289,8 @@ __device__ __forceinline__ void march_run(const StepArgs &a, int bx, int by, lon
 // Iteration done + 1 of strip (bx, by), dispatched on its rare cases: the
 // first iteration after the fields were set (FRESH) and τ = 1 (TAU1).  GEN
 // is chosen per launch by the host (step_general): the common kernel
-// (scalar θ, no thermal noise, no inclination) leaves that code out and so
+// (scalar θ or the θ wave, no thermal noise, no inclination) leaves that
+// code out and so
 // needs fewer registers, which keeps more CTAs per SM.
 template <class S, int NT, bool GEN>
 __device__ __forceinline__ void march_tile(const StepArgs &a, int bx, int by, long long done,
@@ -1285,8 +1310,8 @@ __device__ __forceinline__ void march_tile(const StepArgs &a, int bx, int by, lo
 }
 
 // ------------------------------------------------------------ pair strips
-// The common steady step (FP32 arithmetic, τ = 1, scalar θ, no rare forces)
-// with two adjacent columns per thread.  A CTA of NT threads owns a strip of
+// The common steady step (FP32 arithmetic, τ = 1, scalar θ or the θ wave, no
+// rare forces) with two adjacent columns per thread.  A CTA of NT threads owns a strip of
 // W = 2 NT - 4 columns and H rows; thread t owns columns c = x0 - 2 + 2t and
 // c + 1 for the whole strip.  Lx is even, so c is even: the pair never
 // straddles the periodic boundary, and every plane's pair is one aligned
@@ -1390,13 +1415,24 @@ __device__ __forceinline__ void march2_run(const StepArgs &a, int bx, int by, lo
     void *dst = (done & 1) ? a.fa : a.fb;
     const int x0 = bx * W, y0 = by * H;
     const int rows = min(H, Ly - y0);
-    const R gamma = R(a.gamma), hmin = R(a.hmin), hcrit = R(a.hcrit), kap = R(a.kap);
+    const R gamma = R(a.gamma), hmin = R(a.hmin), hcrit = R(a.hcrit);
     const bool tiny_y = Ly < 3;
     auto wrow = [&](int yy) {
         return tiny_y ? wrapc(yy, Ly) : (yy < 0 ? yy + Ly : (yy >= Ly ? yy - Ly : yy));
     };
     // this thread's pair (c, c + 1); x0 and Lx are even
     const int cx = wrapc(x0 - 2 + 2 * t, Lx);
+    // κ and cospi(θ) of the two columns: the scalar θ, or θ(x, t) of the
+    // moving-wettability wave (depends on x only), as march_run computes them
+    const bool wave = a.theta_mode == THETA_WAVE;
+    R kapA = R(a.kap), kapB = R(a.kap), cosA = R(a.cos_theta), cosB = R(a.cos_theta);
+    if (wave) {
+        const KapCos<R> wA = wave_at<R>(a, cx, tt), wB = wave_at<R>(a, cx + 1, tt);
+        kapA = wA.kap;
+        kapB = wB.kap;
+        cosA = wA.cs;
+        cosB = wB.cs;
+    }
     const bool interior = t >= 1 && t < NT - 1 && x0 - 2 + 2 * t < Lx;
     // lanes 0 / 31: the column and planes of the values from outside the warp
     const bool edge = lane == 0 || lane == 31;
@@ -1473,9 +1509,9 @@ __device__ __forceinline__ void march2_run(const StepArgs &a, int bx, int by, lo
                     *p1 = reinterpret_cast<const float *>(hp);
         // ip = h[i-1,j], jp = h[i,j-1], im = h[i+1,j], jm = h[i,j+1], ...
         const R pA = pressure_cell<false, R>(c.x, c1[tl], m.x, c.y, pl.x, m1[tl], m.y, pl.y, p1[tl],
-                                             kap, gamma, hmin, hcrit, a.n, a.m);
+                                             kapA, gamma, hmin, hcrit, a.n, a.m);
         const R pB = pressure_cell<false, R>(c.y, c.x, m.y, c1[tr], pl.y, m.x, m1[tr], p1[tr], pl.x,
-                                             kap, gamma, hmin, hcrit, a.n, a.m);
+                                             kapB, gamma, hmin, hcrit, a.n, a.m);
         sm.p[r & 3][t] = f2(pA, pB);
     };
 
@@ -1571,10 +1607,12 @@ __device__ __forceinline__ void march2_run(const StepArgs &a, int bx, int by, lo
                 if (wA) {
                     grad9<R>(hc1[tl], hm2.x, h2.y, hp2.x, hm1[tl], hm2.y, hp2.y, hp1[tl], gx2, gy2);
                     area_add(part, R(sqrt(gx2 * gx2 + gy2 * gy2 + R(1))));
+                    if (wave) cos_add(part, cosA);
                 }
                 if (wB) {
                     grad9<R>(h2.x, hm2.y, hc1[tr], hp2.y, hm2.x, hm1[tr], hp1[tr], hp2.x, gx2, gy2);
                     area_add(part, R(sqrt(gx2 * gx2 + gy2 * gy2 + R(1))));
+                    if (wave) cos_add(part, cosB);
                 }
             }
         }
@@ -1587,8 +1625,10 @@ __device__ __forceinline__ void march2_run(const StepArgs &a, int bx, int by, lo
 
 // One iteration of the common steady step on pair strips, plus (when
 // measures are kept and k > 0) the reducer CTA, block 0.
+// (at most 96 registers: 10 CTAs of 64 threads per SM, the budget the wave
+// rule's strip heights were measured with)
 template <class S, int NT>
-__global__ void __launch_bounds__(NT) pair_step_kernel(const StepArgs a, int k) {
+__global__ void __launch_bounds__(NT, 640 / NT) pair_step_kernel(const StepArgs a, int k) {
     __shared__ __align__(16) PairSmem<NT> sm;
     grid_dep_wait();
     int b = blockIdx.x;
@@ -1705,8 +1745,7 @@ __device__ __forceinline__ void tile2d_run(const StepArgs &a, int bx, int by, lo
                     const int gy = wrapc(y0 - 1 + py - fsy, Ly);
                     kap = reinterpret_cast<const R *>(a.kapF)[gy * Lx + wrapc(gx - fsx, Lx)];
                 } else {
-                    const R th = R(a.theta0) + R(a.dtheta) * sinpi_r(R(2) * (R(gx) - R(a.wave_v) * R(tt)) / R(Lx));
-                    kap = kappa_of(th, a.n, a.m, hmin);
+                    kap = wave_at<R>(a, gx, tt).kap;
                 }
             }
             // ip = h[i-1,j], jp = h[i,j-1], im = h[i+1,j], jm = h[i,j+1], ...
@@ -1762,8 +1801,7 @@ __device__ __forceinline__ void tile2d_run(const StepArgs &a, int bx, int by, lo
                     cos_add(part, reinterpret_cast<const R *>(
                                       a.cosF)[wrapc(gy - fsy, Ly) * Lx + wrapc(gx - fsx, Lx)]);
                 } else if (mode == THETA_WAVE) {
-                    const R th = R(a.theta0) + R(a.dtheta) * sinpi_r(R(2) * (R(gx) - R(a.wave_v) * R(tt)) / R(Lx));
-                    cos_add(part, cospi_r(th));
+                    cos_add(part, wave_at<R>(a, gx, tt).cs);
                 }
             }
         }
@@ -1957,8 +1995,11 @@ __global__ void __launch_bounds__(NT) advance_kernel(const StepArgs a, int n) {
 // entries with tx = -1 reduce their lattice's previous iteration.
 // FORM = kFormSteadyTau1 when no lattice is at its first iteration after
 // its fields were set and every lattice has τ = 1 (the host knows both).
+// The steady τ = 1 form is held to 72 registers (14 CTAs of 64 threads per
+// SM), as it compiled before the θ wave joined the common form.
 template <class S, int NT, bool GEN, int FORM = kFormAny>
-__global__ void __launch_bounds__(NT) batch_step_kernel(const StepArgs *__restrict__ args,
+__global__ void __launch_bounds__(NT, (FORM == kFormSteadyTau1 && NT == 64) ? 14 : 1)
+    batch_step_kernel(const StepArgs *__restrict__ args,
                                                         const TileRef *__restrict__ tiles,
                                                         int ntiles, int k) {
     __shared__ MarchSmem<S, NT> sm;
@@ -1975,6 +2016,29 @@ __global__ void __launch_bounds__(NT) batch_step_kernel(const StepArgs *__restri
             else
                 march_tile<S, NT, GEN>(sa, tr.tx, tr.ty, sa.ctl->step_base + k, sm);
         } else if (k > 0)
+            reduce_step<NT>(sa, sa.ctl->step_base + k, sm.redd);
+        __syncthreads();
+    }
+}
+
+// Batch on pair strips: the table's strips are pair strips of NT threads;
+// every lattice is at a steady τ = 1 iteration of the common form (scalar θ
+// or the θ wave) with even Lx (the host knows all three).
+template <class S, int NT>
+__global__ void __launch_bounds__(NT, 640 / NT) batch_pair_kernel(const StepArgs *__restrict__ args,
+                                                                 const TileRef *__restrict__ tiles,
+                                                                 int ntiles, int k) {
+    __shared__ __align__(16) PairSmem<NT> sm;
+    __shared__ StepArgs sa;
+    grid_dep_wait();
+    for (int e = blockIdx.x; e < ntiles; e += gridDim.x) {
+        if (e + (int)gridDim.x >= ntiles) grid_dep_launch();  // this CTA's last entry
+        const TileRef tr = tiles[e];
+        if (threadIdx.x == 0) sa = args[tr.lattice];
+        __syncthreads();
+        if (tr.tx >= 0)
+            march2_run<S, NT>(sa, tr.tx, tr.ty, sa.ctl->step_base + k, sm);
+        else if (k > 0)
             reduce_step<NT>(sa, sa.ctl->step_base + k, sm.redd);
         __syncthreads();
     }
@@ -2074,8 +2138,7 @@ __global__ void pressure_now_kernel(const StepArgs a, double *out) {
             substrate_shift(a, t, &sx, &sy);
             kap = reinterpret_cast<const R *>(a.kapF)[wrapc(j - sy, Ly) * Lx + wrapc(i - sx, Lx)];
         } else
-            kap = kappa_of(R(a.theta0) + R(a.dtheta) * sinpi_r(R(2) * (R(i) - R(a.wave_v) * R(t)) / R(Lx)),
-                           a.n, a.m, R(a.hmin));
+            kap = wave_at<R>(a, i, t).kap;
         out[c] = (double)pressure_cell<S::kLiteral, R>(
             h[c], h[j * Lx + im1], h[jm1 * Lx + i], h[j * Lx + ip1], h[jp1 * Lx + i],
             h[jm1 * Lx + im1], h[jm1 * Lx + ip1], h[jp1 * Lx + ip1], h[jp1 * Lx + im1], kap,

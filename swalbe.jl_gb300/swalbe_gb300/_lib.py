@@ -128,6 +128,7 @@ def lib() -> C.CDLL:
             "swb_batch_step": (i, [p, i64]),
             "swb_batch_sync": (i, [p]),
             "swb_batch_tile": (i, [p, C.POINTER(i), C.POINTER(i), C.POINTER(i)]),
+            "swb_batch_geometry": (i, [p, C.POINTER(i), C.POINTER(i), C.POINTER(i)]),
             "swb_server_create": (i, [C.c_size_t, i, i, C.POINTER(p)]),
             "swb_server_destroy": (i, [p]),
             "swb_server_submit": (i, [p, PP, p, d, d, d, i64, C.POINTER(i64)]),

@@ -774,8 +774,15 @@ class Batch:
         return out
 
     def set_geometry(self, nt: int = 64, rows: int = 32) -> None:
-        """Strips of every lattice: nt threads (nt - 4 columns) x rows."""
+        """Strips of every lattice: nt threads (nt - 4 columns) x rows, or
+        pair strips of -nt threads (2|nt| - 4 columns) for nt = -32, -64, -128."""
         check(lib().swb_batch_set_geometry(self._h, int(nt), int(rows)))
+
+    def geometry(self):
+        """(nt, rows, CTAs per launch) in use; nt < 0: pair strips."""
+        a, b, c = C.c_int(), C.c_int(), C.c_int()
+        check(lib().swb_batch_geometry(self._h, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
 
     def set_theta_wave(self, i: int, theta0: float, dtheta: float, v: float) -> None:
         check(lib().swb_batch_set_theta_wave(self._h, i, theta0, dtheta, v))

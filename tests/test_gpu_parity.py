@@ -367,6 +367,38 @@ def test_batch_matches_single():
         b.close()
 
 
+@pytest.mark.parametrize("T", [np.float32, np.float16])
+def test_batch_pair_strips_equal_single(T):
+    """A batch on pair strips (set, and chosen by the batch tuner), with a
+    θ-wave member, gives each lattice's result alone, bit for bit."""
+    shapes = [(64, 64), (48, 32), (130, 34), (128, 32), (256, 20)]
+    systems = [sysc(Lx, Ly, theta=th) for (Lx, Ly), th in zip(shapes, (1 / 9, 1 / 6, 1 / 12, 1 / 5, 1 / 8))]
+    hs = [droplet(Lx, Ly, min(Lx, Ly) // 4) for (Lx, Ly) in shapes]
+    singles = []
+    for i, (sc, h) in enumerate(zip(systems, hs)):
+        st = sw.Sys(sc, "GB300", T=T)
+        st.height = h
+        if i == 3:
+            st.set_theta_wave(1 / 5, 1 / 36, 1 / 98)
+        st.step(137)
+        singles.append(st.height)
+    for geo in ((-64, 16), None):
+        b = sw.Batch(systems, T=T)
+        if geo:
+            b.set_geometry(*geo)
+        for i, h in enumerate(hs):
+            b.set_height(i, h)
+        b.set_theta_wave(3, 1 / 5, 1 / 36, 1 / 98)
+        b.step(100)
+        b.step(37)
+        b.sync()
+        for i in range(len(shapes)):
+            assert np.array_equal(b.get_height(i), singles[i]), (T, geo, i, b.geometry())
+        if geo:
+            assert b.geometry()[0] == geo[0]
+        b.close()
+
+
 def test_server_alone_equals_mixed():
     import time
     s1 = sysc(64, 64, theta=1 / 8, g=-5e-4)
