@@ -105,6 +105,10 @@ struct StepArgs {
     // cells after every shift_tmove iterations counted from shift_t0
     long long shift_t0;
     int shift_tmove, shift_dx, shift_dy;
+    // batches and the server: iterations after which the lattice stops (its
+    // strips are skipped and its step counter stays there); a served
+    // request's step count, so that ticks need not end when it does
+    long long stop_at;
 };
 
 // Offset of the moving θ field at iteration t (1-based): it has moved

@@ -95,6 +95,7 @@ inline StepArgs lattice_args(const swb_params &p, int precision, char *base, con
     a.records = nullptr;
     a.rec_cap = 0;
     a.meas_mask = 0;
+    a.stop_at = 0x7fffffffffffffffLL;  // runs until told otherwise
     return a;
 }
 

@@ -3,11 +3,15 @@
 // resident solve together (continuous batching: requests that arrive while
 // others run are admitted at the next tick, and finished ones leave).
 //
-// One worker thread owns the GPU stream.  A tick runs `steps_per_tick` time
-// steps (fewer if a resident request finishes sooner) as one batched launch
-// per step over the packed tile table of all resident lattices.  Each
-// lattice's arithmetic is independent of which others share the launch, so
-// a result is bit-identical alone and in the mix.
+// One worker thread owns two streams.  A tick runs up to `steps_per_tick`
+// time steps as one batched launch per step over the packed tile table of
+// all resident lattices; every lattice carries its request's step count and
+// stops there inside the tick, so one short request does not cut the tick
+// for the others.  While a tick runs, the copy stream downloads the results
+// of the requests that finished at the previous tick (and frees their pool
+// memory) and initialises the newly admitted ones, which join at the next
+// tick.  Each lattice's arithmetic is independent of which others share the
+// launch, so a result is bit-identical alone and in the mix.
 //
 // Resident requests advance in lock step, so a request's latency is its
 // step count times the time of one step of the whole resident set.  The
@@ -77,8 +81,11 @@ struct swb_server {
     std::thread worker;
     bool stop = false;
     int64_t next_id = 1;
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;  // the ticks
+    cudaStream_t copy = nullptr;    // admissions and results, beside the ticks
     cudaMemPool_t pool = nullptr;
+    int nt = swb::kBatchNT;         // strip width of served lattices
+    bool fresh_pending = false;     // lattices that joined are at their first iteration
     StepArgs *d_args = nullptr;
     TileRef *d_tiles = nullptr;
     size_t cap_args = 0, cap_tiles = 0;
@@ -104,26 +111,29 @@ void set_error(swb_server *sv, const std::string &m) {
 // budget accounting (which treats it as free again) stays true.
 void release_device(swb_server *sv, Req *r) {
     if (r->dev) {
-        cudaFreeAsync(r->dev, sv->stream);
-        cudaStreamSynchronize(sv->stream);
+        cudaFreeAsync(r->dev, sv->copy);
+        cudaStreamSynchronize(sv->copy);
         r->dev = nullptr;
     }
 }
 
-// Worker-side: allocate and initialise newly admitted requests.
+// Worker-side, on the copy stream (while a tick runs on the compute stream):
+// allocate and initialise a newly admitted request.  Synchronises the copy
+// stream, so the lattice is ready before it joins a tick.
 bool admit_device(swb_server *sv, Req *r) {
-    cudaError_t e = cudaMallocFromPoolAsync((void **)&r->dev, r->bytes, sv->pool, sv->stream);
+    cudaError_t e = cudaMallocFromPoolAsync((void **)&r->dev, r->bytes, sv->pool, sv->copy);
     if (e != cudaSuccess) {
         r->dev = nullptr;
         set_error(sv, std::string("admit: ") + cudaGetErrorString(e));
         return false;
     }
-    r->a = swb::lattice_args(r->p, sv->precision, r->dev, r->L);
+    r->a = swb::lattice_args(r->p, sv->precision, r->dev, r->L, sv->nt, swb::kBatchRows);
     r->a.seed = (unsigned long long)r->id;  // thermal noise stream of this request
+    r->a.stop_at = r->nsteps;  // its strips stop there, whatever the tick length
     swb::set_wave(r->a, r->theta0, r->dtheta, r->v);
     const long long N = (long long)r->p.Lx * r->p.Ly;
     if ((size_t)N > sv->staging_elems) {
-        cudaStreamSynchronize(sv->stream);
+        cudaStreamSynchronize(sv->copy);
         cudaFree(sv->staging);
         sv->staging = nullptr;
         if (cudaMalloc((void **)&sv->staging, (size_t)N * 8) != cudaSuccess) {
@@ -135,9 +145,9 @@ bool admit_device(swb_server *sv, Req *r) {
         }
         sv->staging_elems = N;
     }
-    e = swb::lattice_init(r->a, sv->precision, r->L, r->h0.data(), sv->stream);
-    if (e == cudaSuccess) e = swb::lattice_upload_height(r->a, sv->precision, r->h0.data(), sv->staging, sv->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(sv->stream);
+    e = swb::lattice_init(r->a, sv->precision, r->L, r->h0.data(), sv->copy);
+    if (e == cudaSuccess) e = swb::lattice_upload_height(r->a, sv->precision, r->h0.data(), sv->staging, sv->copy);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(sv->copy);
     if (e != cudaSuccess) {
         release_device(sv, r);
         set_error(sv, std::string("admit: ") + cudaGetErrorString(e));
@@ -180,17 +190,25 @@ int count_tiles(swb_server *sv) {
     return n;
 }
 
+// Tile tables of the resident set: the strips of every lattice (pair strips
+// when every lattice allows them) and, for pair strips, the one-column
+// strips of the iterations the pair form leaves out.
 void worker_main(swb_server *sv) {
     cudaSetDevice(sv->device);
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, sv->device);
     const int occ = swb::batch_blocks_per_sm(sv->precision, swb::kBatchNT);
+    std::vector<Req *> joining;  // initialised on the copy stream; join at the next tick
+    std::vector<Req *> leaving;  // finished at the last tick; results still to download
+    bool changed = false;
     for (;;) {
         std::vector<Req *> admitted;
-        bool changed = false;
         {
             std::unique_lock<std::mutex> lk(sv->mu);
-            sv->cv.wait(lk, [&] { return sv->stop || !sv->queue.empty() || !sv->active.empty(); });
+            sv->cv.wait(lk, [&] {
+                return sv->stop || !sv->queue.empty() || !sv->active.empty() || !joining.empty() ||
+                       !leaving.empty();
+            });
             if (sv->stop) break;
             // drop cancelled residents
             for (auto it = sv->active.begin(); it != sv->active.end();) {
@@ -233,7 +251,7 @@ void worker_main(swb_server *sv) {
                 }
                 const int64_t cells = (int64_t)r->p.Lx * r->p.Ly;
                 if (sv->in_use + r->bytes > sv->budget) break;
-                const bool alone = sv->active.empty() && admitted.empty();
+                const bool alone = sv->active.empty() && admitted.empty() && joining.empty();
                 if (sv->max_cells > 0 && sv->resident_cells + cells > sv->max_cells && !alone) break;
                 sv->queue.erase(pick);
                 sv->in_use += r->bytes;
@@ -244,13 +262,56 @@ void worker_main(swb_server *sv) {
                 sv->st.admitted++;
             }
         }
-        bool fresh_new = false;  // admitted lattices are at their first iteration
+        // 1. the tick: every resident request advances together (a request
+        // whose steps run out stops inside the tick; the tick is as long as
+        // the longest remaining request allows, at most steps_per_tick)
+        if (changed && !sv->active.empty() && !upload_table(sv)) {
+            set_error(sv, "tile table upload failed");
+            std::this_thread::sleep_for(std::chrono::milliseconds(10));
+            continue;
+        }
+        changed = false;
+        int64_t tick = 0;
+        for (Req *r : sv->active) tick = std::max<int64_t>(tick, r->nsteps - r->done);
+        tick = std::min<int64_t>(tick, sv->steps_per_tick);
+        const double tb = sv->now();
+        cudaError_t e = cudaSuccess;
+        if (tick > 0) {
+            const int ntiles = count_tiles(sv);
+            const int grid = std::min(ntiles, sms * occ);
+            bool gen = false, tau1 = true;  // the general kernel if any resident request needs it
+            for (Req *r : sv->active) {
+                gen = gen || swb::step_general(r->a);
+                tau1 = tau1 && r->a.tau_is_one;
+            }
+            for (int64_t k = 0; k < tick && e == cudaSuccess; ++k)
+                e = swb::launch_batch_step(sv->precision, swb::kBatchNT, gen,
+                                           tau1 && !(sv->fresh_pending && k == 0), sv->d_args,
+                                           sv->d_tiles, ntiles, grid, (int)k, sv->stream);
+            if (e == cudaSuccess)
+                e = swb::launch_batch_advance(sv->d_args, (int)sv->active.size(), (int)tick, sv->stream);
+            sv->fresh_pending = false;
+        }
+        // 2. while it runs, on the copy stream: the results of the requests
+        // that finished at the previous tick, then the new admissions
+        for (Req *r : leaving) {
+            r->result.resize((size_t)r->p.Lx * r->p.Ly);
+            cudaError_t de = swb::lattice_download_height(r->a, sv->precision, false, r->result.data(), sv->copy);
+            cudaFreeAsync(r->dev, sv->copy);
+            r->dev = nullptr;
+            std::lock_guard<std::mutex> g(sv->mu);
+            r->status = de == cudaSuccess ? 2 : SWB_ERR_CUDA;
+            r->t_done = sv->now();
+            sv->in_use -= r->bytes;
+            sv->resident_cells -= (int64_t)r->p.Lx * r->p.Ly;
+            sv->st.completed++;
+            r->h0.clear();
+            r->h0.shrink_to_fit();
+        }
+        leaving.clear();
         for (Req *r : admitted) {
             if (admit_device(sv, r)) {
-                std::lock_guard<std::mutex> g(sv->mu);
-                sv->active.push_back(r);
-                changed = true;
-                fresh_new = true;
+                joining.push_back(r);
             } else {
                 std::lock_guard<std::mutex> g(sv->mu);
                 r->status = SWB_ERR_OOM;
@@ -260,70 +321,42 @@ void worker_main(swb_server *sv) {
                 sv->st.rejected++;
             }
         }
-        if (sv->active.empty()) continue;
-        if (changed && !upload_table(sv)) {
-            set_error(sv, "tile table upload failed");
-            std::this_thread::sleep_for(std::chrono::milliseconds(10));
-            continue;
-        }
-        int64_t tick = sv->steps_per_tick;
-        for (Req *r : sv->active) tick = std::min<int64_t>(tick, r->nsteps - r->done);
-        const int ntiles = count_tiles(sv);
-        const int grid = std::min(ntiles, sms * occ);
-        const double tb = sv->now();
-        cudaError_t e = cudaSuccess;
-        bool gen = false, tau1 = true;  // the general kernel if any resident request needs it
-        for (Req *r : sv->active) {
-            gen = gen || swb::step_general(r->a);
-            tau1 = tau1 && r->a.tau_is_one;
-        }
-        for (int64_t k = 0; k < tick && e == cudaSuccess; ++k)
-            e = swb::launch_batch_step(sv->precision, swb::kBatchNT, gen,
-                                       tau1 && !(fresh_new && k == 0), sv->d_args, sv->d_tiles,
-                                       ntiles, grid, (int)k, sv->stream);
-        if (e == cudaSuccess)
-            e = swb::launch_batch_advance(sv->d_args, (int)sv->active.size(), (int)tick, sv->stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(sv->stream);
-        double lu = 0.0;
-        std::vector<Req *> finished;
+        // 3. the end of the tick
+        if (tick > 0 && e == cudaSuccess) e = cudaStreamSynchronize(sv->stream);
         {
             std::lock_guard<std::mutex> g(sv->mu);
+            double lu = 0.0;
             for (Req *r : sv->active) {
-                r->done += tick;
-                lu += (double)r->p.Lx * r->p.Ly * (double)tick;
-                if (r->done >= r->nsteps) finished.push_back(r);
+                const int64_t n = std::min<int64_t>(tick, r->nsteps - r->done);
+                r->done += n;
+                lu += (double)r->p.Lx * r->p.Ly * (double)n;
+                if (r->done >= r->nsteps) {
+                    leaving.push_back(r);
+                    if (e != cudaSuccess) r->status = SWB_ERR_CUDA;
+                }
             }
-        }
-        for (Req *r : finished) {
-            r->result.resize((size_t)r->p.Lx * r->p.Ly);
-            cudaError_t de = swb::lattice_download_height(r->a, sv->precision, false, r->result.data(), sv->stream);
-            cudaFreeAsync(r->dev, sv->stream);
-            r->dev = nullptr;
-            std::lock_guard<std::mutex> g(sv->mu);
-            r->status = (e == cudaSuccess && de == cudaSuccess) ? 2 : SWB_ERR_CUDA;
-            r->t_done = sv->now();
-            sv->in_use -= r->bytes;
-            sv->resident_cells -= (int64_t)r->p.Lx * r->p.Ly;
-            sv->st.completed++;
-            r->h0.clear();
-            r->h0.shrink_to_fit();
-        }
-        {
-            std::lock_guard<std::mutex> g(sv->mu);
-            if (!finished.empty()) {
+            if (!leaving.empty()) {
                 sv->active.erase(std::remove_if(sv->active.begin(), sv->active.end(),
-                                                [](Req *r) { return r->status != 1; }),
+                                                [](Req *r) { return r->done >= r->nsteps; }),
                                  sv->active.end());
                 changed = true;
             }
+            if (!joining.empty()) {
+                sv->active.insert(sv->active.end(), joining.begin(), joining.end());
+                joining.clear();
+                sv->fresh_pending = true;
+                changed = true;
+            }
             sv->st.lattice_updates += lu;
-            sv->st.busy_seconds += sv->now() - tb;
-            sv->st.ticks++;
+            if (tick > 0) {
+                sv->st.busy_seconds += sv->now() - tb;
+                sv->st.ticks++;
+            }
             if (e != cudaSuccess) sv->err = std::string("tick: ") + cudaGetErrorString(e);
         }
-        if (!finished.empty() && !sv->active.empty()) upload_table(sv);
     }
     cudaStreamSynchronize(sv->stream);
+    cudaStreamSynchronize(sv->copy);
 }
 
 }  // namespace
@@ -345,6 +378,7 @@ int swb_server_create(size_t hbm_budget, int precision, int steps_per_tick, swb_
     props.location.type = cudaMemLocationTypeDevice;
     props.location.id = sv->device;
     cudaError_t e = cudaStreamCreateWithFlags(&sv->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&sv->copy, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMemPoolCreate(&sv->pool, &props);
     if (e == cudaSuccess) {
         uint64_t thr = UINT64_MAX;  // keep freed blocks cached in this pool
@@ -352,6 +386,7 @@ int swb_server_create(size_t hbm_budget, int precision, int steps_per_tick, swb_
     }
     if (e != cudaSuccess) {
         if (sv->stream) cudaStreamDestroy(sv->stream);
+        if (sv->copy) cudaStreamDestroy(sv->copy);
         delete sv;
         return sfail(SWB_ERR_CUDA, std::string("server create: ") + cudaGetErrorString(e));
     }
@@ -369,6 +404,7 @@ int swb_server_destroy(swb_server *sv) {
     }
     sv->cv.notify_all();
     if (sv->worker.joinable()) sv->worker.join();
+    cudaStreamSynchronize(sv->copy);
     for (auto &kv : sv->reqs)
         if (kv.second->dev) cudaFreeAsync(kv.second->dev, sv->stream);
     cudaStreamSynchronize(sv->stream);
@@ -377,6 +413,7 @@ int swb_server_destroy(swb_server *sv) {
     cudaFree(sv->staging);
     if (sv->pool) cudaMemPoolDestroy(sv->pool);
     cudaStreamDestroy(sv->stream);
+    cudaStreamDestroy(sv->copy);
     delete sv;
     return SWB_OK;
 }

@@ -2010,13 +2010,15 @@ __global__ void __launch_bounds__(NT, (FORM == kFormSteadyTau1 && NT == 64) ? 14
         const TileRef tr = tiles[e];
         if (threadIdx.x == 0) sa = args[tr.lattice];
         __syncthreads();
+        const long long done = sa.ctl->step_base + k;
         if (tr.tx >= 0) {
-            if constexpr (FORM == kFormSteadyTau1)
-                march_run<S, NT, false, true, GEN>(sa, tr.tx, tr.ty, sa.ctl->step_base + k, sm);
+            if (done >= sa.stop_at) {  // the lattice has stopped
+            } else if constexpr (FORM == kFormSteadyTau1)
+                march_run<S, NT, false, true, GEN>(sa, tr.tx, tr.ty, done, sm);
             else
-                march_tile<S, NT, GEN>(sa, tr.tx, tr.ty, sa.ctl->step_base + k, sm);
-        } else if (k > 0)
-            reduce_step<NT>(sa, sa.ctl->step_base + k, sm.redd);
+                march_tile<S, NT, GEN>(sa, tr.tx, tr.ty, done, sm);
+        } else if (k > 0 && done <= sa.stop_at)
+            reduce_step<NT>(sa, done, sm.redd);
         __syncthreads();
     }
 }
@@ -2036,10 +2038,12 @@ __global__ void __launch_bounds__(NT, 640 / NT) batch_pair_kernel(const StepArgs
         const TileRef tr = tiles[e];
         if (threadIdx.x == 0) sa = args[tr.lattice];
         __syncthreads();
-        if (tr.tx >= 0)
-            march2_run<S, NT>(sa, tr.tx, tr.ty, sa.ctl->step_base + k, sm);
-        else if (k > 0)
-            reduce_step<NT>(sa, sa.ctl->step_base + k, sm.redd);
+        const long long done = sa.ctl->step_base + k;
+        if (tr.tx >= 0) {
+            if (done < sa.stop_at) march2_run<S, NT>(sa, tr.tx, tr.ty, done, sm);
+        } else if (k > 0 && done <= sa.stop_at) {
+            reduce_step<NT>(sa, done, sm.redd);
+        }
         __syncthreads();
     }
 }
@@ -2054,10 +2058,12 @@ __global__ void __launch_bounds__(NT) batch_advance_kernel(const StepArgs *__res
     grid_dep_launch();
     if (threadIdx.x == 0) sa = args[blockIdx.x];
     __syncthreads();
+    // a lattice that stopped during the sequence had its last iteration
+    // reduced by the launch after it
     const long long s = sa.ctl->step_base + n;
-    if (needs_partials(sa) && n > 0) reduce_step<NT>(sa, s, redd);
+    if (needs_partials(sa) && n > 0 && s <= sa.stop_at) reduce_step<NT>(sa, s, redd);
     __syncthreads();
-    if (threadIdx.x == 0) sa.ctl->step_base = s;
+    if (threadIdx.x == 0) sa.ctl->step_base = s < sa.stop_at ? s : sa.stop_at;
 }
 
 // thermal!(fx, fy, h, kbt, mu, delta) of the current height field for

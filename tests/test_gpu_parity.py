@@ -411,11 +411,22 @@ def test_server_alone_equals_mixed():
     time.sleep(0.01)
     rid2 = sv.submit(s1, h1, 330, dtheta=1 / 36, v=1 / 98)
     mixed = _wait(sv, rid2, (64, 64))
-    for o in others:
-        _wait(sv, o, None)
+    outs = [_wait(sv, o, (L_, L_)) for o, L_ in zip(others, (128, 64, 192, 32))]
     assert np.array_equal(alone, mixed)
     st = sv.stats()
     assert st.completed == 6 and st.rejected == 0
+    # the ticks are 50 steps, the requests 330 and 200 + 37 k: each stops
+    # inside a tick, at exactly its own step count, like a solve run alone
+    single = sw.Sys(s1, "GB300", T=np.float32)
+    single.height = h1
+    single.set_theta_wave(1 / 8, 1 / 36, 1 / 98)
+    single.step(330)
+    assert np.array_equal(alone, single.height)
+    for k, (L_, out) in enumerate(zip((128, 64, 192, 32), outs)):
+        st1 = sw.Sys(sysc(L_, L_), "GB300", T=np.float32)
+        st1.height = rough(L_, L_, k)
+        st1.step(200 + 37 * k)
+        assert np.array_equal(out, st1.height), L_
     sv.close()
 
 
