@@ -456,7 +456,7 @@ def side_runs(sw, L, np, torch, hbm):
     return out
 
 
-def ensemble_run(sw, np, count=512, steps=200, plain_sample=8):
+def ensemble_run(sw, np, count=512, steps=200, plain_sample=8, geometry=""):
     """Coalescence ensemble: `count` two-cap lattices (128², 256², 512²,
     1024x256) advanced together in FP32 by the batch kernel, against the
     plain one-at-a-time paths on a sample of the same instances."""
@@ -465,6 +465,8 @@ def ensemble_run(sw, np, count=512, steps=200, plain_sample=8):
     systems = [m.sysc for m in members]
     cells = sum(s.Lx * s.Ly for s in systems)
     b = sw.Batch(systems, T=np.float32)
+    if geometry:  # a fixed strip geometry (the tuner then picks only the CTA count)
+        b.set_geometry(*(int(v) for v in geometry.split(",")))
     for i, m in enumerate(members):
         b.set_height(i, m.h0)
     b.step(40)  # includes the autotuning probes
@@ -641,7 +643,7 @@ def run_workload(args):
         print(json.dumps({"workload": "lattice_2048", **r}), flush=True)
         return
     if args.workload == "ensemble":
-        r = ensemble_run(sw, np)
+        r = ensemble_run(sw, np, geometry=args.geometry)
         line = {"metric": "MLUPS", "value": r["batch_f32"]["MLUPS"], "unit": "MLUPS",
                 "workload": "ensemble", **r}
     else:

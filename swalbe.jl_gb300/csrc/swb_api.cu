@@ -700,7 +700,7 @@ int autotune_geometry(swb_state *s, long long &left) {
     const bool multi_ok = s->precision == SWB_F32 || s->precision == SWB_F16;
     // pair strips: FP32 arithmetic, even Lx, and only the common steady τ = 1
     // step has that form (others would time the one-column fallback)
-    const bool pair_ok = multi_ok && s->p.Lx % 2 == 0 && s->a.tau_is_one && !swb::step_general(s->a);
+    const bool pair_ok = multi_ok && s->p.Lx % 2 == 0 && swb::pair_form_ok(s->a);
     std::vector<std::array<int, 3>> todo;
     for (auto &c : all) todo.push_back({c[0], c[1], c[2]});
     if (pair_ok && s->mode != SWB_STEP_MULTI) {  // and the wave rule's rows

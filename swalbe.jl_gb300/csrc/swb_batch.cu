@@ -167,6 +167,7 @@ struct swb_batch {
     int grid = 0;
     int nt = swb::kBatchNT, rows = swb::kBatchRows;  // strip geometry of every lattice
     bool tuned = false, args_dirty = true, gvalid = false;
+    bool geometry_fixed = false;  // set by the caller: the tuner picks only the CTA count
     bool fresh_pending = true;  // a lattice's next iteration takes h, u from its fields
     long long steps = 0;
     std::string err;
@@ -287,16 +288,21 @@ bool pair_possible(const swb_batch *b) {
 // at any time.
 cudaError_t batch_sequence(swb_batch *b, int n, int grid) {
     cudaError_t e = cudaSuccess;
-    bool gen = false, tau1 = true;  // the general kernel if any lattice needs it
+    bool gen = false, tau1 = true, pair = true, wave = false;  // the general kernel if any lattice needs it
     for (const StepArgs &a : b->args) {
         gen = gen || swb::step_general(a);
         tau1 = tau1 && a.tau_is_one;
+        pair = pair && swb::pair_form_ok(a);
+        wave = wave || a.theta_mode == swb::THETA_WAVE;
     }
     for (int k = 0; k < n && e == cudaSuccess; ++k) {
         const bool steady = tau1 && !(b->fresh_pending && k == 0);
-        if (b->nt < 0 && (gen || !steady))  // an iteration the pair form leaves out
+        if (b->nt < 0 && !(pair && steady))  // an iteration the pair form leaves out
             e = swb::launch_batch_step(b->precision, 64, gen, steady, b->d_args_fb, b->d_tiles_fb,
                                        b->ntiles_fb, grid, k, b->stream);
+        else if (b->nt < 0)
+            e = swb::launch_batch_step(b->precision, b->nt, wave, steady, b->d_args, b->d_tiles,
+                                       b->ntiles, grid, k, b->stream);
         else
             e = swb::launch_batch_step(b->precision, b->nt, gen, steady, b->d_args, b->d_tiles,
                                        b->ntiles, grid, k, b->stream);
@@ -319,19 +325,15 @@ int autotune(swb_batch *b, long long &left) {
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    bool gen = false, tau1 = true;
-    for (const StepArgs &a : b->args) {
-        gen = gen || swb::step_general(a);
-        tau1 = tau1 && a.tau_is_one;
-    }
+    bool pair = true;
+    for (const StepArgs &a : b->args) pair = pair && swb::pair_form_ok(a);
     std::vector<std::array<int, 2>> geos = {{64, 32}, {64, 16}, {128, 16}};
-    if (pair_possible(b) && !gen && tau1) {
+    if (pair_possible(b) && pair) {
         geos.push_back({-64, 16});
         geos.push_back({-64, 32});
         geos.push_back({-32, 16});
     }
-    if (b->nt != swb::kBatchNT || b->rows != swb::kBatchRows)  // a geometry set by the caller
-        geos = {{b->nt, b->rows}};
+    if (b->geometry_fixed) geos = {{b->nt, b->rows}};  // a geometry set by the caller
     const int probe = 2;
     struct Best {
         float ms = 1e30f;
@@ -563,6 +565,7 @@ int swb_batch_set_geometry(swb_batch *b, int nt, int rows) {
                           "batch pair strips: FP32 or FP16 storage and even Lx in every lattice");
     const int rc = apply_geometry(b, nt, rows);
     if (rc) return rc;
+    b->geometry_fixed = true;
     b->tuned = false;  // re-pick the CTA count (the tuner keeps this geometry)
     return SWB_OK;
 }

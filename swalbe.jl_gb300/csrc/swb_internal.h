@@ -180,11 +180,16 @@ struct TileRef {
     int tx, ty;
 };
 
-// Whether a lattice's step needs the general kernel (θ field, thermal
-// noise, inclination) rather than the common one (scalar θ or the θ wave,
-// whose κ depends on the column only).
+// Whether a lattice's step needs the general kernel (θ field or wave,
+// thermal noise, inclination) rather than the common one.
 inline bool step_general(const StepArgs &a) {
-    return a.thermal || a.incl || a.theta_mode == THETA_FIELD;
+    return a.thermal || a.incl || a.theta_mode != THETA_SCALAR;
+}
+// Whether a steady iteration of `a` has a pair-strip kernel: τ = 1, no rare
+// forces, scalar θ or the θ wave (a per-column κ; the pair kernel's WAVE
+// variant).
+inline bool pair_form_ok(const StepArgs &a) {
+    return a.tau_is_one && !a.thermal && !a.incl && a.theta_mode != THETA_FIELD;
 }
 
 // Whether the step kernels of a lattice produce per-step partial measures.
@@ -234,7 +239,8 @@ cudaError_t launch_thermal_field_f64(const StepArgs &a, long long t, double *fx,
                                      cudaStream_t st);
 cudaError_t launch_thermal_field_f32(int precision, const StepArgs &a, long long t, double *fx,
                                      double *fy, cudaStream_t st);
-// gen: some lattice of the batch needs the general kernel (step_general).
+// gen: some lattice of the batch needs the general kernel (step_general);
+// with pair strips (nt < 0): some lattice has the θ wave.
 // steady_tau1: no lattice is at its first iteration after its fields were
 // set and every lattice has τ = 1 (the steady batch form may run it)
 cudaError_t launch_batch_step(int precision, int nt, bool gen, bool steady_tau1,
@@ -267,9 +273,7 @@ int resident_blocks_per_sm(int precision, int h);
 cudaError_t launch_resident_run(int precision, const StepArgs &a, int n, cudaStream_t st);
 // Whether iterations of `a` may run as resident tiles (the common steady
 // τ = 1 step with scalar θ of an FP32-arithmetic lattice).
-inline bool resident_ok(const StepArgs &a) {
-    return a.tau_is_one && !step_general(a) && a.theta_mode == THETA_SCALAR;
-}
+inline bool resident_ok(const StepArgs &a) { return a.tau_is_one && !step_general(a); }
 // Resident CTAs per SM of the pair-strip kernel (FP32 / FP16 storage).
 int pair_blocks_per_sm(int precision, int nt);
 // Rows per pair strip for a lattice: the strip march takes about the same

@@ -3,6 +3,8 @@
 // single-lattice and batch kernels, which inline the same step code, round
 // identically; parity with the Float64 oracle is checked against stated
 // tolerances.
+#include <type_traits>
+
 #include "swb_step_impl.cuh"
 
 namespace swb {
@@ -58,16 +60,23 @@ cudaError_t launch_fused_step_f32(int precision, const StepArgs &a, int k, bool 
     if (a.march_nt == kResGeom)  // one iteration at a time: strips of the same rows
         return launch_fused_step_f32(precision, strip_fallback(a), k, steady, st);
     if (a.march_nt < 0) {
-        if (!(steady && a.tau_is_one && !step_general(a)))
+        if (!(steady && pair_form_ok(a)))
             return launch_fused_step_f32(precision, pair_fallback(a), k, steady, st);
         const int grid = step_grid(a, k);
         cudaError_t e = cudaSuccess;
-        if (a.march_nt == -32)
-            DISPATCH_STORE(precision, e = launch_step(pair_step_kernel<S, 32>, grid, 32, st, a, k));
-        else if (a.march_nt == -128)
-            DISPATCH_STORE(precision, e = launch_step(pair_step_kernel<S, 128>, grid, 128, st, a, k));
+        auto go = [&](auto wave) {
+            constexpr bool W = decltype(wave)::value;
+            if (a.march_nt == -32)
+                DISPATCH_STORE(precision, e = launch_step(pair_step_kernel<S, 32, W>, grid, 32, st, a, k));
+            else if (a.march_nt == -128)
+                DISPATCH_STORE(precision, e = launch_step(pair_step_kernel<S, 128, W>, grid, 128, st, a, k));
+            else
+                DISPATCH_STORE(precision, e = launch_step(pair_step_kernel<S, 64, W>, grid, 64, st, a, k));
+        };
+        if (a.theta_mode == THETA_WAVE)
+            go(std::true_type{});
         else
-            DISPATCH_STORE(precision, e = launch_step(pair_step_kernel<S, 64>, grid, 64, st, a, k));
+            go(std::false_type{});
         return e;
     }
     const int grid = step_grid(a, k);
@@ -117,14 +126,21 @@ cudaError_t launch_batch_step_f32(int precision, int nt, bool gen, bool steady_t
                                   const StepArgs *d_args, const TileRef *d_tiles, int ntiles,
                                   int grid, int k, cudaStream_t st) {
     cudaError_t e = cudaSuccess;
-    if (nt < 0) {  // pair strips: the caller passes their table only for steady common steps
-        if (gen || !steady_tau1) return cudaErrorInvalidValue;
-        if (nt == -32)
-            DISPATCH_STORE(precision, e = launch_step(batch_pair_kernel<S, 32>, grid, 32, st, d_args, d_tiles, ntiles, k));
-        else if (nt == -128)
-            DISPATCH_STORE(precision, e = launch_step(batch_pair_kernel<S, 128>, grid, 128, st, d_args, d_tiles, ntiles, k));
+    if (nt < 0) {  // pair strips: the caller passes their table only for steady steps they have
+        if (!steady_tau1) return cudaErrorInvalidValue;
+        auto go = [&](auto wave) {
+            constexpr bool W = decltype(wave)::value;
+            if (nt == -32)
+                DISPATCH_STORE(precision, e = launch_step(batch_pair_kernel<S, 32, W>, grid, 32, st, d_args, d_tiles, ntiles, k));
+            else if (nt == -128)
+                DISPATCH_STORE(precision, e = launch_step(batch_pair_kernel<S, 128, W>, grid, 128, st, d_args, d_tiles, ntiles, k));
+            else
+                DISPATCH_STORE(precision, e = launch_step(batch_pair_kernel<S, 64, W>, grid, 64, st, d_args, d_tiles, ntiles, k));
+        };
+        if (gen)
+            go(std::true_type{});
         else
-            DISPATCH_STORE(precision, e = launch_step(batch_pair_kernel<S, 64>, grid, 64, st, d_args, d_tiles, ntiles, k));
+            go(std::false_type{});
         return e;
     }
     if (gen)
@@ -140,11 +156,11 @@ cudaError_t launch_batch_step_f32(int precision, int nt, bool gen, bool steady_t
 int pair_blocks_per_sm(int precision, int nt) {
     int n = 0;
     if (nt == -32)
-        DISPATCH_STORE(precision, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pair_step_kernel<S, 32>, 32, 0));
+        DISPATCH_STORE(precision, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pair_step_kernel<S, 32, false>, 32, 0));
     else if (nt == -128)
-        DISPATCH_STORE(precision, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pair_step_kernel<S, 128>, 128, 0));
+        DISPATCH_STORE(precision, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pair_step_kernel<S, 128, false>, 128, 0));
     else
-        DISPATCH_STORE(precision, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pair_step_kernel<S, 64>, 64, 0));
+        DISPATCH_STORE(precision, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, pair_step_kernel<S, 64, false>, 64, 0));
     return n < 1 ? 1 : n;
 }
 
@@ -155,11 +171,11 @@ int batch_blocks_per_sm_f32(int precision, int nt) {
     int n = 0;
     if (nt < 0) {
         if (nt == -32)
-            DISPATCH_STORE(precision, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_pair_kernel<S, 32>, 32, 0));
+            DISPATCH_STORE(precision, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_pair_kernel<S, 32, false>, 32, 0));
         else if (nt == -128)
-            DISPATCH_STORE(precision, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_pair_kernel<S, 128>, 128, 0));
+            DISPATCH_STORE(precision, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_pair_kernel<S, 128, false>, 128, 0));
         else
-            DISPATCH_STORE(precision, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_pair_kernel<S, 64>, 64, 0));
+            DISPATCH_STORE(precision, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_pair_kernel<S, 64, false>, 64, 0));
         return n < 1 ? 1 : n;
     }
     if (nt == kBatchNT)

@@ -1147,8 +1147,7 @@ __device__ __forceinline__ void march_run(const StepArgs &a, int bx, int by, lon
     const double corr = (!LIT && !FRESH && a.mass_corr) ? __ldcg(&a.ctl->corr[tt & 1]) : 0.0;
     // kappa and cospi(θ) of this column: constant (scalar θ) or θ(x, t) of
     // the moving-wettability mode, which depends on x only
-    // GEN = false: scalar θ or the θ wave (a per-column κ, computed once)
-    const int mode = GEN ? a.theta_mode : (a.theta_mode == THETA_WAVE ? THETA_WAVE : THETA_SCALAR);
+    const int mode = GEN ? a.theta_mode : THETA_SCALAR;  // GEN = false: scalar θ
     // θ field: column of this thread and row offset in the (possibly moving) field
     int fsx = 0, fsy = 0;
     if (mode == THETA_FIELD) substrate_shift(a, tt, &fsx, &fsy);
@@ -1289,8 +1288,7 @@ __device__ __forceinline__ void march_run(const StepArgs &a, int bx, int by, lon
 // Iteration done + 1 of strip (bx, by), dispatched on its rare cases: the
 // first iteration after the fields were set (FRESH) and τ = 1 (TAU1).  GEN
 // is chosen per launch by the host (step_general): the common kernel
-// (scalar θ or the θ wave, no thermal noise, no inclination) leaves that
-// code out and so
+// (scalar θ, no thermal noise, no inclination) leaves that code out and so
 // needs fewer registers, which keeps more CTAs per SM.
 template <class S, int NT, bool GEN>
 __device__ __forceinline__ void march_tile(const StepArgs &a, int bx, int by, long long done,
@@ -1310,8 +1308,8 @@ __device__ __forceinline__ void march_tile(const StepArgs &a, int bx, int by, lo
 }
 
 // ------------------------------------------------------------ pair strips
-// The common steady step (FP32 arithmetic, τ = 1, scalar θ or the θ wave, no
-// rare forces) with two adjacent columns per thread.  A CTA of NT threads owns a strip of
+// The steady step (FP32 arithmetic, τ = 1, no rare forces; scalar θ, or with
+// WAVE the moving-wettability θ wave) with two adjacent columns per thread.  A CTA of NT threads owns a strip of
 // W = 2 NT - 4 columns and H rows; thread t owns columns c = x0 - 2 + 2t and
 // c + 1 for the whole strip.  Lx is even, so c is even: the pair never
 // straddles the periodic boundary, and every plane's pair is one aligned
@@ -1399,7 +1397,7 @@ __device__ __forceinline__ __half shfl_lo_down(__half2 w) {
     return __low2half(__shfl_down_sync(0xffffffffu, w, 1));
 }
 
-template <class S, int NT>
+template <class S, int NT, bool WAVE>
 __device__ __forceinline__ void march2_run(const StepArgs &a, int bx, int by, long long done,
                                            PairSmem<NT> &sm) {
     static_assert(!S::kLiteral && NT % 32 == 0, "pair strips: FP32 arithmetic, whole warps");
@@ -1424,9 +1422,9 @@ __device__ __forceinline__ void march2_run(const StepArgs &a, int bx, int by, lo
     const int cx = wrapc(x0 - 2 + 2 * t, Lx);
     // κ and cospi(θ) of the two columns: the scalar θ, or θ(x, t) of the
     // moving-wettability wave (depends on x only), as march_run computes them
-    const bool wave = a.theta_mode == THETA_WAVE;
+    constexpr bool wave = WAVE;
     R kapA = R(a.kap), kapB = R(a.kap), cosA = R(a.cos_theta), cosB = R(a.cos_theta);
-    if (wave) {
+    if constexpr (WAVE) {
         const KapCos<R> wA = wave_at<R>(a, cx, tt), wB = wave_at<R>(a, cx + 1, tt);
         kapA = wA.kap;
         kapB = wB.kap;
@@ -1607,12 +1605,12 @@ __device__ __forceinline__ void march2_run(const StepArgs &a, int bx, int by, lo
                 if (wA) {
                     grad9<R>(hc1[tl], hm2.x, h2.y, hp2.x, hm1[tl], hm2.y, hp2.y, hp1[tl], gx2, gy2);
                     area_add(part, R(sqrt(gx2 * gx2 + gy2 * gy2 + R(1))));
-                    if (wave) cos_add(part, cosA);
+                    if constexpr (wave) cos_add(part, cosA);
                 }
                 if (wB) {
                     grad9<R>(h2.x, hm2.y, hc1[tr], hp2.y, hm2.x, hm1[tr], hp1[tr], hp2.x, gx2, gy2);
                     area_add(part, R(sqrt(gx2 * gx2 + gy2 * gy2 + R(1))));
-                    if (wave) cos_add(part, cosB);
+                    if constexpr (wave) cos_add(part, cosB);
                 }
             }
         }
@@ -1625,10 +1623,8 @@ __device__ __forceinline__ void march2_run(const StepArgs &a, int bx, int by, lo
 
 // One iteration of the common steady step on pair strips, plus (when
 // measures are kept and k > 0) the reducer CTA, block 0.
-// (at most 96 registers: 10 CTAs of 64 threads per SM, the budget the wave
-// rule's strip heights were measured with)
-template <class S, int NT>
-__global__ void __launch_bounds__(NT, 640 / NT) pair_step_kernel(const StepArgs a, int k) {
+template <class S, int NT, bool WAVE>
+__global__ void __launch_bounds__(NT) pair_step_kernel(const StepArgs a, int k) {
     __shared__ __align__(16) PairSmem<NT> sm;
     grid_dep_wait();
     int b = blockIdx.x;
@@ -1640,7 +1636,7 @@ __global__ void __launch_bounds__(NT, 640 / NT) pair_step_kernel(const StepArgs 
         }
         b -= 1;
     }
-    march2_run<S, NT>(a, b % a.tiles_x, b / a.tiles_x, a.ctl->step_base + k, sm);
+    march2_run<S, NT, WAVE>(a, b % a.tiles_x, b / a.tiles_x, a.ctl->step_base + k, sm);
 }
 
 // ------------------------------------------------------------ 2D tiles
@@ -1995,11 +1991,8 @@ __global__ void __launch_bounds__(NT) advance_kernel(const StepArgs a, int n) {
 // entries with tx = -1 reduce their lattice's previous iteration.
 // FORM = kFormSteadyTau1 when no lattice is at its first iteration after
 // its fields were set and every lattice has τ = 1 (the host knows both).
-// The steady τ = 1 form is held to 72 registers (14 CTAs of 64 threads per
-// SM), as it compiled before the θ wave joined the common form.
 template <class S, int NT, bool GEN, int FORM = kFormAny>
-__global__ void __launch_bounds__(NT, (FORM == kFormSteadyTau1 && NT == 64) ? 14 : 1)
-    batch_step_kernel(const StepArgs *__restrict__ args,
+__global__ void __launch_bounds__(NT) batch_step_kernel(const StepArgs *__restrict__ args,
                                                         const TileRef *__restrict__ tiles,
                                                         int ntiles, int k) {
     __shared__ MarchSmem<S, NT> sm;
@@ -2008,12 +2001,16 @@ __global__ void __launch_bounds__(NT, (FORM == kFormSteadyTau1 && NT == 64) ? 14
     for (int e = blockIdx.x; e < ntiles; e += gridDim.x) {
         if (e + (int)gridDim.x >= ntiles) grid_dep_launch();  // this CTA's last entry
         const TileRef tr = tiles[e];
-        if (threadIdx.x == 0) sa = args[tr.lattice];
+        if (threadIdx.x == 0) {
+            sa = args[tr.lattice];
+            // a lattice that has stopped: strips of no output rows, which
+            // write nothing (a branch around the march would cost registers)
+            if (sa.ctl->step_base + k >= sa.stop_at) sa.march_h = 0;
+        }
         __syncthreads();
         const long long done = sa.ctl->step_base + k;
         if (tr.tx >= 0) {
-            if (done >= sa.stop_at) {  // the lattice has stopped
-            } else if constexpr (FORM == kFormSteadyTau1)
+            if constexpr (FORM == kFormSteadyTau1)
                 march_run<S, NT, false, true, GEN>(sa, tr.tx, tr.ty, done, sm);
             else
                 march_tile<S, NT, GEN>(sa, tr.tx, tr.ty, done, sm);
@@ -2024,10 +2021,10 @@ __global__ void __launch_bounds__(NT, (FORM == kFormSteadyTau1 && NT == 64) ? 14
 }
 
 // Batch on pair strips: the table's strips are pair strips of NT threads;
-// every lattice is at a steady τ = 1 iteration of the common form (scalar θ
-// or the θ wave) with even Lx (the host knows all three).
-template <class S, int NT>
-__global__ void __launch_bounds__(NT, 640 / NT) batch_pair_kernel(const StepArgs *__restrict__ args,
+// every lattice is at a steady τ = 1 iteration without rare forces or θ
+// field (WAVE: some lattice has the θ wave) and has even Lx (the host knows).
+template <class S, int NT, bool WAVE>
+__global__ void __launch_bounds__(NT) batch_pair_kernel(const StepArgs *__restrict__ args,
                                                                  const TileRef *__restrict__ tiles,
                                                                  int ntiles, int k) {
     __shared__ __align__(16) PairSmem<NT> sm;
@@ -2036,11 +2033,18 @@ __global__ void __launch_bounds__(NT, 640 / NT) batch_pair_kernel(const StepArgs
     for (int e = blockIdx.x; e < ntiles; e += gridDim.x) {
         if (e + (int)gridDim.x >= ntiles) grid_dep_launch();  // this CTA's last entry
         const TileRef tr = tiles[e];
-        if (threadIdx.x == 0) sa = args[tr.lattice];
+        if (threadIdx.x == 0) {
+            sa = args[tr.lattice];
+            if (sa.ctl->step_base + k >= sa.stop_at) sa.march_h = 0;  // stopped: no output rows
+        }
         __syncthreads();
         const long long done = sa.ctl->step_base + k;
         if (tr.tx >= 0) {
-            if (done < sa.stop_at) march2_run<S, NT>(sa, tr.tx, tr.ty, done, sm);
+            if (WAVE && sa.theta_mode == THETA_WAVE) {
+                march2_run<S, NT, WAVE>(sa, tr.tx, tr.ty, done, sm);
+            } else {
+                march2_run<S, NT, false>(sa, tr.tx, tr.ty, done, sm);
+            }
         } else if (k > 0 && done <= sa.stop_at) {
             reduce_step<NT>(sa, done, sm.redd);
         }
