@@ -58,7 +58,9 @@ def parse():
     ap.add_argument("--step-mode", default="per_iteration", choices=["per_iteration", "multi"],
                     help="launch form for --profile-case")
     ap.add_argument("--case-steps", type=int, default=12)
-    ap.add_argument("--workload", choices=["ensemble", "serving", "spinodal", "lattice2048"],
+    ap.add_argument("--size", type=int, default=0, help="lattice side of --workload dewetting")
+    ap.add_argument("--workload", choices=["ensemble", "serving", "spinodal", "lattice2048",
+                                           "dewetting"],
                     help="print the ensemble, serving, spinodal-comparison or 2048² FP32/FP16 "
                          "line only")
     return ap.parse_args()
@@ -358,6 +360,8 @@ def run_ours(args):
         extras = side_runs(sw, L, np, torch, hbm)
         extras["ensemble"] = ensemble_run(sw, np)
         extras["serving"] = serving_run(sw, np)
+        # spinodal dewetting, bounded: 2048², 10,000 steps in each precision
+        extras["dewetting_2048"] = dewetting_run(sw, np, L, n=2048, steps=10000)
 
     line = {
         "metric": "MLUPS", "value": value, "unit": "MLUPS", "n_gpus": world,
@@ -589,6 +593,43 @@ def serving_run(sw, np, duration=12.0, rate=200.0, budget=24 << 30, steps_per_ti
     return res
 
 
+def dewetting_run(sw, np, L_, n=2048, steps=10000):
+    """The dewetting film (configs.dewetting_film: h0 = 0.2 (1 + U[-0.1,
+    0.1]), θ = 1/9, n²): Float64, FP32 and FP16-storage runs after `steps`
+    iterations: droplets (h > 0.055, periodic 8-connected), relative L2 of h
+    against Float64, mass drift."""
+    from swalbe_gb300 import configs
+    sysc, h0, _ = configs.dewetting_film(n=n)
+    out = {"steps": steps, "lattice": [n, n], "film": "h0 = 0.2 (1 + U[-0.1, 0.1]), seed 3, "
+           "theta = 1/9, gamma = 0.01: ruptures into droplets"}
+    res = {}
+    for name, T in (("f64", np.float64), ("f32", np.float32), ("f16", np.float16)):
+        st = sw.Sys(sysc, "GB300", T=T)
+        st.set_measures(L_.MEAS_MASS)
+        st.height = h0
+        t0 = time.perf_counter()
+        masses, done = [], 0
+        while done < steps:
+            k = min(L_.RECORD_CAPACITY, steps - done)
+            st.step(k)
+            masses += [r.mass for r in st.measures(cap=k)]
+            done += k
+        st.sync()
+        dt = time.perf_counter() - t0
+        h = st.height
+        m = np.array(masses)
+        res[name] = h
+        out[name] = {"seconds": dt, "MLUPS": n * n * steps / dt / 1e6,
+                     "droplets": sw.count_droplets(h), "hmax": float(h.max()),
+                     "mass_drift_max": float(np.abs(m - m[0]).max() / m[0])}
+        del st
+    ref = res["f64"]
+    for name in ("f32", "f16"):
+        out[name]["rel_l2_h_vs_f64"] = float(np.linalg.norm(res[name] - ref) / np.linalg.norm(ref))
+        out[name]["droplets_vs_f64"] = out[name]["droplets"] - out["f64"]["droplets"]
+    return out
+
+
 def spinodal_run(sw, np, L_, steps=100000):
     """The spinodal-comparison film, 2048² (h = 1 + U[-0.1, 0.1], seed 3,
     γ = 0.01, θ = 1/9): FP32 and FP16-storage runs against the Float64 run
@@ -635,6 +676,11 @@ def run_workload(args):
     if args.workload == "spinodal":
         r = spinodal_run(sw, np, L_, steps=args.case_steps if args.case_steps != 12 else 100000)
         print(json.dumps({"workload": "spinodal_2048", **r}), flush=True)
+        return
+    if args.workload == "dewetting":
+        n = args.size or 2048
+        r = dewetting_run(sw, np, L_, n=n, steps=args.case_steps if args.case_steps != 12 else 10000)
+        print(json.dumps({"workload": "dewetting", **r}), flush=True)
         return
     if args.workload == "lattice2048":
         import torch

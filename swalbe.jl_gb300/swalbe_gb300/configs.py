@@ -50,6 +50,20 @@ def spinodal_2048(seed: int = 3):
     return sysc, np.asfortranarray(1.0 + rng.uniform(-0.1, 0.1, (2048, 2048))), 100000
 
 
+def dewetting_film(n: int = 2048, seed: int = 3, h0: float = 0.2, steps: int = 100000):
+    """Thin film that dewets: n², θ=1/9 (π/9), γ=0.01, other parameters the
+    defaults (hmin=0.1, hcrit=0.05, n=9, m=3, δ=1), h = h0 (1 + U[-0.1, 0.1])
+    with h0 = 0.2, twice the disjoining pressure's hmin.  The film is
+    spinodally unstable: it ruptures within ~10,000 steps into droplets
+    (h > 0.055, separated by the precursor film), which then coarsen slowly.
+    The seeded 10 % perturbation, far larger than any rounding, decides
+    where it ruptures, so the droplet count can be compared across
+    precisions (the spinodal-dewetting configuration's comparison)."""
+    sysc = SysConst(n, n, Taumucs(Tmax=steps, tdump=max(1, steps // 10)))
+    rng = np.random.default_rng(seed)
+    return sysc, np.asfortranarray(h0 * (1.0 + rng.uniform(-0.1, 0.1, (n, n)))), steps
+
+
 @dataclass
 class EnsembleMember:
     sysc: SysConst

@@ -10,6 +10,11 @@ past the device ring's capacity.
   same members run alone, Float64 bit-exact against the oracle.
 * time_loop(sys, state, Δh) with Tmax beyond the 65,536-record ring: every
   step's Δh reaches the host, equal to the oracle's.
+* Spinodal dewetting: a thin film (h0 = 0.2 (1 + U[-0.1, 0.1]), θ = 1/9)
+  that ruptures into hundreds of droplets; FP32 and FP16 storage give the
+  Float64 droplet count (within 0.5 %; equal when measured), h within 1e-3
+  relative L2 (the instability amplifies every difference after rupture)
+  and mass drift below 1e-10 (FP32) and 2e-9 (FP16 storage).
 """
 import numpy as np
 import pytest
@@ -139,3 +144,21 @@ def test_dropped_records_are_counted():
     recs = st.measures_array(cap=L.RECORD_CAPACITY + 100)
     assert len(recs) == L.RECORD_CAPACITY and recs["t"][0] == 101
     assert st.measures_dropped() == 100
+
+
+def test_dewetting_droplets_agree_across_precisions():
+    sysc, h0, _ = configs.dewetting_film(n=512)
+    steps = 10000
+    out = {}
+    for T in (np.float64, np.float32, np.float16):
+        st = run(sysc, h0, steps, T, meas=L.MEAS_MASS)
+        m = st.measures_array(cap=steps)["mass"]
+        out[T] = (st.height, sw.count_droplets(st.height), np.abs(m - m[0]).max() / m[0])
+    h64, d64, drift64 = out[np.float64]
+    assert d64 > 300  # the film has dewetted
+    assert drift64 < 1e-14
+    for T, drift_tol in ((np.float32, 1e-10), (np.float16, 2e-9)):
+        h, d, drift = out[T]
+        assert abs(d - d64) <= max(2, 0.005 * d64), (T, d, d64)
+        assert rel_l2(h, h64) < 1e-3, T
+        assert drift < drift_tol, (T, drift)
