@@ -59,6 +59,8 @@ def parse():
                     help="launch form for --profile-case")
     ap.add_argument("--case-steps", type=int, default=12)
     ap.add_argument("--size", type=int, default=0, help="lattice side of --workload dewetting")
+    ap.add_argument("--dry-run", action="store_true",
+                    help="rank set-up and ensemble sharding only, no GPU work")
     ap.add_argument("--workload", choices=["ensemble", "serving", "spinodal", "lattice2048",
                                            "dewetting"],
                     help="print the ensemble, serving, spinodal-comparison or 2048² FP32/FP16 "
@@ -259,6 +261,8 @@ def run_ours(args):
         import torch.distributed as dist
         torch.cuda.set_device(local)
         dist.init_process_group("nccl")
+        if rank == 0:
+            print(f"ranks: {dist.get_world_size()} (nccl)", file=sys.stderr, flush=True)
     else:
         torch.cuda.set_device(0)
     dev = torch.cuda.current_device()
@@ -356,6 +360,8 @@ def run_ours(args):
     traffic = load_traffic(key)
 
     extras = {}
+    if not args.no_extras and world > 1:
+        extras["ensemble"] = ensemble_run(sw, np, rank=rank, world=world, torch=torch)
     if not args.no_extras and world == 1:
         extras = side_runs(sw, L, np, torch, hbm)
         extras["ensemble"] = ensemble_run(sw, np)
@@ -460,12 +466,18 @@ def side_runs(sw, L, np, torch, hbm):
     return out
 
 
-def ensemble_run(sw, np, count=512, steps=200, plain_sample=8, geometry=""):
+def ensemble_run(sw, np, count=512, steps=200, plain_sample=8, geometry="", rank=0, world=1,
+                 torch=None):
     """Coalescence ensemble: `count` two-cap lattices (128², 256², 512²,
     1024x256) advanced together in FP32 by the batch kernel, against the
-    plain one-at-a-time paths on a sample of the same instances."""
+    plain one-at-a-time paths on a sample of the same instances.  With
+    `world` ranks each rank advances its round-robin share of the members
+    (configs.shard; no data moves between ranks) and the line reports all
+    members' lattice updates over the slowest rank's time."""
     from swalbe_gb300 import configs
     members, full_steps = configs.ensemble(count)
+    if world > 1:
+        members = configs.shard(members, rank, world)
     systems = [m.sysc for m in members]
     cells = sum(s.Lx * s.Ly for s in systems)
     b = sw.Batch(systems, T=np.float32)
@@ -479,11 +491,25 @@ def ensemble_run(sw, np, count=512, steps=200, plain_sample=8, geometry=""):
     b.step(steps)
     b.sync()  # raises if any lattice went non-finite
     dt = time.perf_counter() - t0
+    local_cells = cells
+    if world > 1:  # every rank's cells over the slowest rank's time
+        dev = torch.cuda.current_device()
+        t = torch.tensor([dt], device=f"cuda:{dev}", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        c = torch.tensor([float(cells)], device=f"cuda:{dev}", dtype=torch.float64)
+        torch.distributed.all_reduce(c)
+        dt, cells = float(t.item()), int(c.item())
     batch_mlups = cells * steps / dt / 1e6
     tile = b.tile()
     bgeo = b.geometry()
     b.close()
     del b
+    if world > 1:
+        return {"instances": count, "cells": cells, "time_steps_per_sim": full_steps,
+                "batch_f32": {"MLUPS": batch_mlups, "sims_per_s": count * steps / (dt * full_steps),
+                              "timed_steps": steps},
+                "shard": {"ranks": world, "members_on_rank0": len(members),
+                          "cells_on_rank0": local_cells, "split": "round robin (configs.shard)"}}
     # one at a time: the plain Float64 per-op path and the fused FP32 step
     rng = np.random.default_rng(0)
     sample = [members[i] for i in rng.choice(len(members), plain_sample, replace=False)]
@@ -748,8 +774,49 @@ def profile_case(args):
                       "steps": args.case_steps}))
 
 
+def launch_ranks(args) -> int:
+    """`--gpus N` outside a launcher: run this script as N local ranks
+    (torch.distributed.run, one process per GPU, rendezvous on 127.0.0.1)."""
+    import socket
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1",
+           f"--nproc-per-node={args.gpus}", "--master-addr=127.0.0.1", f"--master-port={port}",
+           os.path.abspath(__file__)] + sys.argv[1:]
+    return subprocess.call(cmd)
+
+
+def dry_run(args):
+    """The rank set-up and the ensemble sharding without GPU work (on CPU
+    ranks the process group uses gloo): rank 0 prints the rank count, the
+    backend and every rank's ensemble members."""
+    import torch
+    import torch.distributed as dist
+    rank, world, _ = dist_env()
+    backend = "nccl" if torch.cuda.is_available() else "gloo"
+    if world > 1:
+        dist.init_process_group(backend)
+    from swalbe_gb300 import configs
+    mine = configs.shard(list(range(512)), rank, world)
+    shards = [mine]
+    if world > 1:
+        shards = [None] * world
+        dist.all_gather_object(shards, mine)
+    if rank == 0:
+        print(json.dumps({"dry_run": True, "n_gpus": world, "backend": backend,
+                          "ensemble_shards": shards}), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
 def main():
     args = parse()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        sys.exit(launch_ranks(args))
+    if args.dry_run:
+        dry_run(args)
+        return
     if args.profile_case:
         profile_case(args)
         return

@@ -25,3 +25,20 @@ def test_reference_arm_json_line():
     e2e = line["e2e"]
     assert e2e["value"] == line["value"] and e2e["unit"] == "MLUPS"
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
+
+
+def test_gpus_flag_runs_that_many_ranks():
+    """`--gpus 2` outside a launcher starts two ranks (torch.distributed.run on
+    127.0.0.1; gloo on CPU) and the ensemble splits across them, disjoint and
+    complete."""
+    out = subprocess.run([sys.executable, "bench.py", "--gpus", "2", "--dry-run"], cwd=ROOT,
+                         capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [l for l in out.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    line = json.loads(lines[0])
+    assert line["n_gpus"] == 2 and line["dry_run"] is True
+    shards = line["ensemble_shards"]
+    assert len(shards) == 2
+    assert not set(shards[0]) & set(shards[1])
+    assert sorted(shards[0] + shards[1]) == list(range(512))
