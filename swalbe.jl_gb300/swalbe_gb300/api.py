@@ -410,8 +410,10 @@ def time_loop(sysc: SysConst, state: GB300State, *args, verbose: bool = False):
     - ``time_loop(sys, state, θ)``: θ a number or an Lx x Ly array;
     - ``time_loop(sys, state, Δh)``: Δh a list, max(h) - min(h) pushed every step;
     - ``time_loop(sys, state, f, measure)``: the callback runs after the forces
-      each step; ``wetted_`` and ``inclination_`` run fused on the device, any
-      other callable needs a ``"GB300-plain"`` state (it is called between ops).
+      each step; ``wetted_`` and ``inclination_`` run fused on the device; any
+      other callable runs between the reference's ops on the per-op Float64
+      path (a ``"GB300-plain"`` state, or a per-op twin of a fused state that
+      hands the populations back at the end).
     """
     from . import d1
     if isinstance(sysc, d1.SysConst_1D):
@@ -434,14 +436,15 @@ def time_loop(sysc: SysConst, state: GB300State, *args, verbose: bool = False):
             mask |= L.MEAS_WETTED
         elif callback is inclination_:
             state.set_inclination(measure)
-        elif state.precision != L.SWB_PLAIN64:
-            raise NotImplementedError("arbitrary callbacks need device='GB300-plain'")
     elif args:
         raise TypeError("time_loop(sys, state[, θ | Δh | f, measure])")
     state.set_measures(mask)
     if callback is not None and callback not in (wetted_, inclination_):
-        for _ in range(Tmax):
-            _plain_iteration_with_callback(sysc, state, callback, measure)
+        if state.precision == L.SWB_PLAIN64:
+            for _ in range(Tmax):
+                _plain_iteration_with_callback(sysc, state, callback, measure)
+        else:
+            _callback_loop_on_plain_twin(sysc, state, callback, measure, Tmax)
         recs = state.measures_array(cap=max(Tmax, 1))
     else:
         # the device ring holds RECORD_CAPACITY per-step records: step in
@@ -472,6 +475,30 @@ def time_loop(sysc: SysConst, state: GB300State, *args, verbose: bool = False):
     if callback is not None:
         return state, measure
     return state
+
+
+def _callback_loop_on_plain_twin(sysc, state, f: Callable, measure, Tmax: int) -> None:
+    """time_loop(sys, state, f, measure) with a callback the fused kernels
+    cannot run (any f other than wetted!/inclination!): the reference calls
+    f(measure, state) after the forces of every iteration and f may read or
+    change any field (src/simulate.jl:68-96).  The loop runs on a per-op
+    Float64 twin of the state (the reference's op sequence, one kernel per
+    op, f between the ops) and hands the populations and fields back: the
+    twin starts from the state's fout, h and u, and the state continues from
+    the twin's.  θ is sys.param.θ, as filmpressure!(state, sys) takes it."""
+    twin = GB300State(sysc, L.SWB_PLAIN64)
+    twin.set_theta(sysc.param.theta)
+    twin.set("fout", state.get("fout"))
+    twin.height = state.height
+    twin.velx = state.velx
+    twin.vely = state.vely
+    for _ in range(Tmax):
+        _plain_iteration_with_callback(sysc, twin, f, measure)
+    state.set("fout", twin.get("fout"))
+    state.height = twin.height
+    state.velx = twin.velx
+    state.vely = twin.vely
+    del twin
 
 
 def _plain_iteration_with_callback(sysc, state, f: Callable, measure):

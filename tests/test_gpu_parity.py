@@ -588,3 +588,35 @@ def test_batch_height_reset_matches_single():
     assert np.array_equal(b.get_height(0), single0.height)
     assert np.array_equal(b.get_height(1), single1.height)
     b.close()
+
+
+@pytest.mark.parametrize("T", [np.float64, np.float32])
+def test_time_loop_arbitrary_callback_on_fused_state(T):
+    """time_loop(sys, state, f, measure) with a callback of the user's own (it
+    reads the height and adds a force after the force sum every iteration,
+    like the reference's callbacks, src/simulate.jl:68-96) runs on a fused
+    state: bit for bit the per-op Float64 path with the same callback."""
+    Lx, Ly, steps = 40, 32, 60
+    s = sysc(Lx, Ly, Tmax=steps, delta=2.0)
+    h0 = droplet(Lx, Ly, 10)
+
+    def push(measure, state):
+        measure.append(float(state.height.max()))
+        state.Fx = state.Fx + 1e-5 * state.height
+
+    ref = sw.Sys(s, "GB300-plain", T=np.float64)
+    ref.height = h0
+    m_ref = []
+    sw.time_loop(s, ref, push, m_ref)
+    st = sw.Sys(s, "GB300", T=T)
+    st.height = h0
+    m = []
+    sw.time_loop(s, st, push, m)
+    assert m == m_ref and len(m) == steps
+    if T == np.float64:
+        assert np.array_equal(st.height, ref.height)
+    else:  # the handed-back height is stored in the state's FP32 field
+        assert np.allclose(st.height, ref.height, rtol=2 ** -23, atol=0)
+    # and the state goes on from there in its own precision
+    st.step(10)
+    assert np.isfinite(st.height).all()
