@@ -23,6 +23,7 @@ const SWB_ERR_NAN = Cint(-4)
 const PRECISION = Dict(Float64 => Cint(0), Float32 => Cint(1), Float16 => Cint(2))
 const SWB_PLAIN64 = Cint(3)
 const FIELD_HEIGHT, FIELD_VELX, FIELD_VELY, FIELD_PRESSURE = Cint(0), Cint(1), Cint(2), Cint(3)
+const FIELD_FOUT, FIELD_FX, FIELD_FY = Cint(4), Cint(6), Cint(7)
 const MEAS_MASS, MEAS_WETTED, MEAS_MAXMIN, MEAS_AREA = Cint(1), Cint(2), Cint(4), Cint(8)
 
 # swb_params: the same field order and C types
@@ -70,10 +71,13 @@ scripts that call `filmpressure!`, `h∇p!`, ... themselves.
 mutable struct GB300State <: Swalbe.LBM_state_2D
     handle::Ptr{Cvoid}
     sys::Swalbe.SysConst
+    plain::Bool
     height::Matrix{Float64}
     velx::Matrix{Float64}
     vely::Matrix{Float64}
     pressure::Matrix{Float64}
+    Fx::Matrix{Float64}  # plain states: the forces a callback sees and may change
+    Fy::Matrix{Float64}
 end
 
 function GB300State(sys::Swalbe.SysConst; T = Float64, plain = false)
@@ -82,8 +86,8 @@ function GB300State(sys::Swalbe.SysConst; T = Float64, plain = false)
     p = Ref(SwbParams(sys))
     check(ccall((:swb_create, libswb), Cint, (Ref{SwbParams}, Cint, Ref{Ptr{Cvoid}}), p, prec, ref),
           C_NULL)
-    s = GB300State(ref[], sys, ones(sys.Lx, sys.Ly), zeros(sys.Lx, sys.Ly),
-                   zeros(sys.Lx, sys.Ly), zeros(sys.Lx, sys.Ly))
+    z() = zeros(sys.Lx, sys.Ly)
+    s = GB300State(ref[], sys, plain, ones(sys.Lx, sys.Ly), z(), z(), z(), z(), z())
     finalizer(s) do x
         x.handle == C_NULL || ccall((:swb_destroy, libswb), Cint, (Ptr{Cvoid},), x.handle)
         x.handle = C_NULL
@@ -133,20 +137,87 @@ function measures(s::GB300State, n::Integer)
     return resize!(out, cnt[])
 end
 
-function run!(sys, s::GB300State; verbose = false)
+# The device ring holds SWB_RECORD_CAPACITY per-step records: loops step in
+# chunks no longer than that and drain after each (the reference pushes
+# Δh and wetted! every step, src/simulate.jl:56, src/measures.jl:13-17).
+const RECORD_CAPACITY = 65536
+
+measures_dropped(s::GB300State) = (n = Ref{Int64}(0);
+    check(ccall((:swb_measures_dropped, libswb), Cint, (Ptr{Cvoid}, Ref{Int64}), s.handle, n),
+          s.handle); n[])
+
+# Tmax iterations; `drain(records)` receives each chunk's per-step records.
+function run!(sys, s::GB300State; verbose = false, drain = nothing)
     Tmax, tdump = sys.param.Tmax, sys.param.tdump
     upload!(s)
+    drain === nothing || measures(s, RECORD_CAPACITY)  # records of earlier calls
+    dropped0 = measures_dropped(s)
     done = 0
     while done < Tmax
-        n = verbose ? min(tdump - done % tdump, Tmax - done) : Tmax - done
+        n = min(Tmax - done, RECORD_CAPACITY)
+        verbose && (n = min(n, tdump - done % tdump))
         step!(s, n)
         done += n
+        drain === nothing || drain(measures(s, n))
         if verbose && done % tdump == 0
             get_field!(s.height, s, FIELD_HEIGHT)
             println("Time step $done mass is $(round(sum(s.height), digits=3))")
         end
     end
+    measures_dropped(s) == dropped0 ||
+        throw(SwbError(Cint(-1), "per-step records were overwritten before they were read"))
     return download!(s)
+end
+
+set_inclination!(s::GB300State, α; t = 1000, tstart = 0, tsmooth = 1, loop_time = false) =
+    check(ccall((:swb_set_inclination, libswb), Cint,
+                (Ptr{Cvoid}, Cdouble, Cdouble, Cint, Int64, Int64, Int64), s.handle, α[1], α[2],
+                loop_time, t, tstart, tsmooth), s.handle)
+
+"""
+    set_theta_wave!(s, θ₀, Δθ, v)
+
+Moving wettability θ(x, t) = θ₀ + Δθ sinpi(2(x - v t)/Lx), evaluated in the
+kernels (scripts/Moving_wettability_structs.jl:183-186).
+"""
+set_theta_wave!(s::GB300State, θ0, dθ, v) =
+    check(ccall((:swb_set_theta_wave, libswb), Cint, (Ptr{Cvoid}, Cdouble, Cdouble, Cdouble),
+                s.handle, θ0, dθ, v), s.handle)
+
+"""
+    move_substrate!(s, tmove; direction = "diagonal")
+
+move_substrate! of scripts/Moving_wettability_structs.jl:139-152 on the
+device: the θ field set last moves one cell along `direction` after every
+`tmove` iterations from now (no copy; tmove = 0 stops it).
+"""
+function move_substrate!(s::GB300State, tmove; direction = "diagonal")
+    dx, dy = Dict("diagonal" => (1, 1), "x" => (1, 0), "y" => (0, 1))[direction]
+    check(ccall((:swb_set_substrate_motion, libswb), Cint, (Ptr{Cvoid}, Int64, Cint, Cint),
+                s.handle, tmove, dx, dy), s.handle)
+end
+
+"""
+    set_snapshots!(s, dumping; capacity = 64), snapshots(s)
+
+snapshot!(fluid, height, t; dumping) (src/measures.jl:99-105) on the device:
+the height after every `dumping`-th iteration goes into a device ring;
+`snapshots` returns the ones taken since the last call as the rows of a
+matrix (the reference's `vec(h)` rows) and their iterations.
+"""
+set_snapshots!(s::GB300State, dumping; capacity = 64) =
+    check(ccall((:swb_set_snapshots, libswb), Cint, (Ptr{Cvoid}, Int64, Int64), s.handle,
+                dumping, capacity), s.handle)
+function snapshots(s::GB300State; cap = 4096)
+    N = s.sys.Lx * s.sys.Ly
+    buf = Vector{Float64}(undef, cap * N)
+    times = Vector{Int64}(undef, cap)
+    cnt = Ref{Int64}(0)
+    check(ccall((:swb_get_snapshots, libswb), Cint,
+                (Ptr{Cvoid}, Ptr{Float64}, Int64, Ref{Int64}, Ptr{Int64}), s.handle, buf, cap, cnt,
+                times), s.handle)
+    n = cnt[]
+    return permutedims(reshape(buf[1:n*N], N, n)), times[1:n]
 end
 
 # time_loop(sys, state) and time_loop(sys, state, θ) (src/simulate.jl:6-45)
@@ -162,19 +233,69 @@ end
 # time_loop(sys, state, Δh) (src/simulate.jl:47-66): max - min every iteration
 function Swalbe.time_loop(sys::Swalbe.SysConst, s::GB300State, Δh::Vector; verbose = false)
     set_measures!(s, MEAS_MAXMIN)
-    run!(sys, s; verbose)
-    append!(Δh, (m.hmax - m.hmin for m in measures(s, sys.param.Tmax)))
+    run!(sys, s; verbose, drain = recs -> append!(Δh, (m.hmax - m.hmin for m in recs)))
     return s
 end
-# time_loop(sys, state, f, measure) (src/simulate.jl:68-96): wetted! is fused;
-# any other callback needs the forces on the host every iteration
+
+# One iteration of the reference's op sequence on a plain state with the
+# callback after the forces (src/simulate.jl:84-94); the callback sees the
+# state's host mirrors of height, velx, vely, Fx and Fy, and its changes to
+# Fx and Fy reach the device.
+function callback_iteration!(sys, s::GB300State, f, measure)
+    for op in (:swb_op_filmpressure, :swb_op_hgradp, :swb_op_slippage, :swb_op_force_sum)
+        check(ccall((op, libswb), Cint, (Ptr{Cvoid},), s.handle), s.handle)
+    end
+    download!(s)
+    get_field!(s.Fx, s, FIELD_FX)
+    get_field!(s.Fy, s, FIELD_FY)
+    f(measure, s)
+    set_field!(s, FIELD_FX, s.Fx)
+    set_field!(s, FIELD_FY, s.Fy)
+    for op in (:swb_op_equilibrium, :swb_op_bgk_stream, :swb_op_moments)
+        check(ccall((op, libswb), Cint, (Ptr{Cvoid},), s.handle), s.handle)
+    end
+end
+
+# time_loop(sys, state, f, measure) (src/simulate.jl:68-96): wetted! is a
+# fused measure and inclination! a fused force (with the callback's default
+# t = 1000); any other callback runs between the ops of the per-op Float64
+# path, on the state itself when it is plain, else on a plain twin that
+# starts from the state's populations and fields and hands them back.
 function Swalbe.time_loop(sys::Swalbe.SysConst, s::GB300State, f::Function, measure::Vector;
                           verbose = false)
-    f === Swalbe.wetted! || throw(ArgumentError(
-        "GB300State fuses wetted! only; run other per-iteration callbacks on a CPU State"))
-    set_measures!(s, MEAS_WETTED)
-    run!(sys, s; verbose)
-    append!(measure, (m.wetted for m in measures(s, sys.param.Tmax)))
+    if f === Swalbe.wetted!
+        set_measures!(s, MEAS_WETTED)
+        run!(sys, s; verbose, drain = recs -> append!(measure, (m.wetted for m in recs)))
+    elseif f === Swalbe.inclination!
+        set_measures!(s, 0)
+        set_inclination!(s, measure)
+        run!(sys, s; verbose)
+        set_inclination!(s, (0.0, 0.0))
+    elseif s.plain
+        upload!(s)
+        set_theta!(s, sys.param.θ)
+        for _ in 1:sys.param.Tmax
+            callback_iteration!(sys, s, f, measure)
+        end
+        download!(s)
+    else
+        upload!(s)
+        twin = GB300State(s.sys; plain = true)
+        fout = Array{Float64}(undef, s.sys.Lx, s.sys.Ly, 9)
+        get_field!(fout, s, FIELD_FOUT)
+        set_field!(twin, FIELD_FOUT, fout)
+        twin.height .= s.height; twin.velx .= s.velx; twin.vely .= s.vely
+        upload!(twin)
+        set_theta!(twin, sys.param.θ)
+        for _ in 1:sys.param.Tmax
+            callback_iteration!(sys, twin, f, measure)
+        end
+        get_field!(fout, twin, FIELD_FOUT)
+        set_field!(s, FIELD_FOUT, fout)
+        download!(twin)
+        s.height .= twin.height; s.velx .= twin.velx; s.vely .= twin.vely
+        upload!(s)
+    end
     return s, measure
 end
 
@@ -189,5 +310,10 @@ Swalbe.h∇p!(s::GB300State) =
     check(ccall((:swb_op_hgradp, libswb), Cint, (Ptr{Cvoid},), s.handle), s.handle)
 Swalbe.moments!(s::GB300State) =
     check(ccall((:swb_op_moments, libswb), Cint, (Ptr{Cvoid},), s.handle), s.handle)
+# inclination!(α, state; t, tstart, tsmooth) (src/forcing.jl:363-368): Fx .+= h α₁ (...)
+Swalbe.inclination!(α::Vector, s::GB300State; t = 1000, tstart = 0, tsmooth = 1) =
+    check(ccall((:swb_op_inclination, libswb), Cint,
+                (Ptr{Cvoid}, Cdouble, Cdouble, Int64, Int64, Int64), s.handle, α[1], α[2], t,
+                tstart, tsmooth), s.handle)
 
 end  # module
