@@ -210,12 +210,12 @@ cudaError_t launch_pressure_now(int precision, const StepArgs &a, double *out, c
 }
 cudaError_t launch_batch_step(int precision, int nt, bool gen, bool steady_tau1,
                               const StepArgs *d_args, const TileRef *d_tiles, int ntiles,
-                              int grid, int k, cudaStream_t st) {
+                              int grid, int k, cudaStream_t st, bool rare) {
     count_launches(1);
     return precision == SWB_F64
                ? launch_batch_step_f64(nt, gen, d_args, d_tiles, ntiles, grid, k, st)
                : launch_batch_step_f32(precision, nt, gen, steady_tau1, d_args, d_tiles, ntiles,
-                                       grid, k, st);
+                                       grid, k, st, rare);
 }
 int batch_blocks_per_sm(int precision, int nt) {
     return precision == SWB_F64 ? batch_blocks_per_sm_f64(nt) : batch_blocks_per_sm_f32(precision, nt);

@@ -288,9 +288,10 @@ bool pair_possible(const swb_batch *b) {
 // at any time.
 cudaError_t batch_sequence(swb_batch *b, int n, int grid) {
     cudaError_t e = cudaSuccess;
-    bool gen = false, tau1 = true, pair = true, wave = false;  // the general kernel if any lattice needs it
+    bool gen = false, tau1 = true, pair = true, wave = false, rare = false;  // the general kernel if any lattice needs it
     for (const StepArgs &a : b->args) {
         gen = gen || swb::step_general(a);
+        rare = rare || swb::step_rare(a);
         tau1 = tau1 && a.tau_is_one;
         pair = pair && swb::pair_form_ok(a);
         wave = wave || a.theta_mode == swb::THETA_WAVE;
@@ -299,13 +300,13 @@ cudaError_t batch_sequence(swb_batch *b, int n, int grid) {
         const bool steady = tau1 && !(b->fresh_pending && k == 0);
         if (b->nt < 0 && !(pair && steady))  // an iteration the pair form leaves out
             e = swb::launch_batch_step(b->precision, 64, gen, steady, b->d_args_fb, b->d_tiles_fb,
-                                       b->ntiles_fb, grid, k, b->stream);
+                                       b->ntiles_fb, grid, k, b->stream, rare);
         else if (b->nt < 0)
             e = swb::launch_batch_step(b->precision, b->nt, wave, steady, b->d_args, b->d_tiles,
                                        b->ntiles, grid, k, b->stream);
         else
             e = swb::launch_batch_step(b->precision, b->nt, gen, steady, b->d_args, b->d_tiles,
-                                       b->ntiles, grid, k, b->stream);
+                                       b->ntiles, grid, k, b->stream, rare);
     }
     if (e == cudaSuccess && n > 0) e = swb::launch_batch_advance(b->d_args, b->count, n, b->stream);
     return e;

@@ -185,6 +185,12 @@ struct TileRef {
 inline bool step_general(const StepArgs &a) {
     return a.thermal || a.incl || a.theta_mode != THETA_SCALAR;
 }
+// Whether `a` needs the general kernel for more than the θ wave (θ field,
+// thermal noise, inclination); steady iterations of wave-only lattices have
+// a WAVE variant of the common kernels.
+inline bool step_rare(const StepArgs &a) {
+    return a.thermal || a.incl || a.theta_mode == THETA_FIELD;
+}
 // Whether a steady iteration of `a` has a pair-strip kernel: τ = 1, no rare
 // forces, scalar θ or the θ wave (a per-column κ; the pair kernel's WAVE
 // variant).
@@ -245,7 +251,7 @@ cudaError_t launch_thermal_field_f32(int precision, const StepArgs &a, long long
 // set and every lattice has τ = 1 (the steady batch form may run it)
 cudaError_t launch_batch_step(int precision, int nt, bool gen, bool steady_tau1,
                               const StepArgs *d_args, const TileRef *d_tiles, int ntiles,
-                              int grid, int k, cudaStream_t st);
+                              int grid, int k, cudaStream_t st, bool rare = true);
 int batch_blocks_per_sm(int precision, int nt);
 cudaError_t launch_fused_step_f64(const StepArgs &a, int k, cudaStream_t st);
 cudaError_t launch_moments_f64(const StepArgs &a, cudaStream_t st);
@@ -261,9 +267,12 @@ cudaError_t launch_moments_f32(int precision, const StepArgs &a, cudaStream_t st
 cudaError_t launch_fout_f32(int precision, const StepArgs &a, double *out, cudaStream_t st);
 cudaError_t launch_pressure_now_f32(int precision, const StepArgs &a, double *out,
                                     cudaStream_t st);
+// rare: some lattice needs the general kernel for more than the θ wave
+// (step_rare); otherwise steady τ = 1 launches of wave lattices take the
+// WAVE variant of the steady kernel.
 cudaError_t launch_batch_step_f32(int precision, int nt, bool gen, bool steady_tau1,
                                   const StepArgs *d_args, const TileRef *d_tiles, int ntiles,
-                                  int grid, int k, cudaStream_t st);
+                                  int grid, int k, cudaStream_t st, bool rare = true);
 int batch_blocks_per_sm_f64(int nt);
 // Resident tiles: dynamic shared memory of a tile of h rows, CTAs per SM
 // that hold it (0: not possible), and n iterations in one cooperative launch

@@ -279,15 +279,16 @@ void worker_main(swb_server *sv) {
         if (tick > 0) {
             const int ntiles = count_tiles(sv);
             const int grid = std::min(ntiles, sms * occ);
-            bool gen = false, tau1 = true;  // the general kernel if any resident request needs it
+            bool gen = false, tau1 = true, rare = false;  // the general kernel if any resident request needs it
             for (Req *r : sv->active) {
                 gen = gen || swb::step_general(r->a);
+                rare = rare || swb::step_rare(r->a);
                 tau1 = tau1 && r->a.tau_is_one;
             }
             for (int64_t k = 0; k < tick && e == cudaSuccess; ++k)
                 e = swb::launch_batch_step(sv->precision, swb::kBatchNT, gen,
                                            tau1 && !(sv->fresh_pending && k == 0), sv->d_args,
-                                           sv->d_tiles, ntiles, grid, (int)k, sv->stream);
+                                           sv->d_tiles, ntiles, grid, (int)k, sv->stream, rare);
             if (e == cudaSuccess)
                 e = swb::launch_batch_advance(sv->d_args, (int)sv->active.size(), (int)tick, sv->stream);
             sv->fresh_pending = false;

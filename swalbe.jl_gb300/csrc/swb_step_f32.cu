@@ -83,8 +83,13 @@ cudaError_t launch_fused_step_f32(int precision, const StepArgs &a, int k, bool 
     cudaError_t e = cudaSuccess;
     if (a.march_nt == kTileGeom) {
         DISPATCH_STORE(precision, e = launch_step(fused_tile_kernel<S>, grid, kT2NT, st, a, k));
-    } else if (step_general(a)) {
+    } else if (step_general(a) && !(steady && !step_rare(a) && (a.march_nt == 64 || a.march_nt == 128))) {
         DISPATCH_STORE(precision, DISPATCH_NT(a.march_nt, e = launch_step(fused_step_kernel<S, NT, true>, grid, NT, st, a, k)));
+    } else if (step_general(a)) {  // the θ wave alone: WAVE variant of the steady forms
+        if (a.tau_is_one)
+            DISPATCH_STORE(precision, DISPATCH_NT_NARROW(a.march_nt, e = launch_step(fused_step_kernel<S, NT, false, kFormSteadyTau1, true>, grid, NT, st, a, k)));
+        else
+            DISPATCH_STORE(precision, DISPATCH_NT_NARROW(a.march_nt, e = launch_step(fused_step_kernel<S, NT, false, kFormSteady, true>, grid, NT, st, a, k)));
     } else if (steady && (a.march_nt == 64 || a.march_nt == 128)) {
         if (a.tau_is_one)
             DISPATCH_STORE(precision, DISPATCH_NT_NARROW(a.march_nt, e = launch_step(fused_step_kernel<S, NT, false, kFormSteadyTau1>, grid, NT, st, a, k)));
@@ -124,7 +129,7 @@ cudaError_t launch_pressure_now_f32(int precision, const StepArgs &a, double *ou
 
 cudaError_t launch_batch_step_f32(int precision, int nt, bool gen, bool steady_tau1,
                                   const StepArgs *d_args, const TileRef *d_tiles, int ntiles,
-                                  int grid, int k, cudaStream_t st) {
+                                  int grid, int k, cudaStream_t st, bool rare) {
     cudaError_t e = cudaSuccess;
     if (nt < 0) {  // pair strips: the caller passes their table only for steady steps they have
         if (!steady_tau1) return cudaErrorInvalidValue;
@@ -143,7 +148,9 @@ cudaError_t launch_batch_step_f32(int precision, int nt, bool gen, bool steady_t
             go(std::false_type{});
         return e;
     }
-    if (gen)
+    if (gen && !rare && steady_tau1 && nt == kBatchNT)  // the θ wave alone
+        DISPATCH_STORE(precision, e = launch_step(batch_step_kernel<S, kBatchNT, false, kFormSteadyTau1, true>, grid, kBatchNT, st, d_args, d_tiles, ntiles, k));
+    else if (gen)
         DISPATCH_STORE(precision, DISPATCH_NT(nt, e = launch_step(batch_step_kernel<S, NT, true>, grid, NT, st, d_args, d_tiles, ntiles, k)));
     else if (steady_tau1 && nt == kBatchNT)
         DISPATCH_STORE(precision, e = launch_step(batch_step_kernel<S, kBatchNT, false, kFormSteadyTau1>, grid, kBatchNT, st, d_args, d_tiles, ntiles, k));

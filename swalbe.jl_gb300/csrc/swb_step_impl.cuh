@@ -1114,7 +1114,7 @@ __device__ __forceinline__ void collide_cell(const StepArgs &a,
 // compiled for the iteration's rare cases: FRESH (the first iteration after
 // the fields were set: h, u come from the fields) and TAU1 (τ = 1: the
 // previous populations drop out of the collision).
-template <class S, int NT, bool FRESH, bool TAU1, bool GEN>
+template <class S, int NT, bool FRESH, bool TAU1, bool GEN, bool WAVE = false>
 __device__ __forceinline__ void march_run(const StepArgs &a, int bx, int by, long long done,
                                           MarchSmem<S, NT> &sm) {
     using R = typename S::real;
@@ -1147,7 +1147,9 @@ __device__ __forceinline__ void march_run(const StepArgs &a, int bx, int by, lon
     const double corr = (!LIT && !FRESH && a.mass_corr) ? __ldcg(&a.ctl->corr[tt & 1]) : 0.0;
     // kappa and cospi(θ) of this column: constant (scalar θ) or θ(x, t) of
     // the moving-wettability mode, which depends on x only
-    const int mode = GEN ? a.theta_mode : THETA_SCALAR;  // GEN = false: scalar θ
+    // GEN = false: scalar θ, or with WAVE also the θ wave (a per-column κ)
+    const int mode = GEN ? a.theta_mode
+                         : ((WAVE && a.theta_mode == THETA_WAVE) ? THETA_WAVE : THETA_SCALAR);
     // θ field: column of this thread and row offset in the (possibly moving) field
     int fsx = 0, fsy = 0;
     if (mode == THETA_FIELD) substrate_shift(a, tt, &fsx, &fsy);
@@ -1952,7 +1954,7 @@ enum StepForm { kFormAny = 0, kFormSteadyTau1 = 1, kFormSteady = 2 };
 
 // Single lattice: one CTA per strip, plus (when measures are kept and k > 0)
 // a reducer CTA, block 0, for the previous iteration's measures.
-template <class S, int NT, bool GEN, int FORM = kFormAny>
+template <class S, int NT, bool GEN, int FORM = kFormAny, bool WAVE = false>
 __global__ void __launch_bounds__(NT) fused_step_kernel(const StepArgs a, int k) {
     __shared__ MarchSmem<S, NT> sm;
     grid_dep_wait();
@@ -1967,9 +1969,9 @@ __global__ void __launch_bounds__(NT) fused_step_kernel(const StepArgs a, int k)
     }
     const long long done = a.ctl->step_base + k;
     if constexpr (FORM == kFormSteadyTau1)
-        march_run<S, NT, false, true, GEN>(a, b % a.tiles_x, b / a.tiles_x, done, sm);
+        march_run<S, NT, false, true, GEN, WAVE>(a, b % a.tiles_x, b / a.tiles_x, done, sm);
     else if constexpr (FORM == kFormSteady)
-        march_run<S, NT, false, false, GEN>(a, b % a.tiles_x, b / a.tiles_x, done, sm);
+        march_run<S, NT, false, false, GEN, WAVE>(a, b % a.tiles_x, b / a.tiles_x, done, sm);
     else
         march_tile<S, NT, GEN>(a, b % a.tiles_x, b / a.tiles_x, done, sm);
 }
@@ -1991,7 +1993,7 @@ __global__ void __launch_bounds__(NT) advance_kernel(const StepArgs a, int n) {
 // entries with tx = -1 reduce their lattice's previous iteration.
 // FORM = kFormSteadyTau1 when no lattice is at its first iteration after
 // its fields were set and every lattice has τ = 1 (the host knows both).
-template <class S, int NT, bool GEN, int FORM = kFormAny>
+template <class S, int NT, bool GEN, int FORM = kFormAny, bool WAVE = false>
 __global__ void __launch_bounds__(NT) batch_step_kernel(const StepArgs *__restrict__ args,
                                                         const TileRef *__restrict__ tiles,
                                                         int ntiles, int k) {
@@ -2011,7 +2013,7 @@ __global__ void __launch_bounds__(NT) batch_step_kernel(const StepArgs *__restri
         const long long done = sa.ctl->step_base + k;
         if (tr.tx >= 0) {
             if constexpr (FORM == kFormSteadyTau1)
-                march_run<S, NT, false, true, GEN>(sa, tr.tx, tr.ty, done, sm);
+                march_run<S, NT, false, true, GEN, WAVE>(sa, tr.tx, tr.ty, done, sm);
             else
                 march_tile<S, NT, GEN>(sa, tr.tx, tr.ty, done, sm);
         } else if (k > 0 && done <= sa.stop_at)

@@ -595,7 +595,8 @@ def test_time_loop_arbitrary_callback_on_fused_state(T):
     """time_loop(sys, state, f, measure) with a callback of the user's own (it
     reads the height and adds a force after the force sum every iteration,
     like the reference's callbacks, src/simulate.jl:68-96) runs on a fused
-    state: bit for bit the per-op Float64 path with the same callback."""
+    state: bit for bit the per-op Float64 path with the same callback, from
+    the same (for an FP32 state, FP32-rounded) initial film."""
     Lx, Ly, steps = 40, 32, 60
     s = sysc(Lx, Ly, Tmax=steps, delta=2.0)
     h0 = droplet(Lx, Ly, 10)
@@ -605,7 +606,8 @@ def test_time_loop_arbitrary_callback_on_fused_state(T):
         state.Fx = state.Fx + 1e-5 * state.height
 
     ref = sw.Sys(s, "GB300-plain", T=np.float64)
-    ref.height = h0
+    # an FP32 state holds h0 rounded to FP32: the per-op run starts from that
+    ref.height = h0 if T == np.float64 else h0.astype(np.float32).astype(np.float64)
     m_ref = []
     sw.time_loop(s, ref, push, m_ref)
     st = sw.Sys(s, "GB300", T=T)
