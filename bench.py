@@ -141,6 +141,11 @@ class ClockSampler:
 def kernel_name(prec, geo, form):
     """The dominant kernel of a run with this geometry and launch form."""
     store = {"f32": "StoreF32", "f16": "StoreF16", "f64": "StoreF64"}[prec]
+    if geo[0] == 33:
+        return (f"resident_run_kernel<{store}> (tiles of 64x{geo[1]} in shared memory, up to "
+                "1024 iterations per cooperative launch; figures per iteration)")
+    if geo[0] < 0:
+        return f"pair_step_kernel<{store}, {-geo[0]}> (pair strips of {-2 * geo[0] - 4}x{geo[1]})"
     if form == "multi":
         return f"fused_run_kernel<{store}, {256 if geo[0] == 32 else geo[0]}, {geo[0] == 32}>"
     if geo[0] == 32:
@@ -356,7 +361,8 @@ def run_ours(args):
     t_launch = statistics.median(launch_ms) / 1e3
     alg_bytes = B_ALG[args.precision] * N
     achieved = alg_bytes / t_launch / 1e9
-    key = f"fused_step_{args.precision}_512"
+    key = (f"resident_{args.precision}_512" if geo[0] == 33 else
+           f"pair_{args.precision}_512" if geo[0] < 0 else f"fused_step_{args.precision}_512")
     traffic = load_traffic(key)
 
     extras = {}
