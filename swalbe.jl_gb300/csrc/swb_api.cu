@@ -547,11 +547,11 @@ int sm_count() {
 
 // Rows of resident tiles for a lattice: the shortest tiles (the most CTAs)
 // whose CTAs are all co-resident; 0 when even kResMaxTH rows do not fit.
-int resident_rows(int Lx, int Ly, int precision) {
+int resident_rows(int Lx, int Ly, int precision, int nt = swb::kResGeom) {
     const long long tx = (Lx + swb::kResTW - 1) / swb::kResTW, sms = sm_count();
     for (int h = 1; h <= swb::kResMaxTH; ++h) {
         const long long tiles = tx * ((Ly + h - 1) / h);
-        const int per_sm = swb::resident_blocks_per_sm(precision, h);
+        const int per_sm = swb::resident_blocks_per_sm(precision, h, nt);
         if (per_sm > 0 && tiles <= per_sm * sms) return h < Ly ? h : Ly;
     }
     return 0;
@@ -562,8 +562,8 @@ int resident_rows(int Lx, int Ly, int precision) {
 // tile, all of which must be co-resident (0: not possible).
 int run_grid(swb_state *s) {
     const long long tiles = (long long)s->a.tiles_x * s->a.tiles_y;
-    if (s->a.march_nt == swb::kResGeom) {
-        const int per_sm = swb::resident_blocks_per_sm(s->precision, s->a.march_h);
+    if (swb::resident_geometry(s->a.march_nt)) {
+        const int per_sm = swb::resident_blocks_per_sm(s->precision, s->a.march_h, s->a.march_nt);
         return (per_sm > 0 && tiles <= (long long)per_sm * sm_count()) ? (int)tiles : 0;
     }
     const int per_sm = swb::fused_run_blocks_per_sm(s->precision, s->a.march_nt);
@@ -578,7 +578,8 @@ int run_grid(swb_state *s) {
 // common steady τ = 1 step.
 bool run_possible(const swb_state *s) {
     if (s->precision != SWB_F32 && s->precision != SWB_F16) return false;
-    if (s->a.march_nt == swb::kResGeom) return swb::resident_ok(s->a) && run_grid(const_cast<swb_state *>(s)) > 0;
+    if (swb::resident_geometry(s->a.march_nt))
+        return swb::resident_ok(s->a) && run_grid(const_cast<swb_state *>(s)) > 0;
     return s->a.march_nt == 64 || s->a.march_nt == 128 || s->a.march_nt == swb::kTileGeom;
 }
 
@@ -588,7 +589,7 @@ cudaError_t run_sequence(swb_state *s, long long n) {
     if (grid <= 0) return cudaErrorInvalidConfiguration;
     while (n > 0) {
         const int c = (int)(n < kRunChunk ? n : kRunChunk);
-        cudaError_t e = s->a.march_nt == swb::kResGeom
+        cudaError_t e = swb::resident_geometry(s->a.march_nt)
                             ? swb::launch_resident_run(s->precision, s->a, c, s->stream)
                             : swb::launch_fused_run(s->precision, s->a, c, grid, s->stream);
         if (e != cudaSuccess) return e;
@@ -603,7 +604,7 @@ cudaError_t run_sequence(swb_state *s, long long n) {
 // graph-replayed launches at 512^2..2048^2; the tuner times both) or the
 // geometry is resident tiles (a multi-step form only).
 bool persist_default(const swb_state *s) {
-    return (s->mode == SWB_STEP_MULTI || s->a.march_nt == swb::kResGeom) && run_possible(s);
+    return (s->mode == SWB_STEP_MULTI || swb::resident_geometry(s->a.march_nt)) && run_possible(s);
 }
 
 // n step launches (k = 0..n-1) and the advance kernel that closes them.
@@ -708,14 +709,18 @@ int autotune_geometry(swb_state *s, long long &left) {
     }
     // resident tiles (a multi-step form) where the lattice fits in the CTAs'
     // shared memory: the shortest co-resident tiles
-    const int res_h = (multi_ok && swb::resident_ok(s->a)) ? resident_rows(s->p.Lx, s->p.Ly, s->precision) : 0;
-    if (res_h > 0) todo.push_back({swb::kResGeom, res_h, 1});
+    if (multi_ok && swb::resident_ok(s->a)) {
+        for (int rg : {swb::kResGeom, swb::kResGeom2}) {
+            const int res_h = resident_rows(s->p.Lx, s->p.Ly, s->precision, rg);
+            if (res_h > 0) todo.push_back({rg, res_h, 1});
+        }
+    }
     for (auto &c : todo) {
         if (c[0] == K && !multi_ok) continue;
         if (c[0] < 0 && !pair_ok) continue;
         // the multi-step form only when asked for: it never won on GB300
         // (sweeps at 512^2..2048^2), and a 16-iteration probe can misjudge it
-        if (c[2] && c[0] != swb::kResGeom && (!multi_ok || s->mode != SWB_STEP_MULTI)) continue;
+        if (c[2] && !swb::resident_geometry(c[0]) && (!multi_ok || s->mode != SWB_STEP_MULTI)) continue;
         if (!c[2] && s->mode == SWB_STEP_MULTI) continue;
         cands.push_back({c[0], c[1], c[2]});
     }
@@ -1193,17 +1198,17 @@ int swb_set_geometry(swb_state *s, int nt, int h) {
         if (s->precision == SWB_F64)
             return fail(&s->err, SWB_ERR_UNSUPPORTED, "2D tiles: FP32 and FP16 storage only");
         h = swb::kTileY;
-    } else if (nt == swb::kResGeom) {
+    } else if (swb::resident_geometry(nt)) {
         if (s->precision != SWB_F32 && s->precision != SWB_F16)
             return fail(&s->err, SWB_ERR_UNSUPPORTED, "resident tiles: FP32 and FP16 storage only");
-        if (h == 0) h = resident_rows(s->p.Lx, s->p.Ly, s->precision);
+        if (h == 0) h = resident_rows(s->p.Lx, s->p.Ly, s->precision, nt);
         if (h < 1 || h > swb::kResMaxTH)
             return fail(&s->err, SWB_ERR_UNSUPPORTED,
                         "resident tiles: the lattice does not fit in the GPU's shared memory "
                         "(rows must be 1..40 with every tile co-resident)");
         const long long tiles = (long long)((s->p.Lx + swb::kResTW - 1) / swb::kResTW) *
                                 ((s->p.Ly + h - 1) / h);
-        if (tiles > (long long)swb::resident_blocks_per_sm(s->precision, h) * sm_count())
+        if (tiles > (long long)swb::resident_blocks_per_sm(s->precision, h, nt) * sm_count())
             return fail(&s->err, SWB_ERR_UNSUPPORTED,
                         "resident tiles: more tiles than the GPU holds at once; use more rows");
     } else if (swb::pair_geometry(nt)) {
@@ -1248,7 +1253,7 @@ int swb_set_step_mode(swb_state *s, int mode) {
         swb::default_geometry(s->p.Lx, s->p.Ly, s->precision, &nt, &h);
         swb::set_geometry(s->a, nt, h);
     }
-    if (mode == SWB_STEP_PER_ITERATION && s->a.march_nt == swb::kResGeom) {
+    if (mode == SWB_STEP_PER_ITERATION && swb::resident_geometry(s->a.march_nt)) {
         int nt = 0, h = 0;  // resident tiles are a multi-step form
         swb::default_geometry(s->p.Lx, s->p.Ly, s->precision, &nt, &h);
         swb::set_geometry(s->a, nt, h);

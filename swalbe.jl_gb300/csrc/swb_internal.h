@@ -140,7 +140,11 @@ inline bool pair_geometry(int nt) { return nt == -32 || nt == -64 || nt == -128;
 // shared memory, all CTAs co-resident.  Only the common steady τ = 1 step
 // has this form; other iterations run on strips (strip_fallback).
 constexpr int kResGeom = 33;
+// kResGeom2: the same with CTAs of kResThreads / 2 threads, two per SM (one
+// CTA's phases run while the other waits at a barrier; tiles half as tall).
+constexpr int kResGeom2 = 34;
 constexpr int kResTW = 64, kResMaxTH = 40, kResThreads = 512;
+inline bool resident_geometry(int nt) { return nt == kResGeom || nt == kResGeom2; }
 
 inline void set_geometry(StepArgs &a, int nt, int h) {
     a.march_nt = nt;
@@ -150,7 +154,7 @@ inline void set_geometry(StepArgs &a, int nt, int h) {
         a.tiles_y = (a.Ly + kTileY - 1) / kTileY;
         return;
     }
-    if (nt == kResGeom) {
+    if (resident_geometry(nt)) {
         a.march_h = h;
         a.tiles_x = (a.Lx + kResTW - 1) / kResTW;
         a.tiles_y = (a.Ly + h - 1) / h;
@@ -163,7 +167,9 @@ inline void set_geometry(StepArgs &a, int nt, int h) {
 }
 // Threads per CTA of a geometry.
 inline int geometry_threads(int nt) {
-    return nt == kTileGeom ? kTileThreads : (nt == kResGeom ? kResThreads : (nt < 0 ? -nt : nt));
+    return nt == kTileGeom ? kTileThreads
+                           : (nt == kResGeom ? kResThreads
+                                             : (nt == kResGeom2 ? kResThreads / 2 : (nt < 0 ? -nt : nt)));
 }
 // The one-column strips (64 threads, the same rows) that run the iterations
 // the pair-strip and resident-tile forms leave out.
@@ -277,8 +283,8 @@ int batch_blocks_per_sm_f64(int nt);
 // Resident tiles: dynamic shared memory of a tile of h rows, CTAs per SM
 // that hold it (0: not possible), and n iterations in one cooperative launch
 // of tiles_x * tiles_y CTAs (closes the sequence itself).
-size_t resident_smem_bytes(int h);
-int resident_blocks_per_sm(int precision, int h);
+size_t resident_smem_bytes(int h, int nt = kResGeom);
+int resident_blocks_per_sm(int precision, int h, int nt = kResGeom);
 cudaError_t launch_resident_run(int precision, const StepArgs &a, int n, cudaStream_t st);
 // Whether iterations of `a` may run as resident tiles (the common steady
 // τ = 1 step with scalar θ of an FP32-arithmetic lattice).

@@ -21,6 +21,8 @@
 // measures go through the same integer accumulators and reducer.  The common
 // steady τ = 1 step only (scalar θ, no rare forces): the host runs every
 // other iteration on strips.
+#include <type_traits>
+
 #include "swb_step_impl.cuh"
 
 namespace swb {
@@ -80,8 +82,8 @@ __device__ __forceinline__ bool res_wait(unsigned int *ctr, int *err, unsigned i
     return __syncthreads_and(ok) != 0;
 }
 
-template <class S>
-__global__ void __launch_bounds__(kResThreads, 1) resident_run_kernel(const StepArgs a, int n) {
+template <class S, int NT>
+__global__ void __launch_bounds__(NT, kResThreads / NT) resident_run_kernel(const StepArgs a, int n) {
     using R = float;
     extern __shared__ __align__(16) float dsm[];
     const int TH = a.march_h;
@@ -93,7 +95,7 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_run_kernel(const Step
     float *JY = JX + TH * kResTW;
     float *LO = JY + TH * kResTW;
     PartQ *red = reinterpret_cast<PartQ *>(LO + TH * kResTW);  // 8-byte aligned: every size above is even
-    RedPart *redd = reinterpret_cast<RedPart *>(red + kResThreads / 32);
+    RedPart *redd = reinterpret_cast<RedPart *>(red + NT / 32);
 
     const int t = threadIdx.x;
     const int G = gridDim.x, b = blockIdx.x;
@@ -121,7 +123,7 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_run_kernel(const Step
     auto load = [&](long long done, bool ring_only) {
         const void *src = (done & 1) ? a.fb : a.fa;
         if (!ring_only) {
-            for (int i = t; i < kEW * eh; i += kResThreads) {
+            for (int i = t; i < kEW * eh; i += NT) {
                 const int lx = i % kEW, ly = i / kEW;
                 if (lx < ew) load_cell(src, lx, ly);
             }
@@ -129,7 +131,7 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_run_kernel(const Step
         }
         // 3 rows above and below the tile (all columns), then 3 columns
         // left and right of it (the tile's rows)
-        constexpr int kLd = kResThreads - 32;  // threads 32.. (warp 0 may be reducing)
+        constexpr int kLd = NT - 32;  // threads 32.. (warp 0 may be reducing)
         for (int i = t - 32; i < 6 * kEW; i += kLd) {
             const int lx = i % kEW, r = i / kEW;
             if (lx < ew) load_cell(src, lx, r < 3 ? r : th + r);
@@ -147,7 +149,7 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_run_kernel(const Step
             // the previous iteration's measures (warp 0 of the last CTA),
             // while warps 1.. load the ring
             if (t < 32) {
-                if (red_on && b == G - 1) reduce_step<kResThreads>(a, done, redd);
+                if (red_on && b == G - 1) reduce_step<NT>(a, done, redd);
             } else {
                 load(done, true);
             }
@@ -156,7 +158,7 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_run_kernel(const Step
         // A. pull and moments on the tile and 2 rings
         {
             const int w2 = tw + 4;
-            for (int i = t; i < kHW * (th + 4); i += kResThreads) {
+            for (int i = t; i < kHW * (th + 4); i += NT) {
                 const int hx = i % kHW, hy = i / kHW;
                 if (hx >= w2) continue;
                 const float *c = F + (hy + 1) * kEW + (hx + 1);
@@ -186,7 +188,7 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_run_kernel(const Step
         // B. film pressure on the tile and 1 ring
         {
             const int w1 = tw + 2;
-            for (int i = t; i < kPW * (th + 2); i += kResThreads) {
+            for (int i = t; i < kPW * (th + 2); i += NT) {
                 const int px = i % kPW, py = i / kPW;
                 if (px >= w1) continue;
                 const float *hc = Hs + (py + 1) * kHW + (px + 1), *hm = hc - kHW, *hp = hc + kHW;
@@ -204,7 +206,7 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_run_kernel(const Step
         PartQ part;
         part_init(part);
         int any_nan = 0;
-        for (int i = t; i < kResTW * th; i += kResThreads) {
+        for (int i = t; i < kResTW * th; i += NT) {
             const int ox = i % kResTW, oy = i / kResTW;
             if (ox >= tw) continue;
             const int cell = (Y0 + oy) * Lx + X0 + ox;
@@ -253,7 +255,7 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_run_kernel(const Step
         }
         any_nan = __syncthreads_or(any_nan);
         if (any_nan && t == 0) a.ctl->nan_flag = 1;
-        if (measure) write_partials<kResThreads>(a, part, tt, b, red);
+        if (measure) write_partials<NT>(a, part, tt, b, red);
         res_arrive(a.bar);
         // after the last iteration only the last CTA waits (to reduce it)
         if ((k + 1 < n || b == G - 1) &&
@@ -261,7 +263,7 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_run_kernel(const Step
             return;
     }
     if (b == G - 1) {
-        if (red_on && n > 0) reduce_step<kResThreads>(a, base + n, redd);
+        if (red_on && n > 0) reduce_step<NT>(a, base + n, redd);
         __syncthreads();
         if (t == 0) {
             a.ctl->step_base = base + n;
@@ -273,56 +275,63 @@ __global__ void __launch_bounds__(kResThreads, 1) resident_run_kernel(const Step
 // Allow the kernel the dynamic shared memory of a tile (a host-side
 // attribute of the current device's context; set before every query or
 // launch, which is cheap and keeps it right on every device).
-template <class S>
+template <class S, int NT>
 cudaError_t prepare(size_t bytes) {
-    return cudaFuncSetAttribute(resident_run_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)bytes);
+    return cudaFuncSetAttribute(resident_run_kernel<S, NT>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+// Runs f(store tag, threads) for a precision and resident geometry.
+template <class F>
+cudaError_t res_dispatch(int precision, int nt, F &&f) {
+    const bool half = precision == SWB_F16;
+    if (nt == kResGeom2)
+        return half ? f(StoreF16T<LdCG>{}, std::integral_constant<int, kResThreads / 2>{})
+                    : f(StoreF32T<LdCG>{}, std::integral_constant<int, kResThreads / 2>{});
+    return half ? f(StoreF16T<LdCG>{}, std::integral_constant<int, kResThreads>{})
+                : f(StoreF32T<LdCG>{}, std::integral_constant<int, kResThreads>{});
 }
 
 }  // namespace
 
-size_t resident_smem_bytes(int h) {
-    return res_floats(h) * sizeof(float) + (size_t)(kResThreads / 32) * (sizeof(PartQ) + sizeof(RedPart));
+size_t resident_smem_bytes(int h, int nt) {
+    const size_t threads = nt == kResGeom2 ? kResThreads / 2 : kResThreads;
+    return res_floats(h) * sizeof(float) + (threads / 32) * (sizeof(PartQ) + sizeof(RedPart));
 }
 
-int resident_blocks_per_sm(int precision, int h) {
+int resident_blocks_per_sm(int precision, int h, int nt) {
     if ((precision != SWB_F32 && precision != SWB_F16) || h < 1 || h > kResMaxTH) return 0;
-    const size_t bytes = resident_smem_bytes(h);
+    const size_t bytes = resident_smem_bytes(h, nt);
     int n = 0;
-    if (precision == SWB_F16) {
-        if (prepare<StoreF16T<LdCG>>(bytes) != cudaSuccess) return 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, resident_run_kernel<StoreF16T<LdCG>>,
-                                                      kResThreads, bytes);
-    } else {
-        if (prepare<StoreF32T<LdCG>>(bytes) != cudaSuccess) return 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, resident_run_kernel<StoreF32T<LdCG>>,
-                                                      kResThreads, bytes);
-    }
-    return n;
+    cudaError_t e = res_dispatch(precision, nt, [&](auto store, auto threads) {
+        using S = decltype(store);
+        constexpr int NT = decltype(threads)::value;
+        cudaError_t r = prepare<S, NT>(bytes);
+        if (r == cudaSuccess)
+            r = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, resident_run_kernel<S, NT>, NT, bytes);
+        return r;
+    });
+    return e == cudaSuccess ? n : 0;
 }
 
 cudaError_t launch_resident_run(int precision, const StepArgs &a, int n, cudaStream_t st) {
-    if ((precision != SWB_F32 && precision != SWB_F16) || a.march_nt != kResGeom || !a.bar ||
+    if ((precision != SWB_F32 && precision != SWB_F16) || !resident_geometry(a.march_nt) || !a.bar ||
         a.march_h < 1 || a.march_h > kResMaxTH)
         return cudaErrorInvalidValue;
-    const size_t bytes = resident_smem_bytes(a.march_h);
+    const size_t bytes = resident_smem_bytes(a.march_h, a.march_nt);
     StepArgs args = a;
     int steps = n;
     void *params[] = {&args, &steps};
-    const dim3 grid((unsigned)(a.tiles_x * a.tiles_y)), block(kResThreads);
-    cudaError_t e;
-    if (precision == SWB_F16) {
-        e = prepare<StoreF16T<LdCG>>(bytes);
-        if (e == cudaSuccess)
-            e = cudaLaunchCooperativeKernel((const void *)resident_run_kernel<StoreF16T<LdCG>>,
-                                            grid, block, params, bytes, st);
-    } else {
-        e = prepare<StoreF32T<LdCG>>(bytes);
-        if (e == cudaSuccess)
-            e = cudaLaunchCooperativeKernel((const void *)resident_run_kernel<StoreF32T<LdCG>>,
-                                            grid, block, params, bytes, st);
-    }
-    return e;
+    const dim3 grid((unsigned)(a.tiles_x * a.tiles_y));
+    return res_dispatch(precision, a.march_nt, [&](auto store, auto threads) {
+        using S = decltype(store);
+        constexpr int NT = decltype(threads)::value;
+        cudaError_t r = prepare<S, NT>(bytes);
+        if (r == cudaSuccess)
+            r = cudaLaunchCooperativeKernel((const void *)resident_run_kernel<S, NT>, grid, dim3(NT),
+                                            params, bytes, st);
+        return r;
+    });
 }
 
 }  // namespace swb

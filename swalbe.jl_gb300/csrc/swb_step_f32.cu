@@ -57,7 +57,7 @@ int grid_for(long long n, int threads) {
 
 cudaError_t launch_fused_step_f32(int precision, const StepArgs &a, int k, bool steady,
                                   cudaStream_t st) {
-    if (a.march_nt == kResGeom)  // one iteration at a time: strips of the same rows
+    if (resident_geometry(a.march_nt))  // one iteration at a time: strips of the same rows
         return launch_fused_step_f32(precision, strip_fallback(a), k, steady, st);
     if (a.march_nt < 0) {
         if (!(steady && pair_form_ok(a)))
