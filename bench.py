@@ -605,6 +605,8 @@ def serving_run(sw, np, duration=12.0, rate=200.0, budget=24 << 30, steps_per_ti
         "duration_s": wall, "offered_req_per_s": rate, "arrivals": i,
         "offered_MLUPS": offered_lu / duration / 1e6,
         "served_MLUPS": st.lattice_updates / wall / 1e6,
+        "ticks": int(st.ticks), "tick_busy_s": st.busy_seconds, "device_s": st.device_seconds,
+        "device_MLUPS": st.lattice_updates / st.device_seconds / 1e6 if st.device_seconds else None,
         "completed": len(done), "admitted": int(st.admitted), "rejected_queue_full": rejected,
         "resident_at_end": int(st.running), "queued_at_end": int(st.queued),
         "latency_s": {"p50": pct(0.50), "p99": pct(0.99), "max": lat[-1] if lat else None,

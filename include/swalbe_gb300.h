@@ -347,6 +347,7 @@ typedef struct swb_server_stats {
     double busy_seconds;    /* time with at least one resident request   */
     size_t hbm_in_use, hbm_budget;
     int64_t ticks;
+    double device_seconds;  /* device time of the ticks (CUDA events)     */
 } swb_server_stats;
 
 /* hbm_budget: bytes of device memory the resident states may use.

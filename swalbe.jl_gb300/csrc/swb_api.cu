@@ -217,8 +217,8 @@ cudaError_t launch_batch_step(int precision, int nt, bool gen, bool steady_tau1,
                : launch_batch_step_f32(precision, nt, gen, steady_tau1, d_args, d_tiles, ntiles,
                                        grid, k, st, rare);
 }
-int batch_blocks_per_sm(int precision, int nt) {
-    return precision == SWB_F64 ? batch_blocks_per_sm_f64(nt) : batch_blocks_per_sm_f32(precision, nt);
+int batch_blocks_per_sm(int precision, int nt, bool wave) {
+    return precision == SWB_F64 ? batch_blocks_per_sm_f64(nt) : batch_blocks_per_sm_f32(precision, nt, wave);
 }
 
 // Default strip geometry by lattice size (from sweeps on GB300): narrow

@@ -326,12 +326,16 @@ int autotune(swb_batch *b, long long &left) {
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    bool pair = true;
-    for (const StepArgs &a : b->args) pair = pair && swb::pair_form_ok(a);
+    bool pair = true, wave = false;
+    for (const StepArgs &a : b->args) {
+        pair = pair && swb::pair_form_ok(a);
+        wave = wave || a.theta_mode == swb::THETA_WAVE;
+    }
     std::vector<std::array<int, 2>> geos = {{64, 32}, {64, 16}, {128, 16}};
     if (pair_possible(b) && pair) {
         geos.push_back({-64, 16});
         geos.push_back({-64, 32});
+        geos.push_back({-64, 64});
         geos.push_back({-32, 16});
     }
     if (b->geometry_fixed) geos = {{b->nt, b->rows}};  // a geometry set by the caller
@@ -350,7 +354,7 @@ int autotune(swb_batch *b, long long &left) {
             rc = apply_geometry(b, g[0], g[1]);
             if (rc) break;
         }
-        const int occ = swb::batch_blocks_per_sm(b->precision, b->nt);
+        const int occ = swb::batch_blocks_per_sm(b->precision, b->nt, wave);
         std::vector<int> grids = {b->ntiles, std::min(b->ntiles, sms * occ),
                                   std::min(b->ntiles, sms * std::max(1, occ / 2))};
         std::sort(grids.begin(), grids.end());
@@ -378,7 +382,7 @@ int autotune(swb_batch *b, long long &left) {
             rc = apply_geometry(b, swb::kBatchNT, swb::kBatchRows);
             if (rc) return rc;
         }
-        b->grid = std::min(b->ntiles, sms * swb::batch_blocks_per_sm(b->precision, b->nt));
+        b->grid = std::min(b->ntiles, sms * swb::batch_blocks_per_sm(b->precision, b->nt, wave));
     } else {
         if (best.nt != b->nt || best.rows != b->rows) {
             rc = apply_geometry(b, best.nt, best.rows);

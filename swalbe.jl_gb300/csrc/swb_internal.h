@@ -258,7 +258,7 @@ cudaError_t launch_thermal_field_f32(int precision, const StepArgs &a, long long
 cudaError_t launch_batch_step(int precision, int nt, bool gen, bool steady_tau1,
                               const StepArgs *d_args, const TileRef *d_tiles, int ntiles,
                               int grid, int k, cudaStream_t st, bool rare = true);
-int batch_blocks_per_sm(int precision, int nt);
+int batch_blocks_per_sm(int precision, int nt, bool wave = false);
 cudaError_t launch_fused_step_f64(const StepArgs &a, int k, cudaStream_t st);
 cudaError_t launch_moments_f64(const StepArgs &a, cudaStream_t st);
 cudaError_t launch_fout_f64(const StepArgs &a, double *out, cudaStream_t st);
@@ -295,7 +295,7 @@ int pair_blocks_per_sm(int precision, int nt);
 // time in every CTA, so a launch lasts (waves of resident CTAs) x (rows + 4
 // halo rows); the rule takes the height that minimises that product.
 int pair_rows(int Lx, int Ly, int precision, int nt);
-int batch_blocks_per_sm_f32(int precision, int nt);
+int batch_blocks_per_sm_f32(int precision, int nt, bool wave = false);
 
 // plain FP64 per-op kernels (reference operation order)
 struct PlainState {

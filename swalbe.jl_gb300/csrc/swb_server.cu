@@ -84,11 +84,18 @@ struct swb_server {
     cudaStream_t stream = nullptr;  // the ticks
     cudaStream_t copy = nullptr;    // admissions and results, beside the ticks
     cudaMemPool_t pool = nullptr;
-    int nt = swb::kBatchNT;         // strip width of served lattices
+    int nt = swb::kBatchNT;         // strip geometry of the resident set (< 0: pair strips)
     bool fresh_pending = false;     // lattices that joined are at their first iteration
     StepArgs *d_args = nullptr;
     TileRef *d_tiles = nullptr;
     size_t cap_args = 0, cap_tiles = 0;
+    int ntiles = 0;
+    // pair strips: the one-column strips of the iterations the pair form
+    // leaves out (a lattice's first iteration after it joined)
+    StepArgs *d_args_fb = nullptr;
+    TileRef *d_tiles_fb = nullptr;
+    size_t cap_args_fb = 0, cap_tiles_fb = 0;
+    int ntiles_fb = 0;
     double *staging = nullptr;
     size_t staging_elems = 0;
     swb_server_stats st{};
@@ -127,7 +134,8 @@ bool admit_device(swb_server *sv, Req *r) {
         set_error(sv, std::string("admit: ") + cudaGetErrorString(e));
         return false;
     }
-    r->a = swb::lattice_args(r->p, sv->precision, r->dev, r->L, sv->nt, swb::kBatchRows);
+    // the strip geometry is set again when the lattice joins (choose_geometry)
+    r->a = swb::lattice_args(r->p, sv->precision, r->dev, r->L, swb::kBatchNT, swb::kBatchRows);
     r->a.seed = (unsigned long long)r->id;  // thermal noise stream of this request
     r->a.stop_at = r->nsteps;  // its strips stop there, whatever the tick length
     swb::set_wave(r->a, r->theta0, r->dtheta, r->v);
@@ -156,48 +164,106 @@ bool admit_device(swb_server *sv, Req *r) {
     return true;
 }
 
-bool upload_table(swb_server *sv) {
-    std::vector<StepArgs> args;
+// Strip geometry of the resident set, chosen whenever it changes: pair
+// strips when every lattice allows them (FP32 arithmetic, even Lx, the
+// common τ = 1 step), else one-column strips of kBatchNT threads.  Pair
+// strips are about 1.3x faster per cell.  Each strip recomputes 2 columns
+// and 2 rows on each side, and the last strip of a lattice is partly empty,
+// so the strip width is chosen for the set: 124 columns (64 threads) or 60
+// (32 threads), whichever processes fewer cells in all (60-column strips
+// waste less on the small lattices a shortest-job-first queue favours).
+// Rows are set per lattice to the balanced height of at most 64 rows that
+// covers it (a 64-row lattice is one strip, 100 rows two of 50).  Results
+// do not depend on the geometry.
+constexpr int kServePairRows = 64;
+int balanced_rows(int Ly, int cap) {
+    const int strips = (Ly + cap - 1) / cap;
+    return (Ly + strips - 1) / strips;
+}
+double padded_cells(const std::vector<Req *> &set, int nt) {
+    const int w = -2 * nt - 4;
+    double n = 0.0;
+    for (const Req *r : set) {
+        const int h = balanced_rows(r->p.Ly, kServePairRows);
+        n += (double)((r->p.Lx + w - 1) / w) * (w + 4) * (double)((r->p.Ly + h - 1) / h) * (h + 4);
+    }
+    return n;
+}
+void choose_geometry(swb_server *sv) {
+    bool pair = sv->precision == SWB_F32 || sv->precision == SWB_F16;
+    for (Req *r : sv->active) pair = pair && r->p.Lx % 2 == 0 && swb::pair_form_ok(r->a);
+    sv->nt = swb::kBatchNT;
+    if (pair) sv->nt = padded_cells(sv->active, -32) < padded_cells(sv->active, -64) ? -32 : -64;
+    for (Req *r : sv->active) {
+        const int h = pair ? balanced_rows(r->p.Ly, kServePairRows) : std::min(swb::kBatchRows, r->p.Ly);
+        swb::set_geometry(r->a, sv->nt, std::max(h, swb::kMinRows));
+    }
+}
+
+// Packed table of (lattice, strip) entries, the lattices' reducers first.
+std::vector<TileRef> tile_table(const std::vector<StepArgs> &args) {
     std::vector<TileRef> tiles, reducers;
-    for (size_t i = 0; i < sv->active.size(); ++i) {
-        const StepArgs &a = sv->active[i]->a;
-        args.push_back(a);
+    for (size_t i = 0; i < args.size(); ++i) {
+        const StepArgs &a = args[i];
         if (swb::needs_partials(a)) reducers.push_back({(int)i, -1, 0});
         for (int ty = 0; ty < a.tiles_y; ++ty)
             for (int tx = 0; tx < a.tiles_x; ++tx) tiles.push_back({(int)i, tx, ty});
     }
     tiles.insert(tiles.begin(), reducers.begin(), reducers.end());
-    if (args.size() > sv->cap_args) {
-        cudaFree(sv->d_args);
-        sv->cap_args = std::max<size_t>(args.size(), 2 * sv->cap_args);
-        if (cudaMalloc((void **)&sv->d_args, sv->cap_args * sizeof(StepArgs)) != cudaSuccess) return false;
+    return tiles;
+}
+
+// Device copy of a table on the tick stream, growing its buffer when needed.
+template <class T>
+bool put_table(swb_server *sv, const std::vector<T> &v, T **d, size_t *cap) {
+    if (v.size() > *cap) {
+        cudaFree(*d);
+        *d = nullptr;
+        *cap = std::max<size_t>(v.size(), 2 * *cap);
+        if (cudaMalloc((void **)d, *cap * sizeof(T)) != cudaSuccess) {
+            *cap = 0;
+            return false;
+        }
     }
-    if (tiles.size() > sv->cap_tiles) {
-        cudaFree(sv->d_tiles);
-        sv->cap_tiles = std::max<size_t>(tiles.size(), 2 * sv->cap_tiles);
-        if (cudaMalloc((void **)&sv->d_tiles, sv->cap_tiles * sizeof(TileRef)) != cudaSuccess) return false;
+    return cudaMemcpyAsync(*d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, sv->stream) ==
+           cudaSuccess;
+}
+
+// The tables of the resident set (and, for pair strips, of its one-column
+// fallback strips), uploaded on the tick stream.
+bool upload_table(swb_server *sv) {
+    choose_geometry(sv);
+    std::vector<StepArgs> args;
+    for (Req *r : sv->active) args.push_back(r->a);
+    const std::vector<TileRef> tiles = tile_table(args);
+    std::vector<StepArgs> fb;
+    std::vector<TileRef> fbt;
+    if (sv->nt < 0) {
+        for (const StepArgs &a : args) fb.push_back(swb::strip_fallback(a));
+        fbt = tile_table(fb);
     }
-    if (cudaMemcpyAsync(sv->d_args, args.data(), args.size() * sizeof(StepArgs), cudaMemcpyHostToDevice, sv->stream) != cudaSuccess)
+    if (!put_table(sv, args, &sv->d_args, &sv->cap_args) ||
+        !put_table(sv, tiles, &sv->d_tiles, &sv->cap_tiles))
         return false;
-    if (cudaMemcpyAsync(sv->d_tiles, tiles.data(), tiles.size() * sizeof(TileRef), cudaMemcpyHostToDevice, sv->stream) != cudaSuccess)
-        return false;
+    sv->ntiles = (int)tiles.size();
+    if (sv->nt < 0) {
+        if (!put_table(sv, fb, &sv->d_args_fb, &sv->cap_args_fb) ||
+            !put_table(sv, fbt, &sv->d_tiles_fb, &sv->cap_tiles_fb))
+            return false;
+        sv->ntiles_fb = (int)fbt.size();
+    }
+    // the copies read the host vectors: wait for them before they go
     return cudaStreamSynchronize(sv->stream) == cudaSuccess;
 }
 
-int count_tiles(swb_server *sv) {
-    int n = 0;
-    for (Req *r : sv->active) n += r->a.tiles_x * r->a.tiles_y + (swb::needs_partials(r->a) ? 1 : 0);
-    return n;
-}
-
-// Tile tables of the resident set: the strips of every lattice (pair strips
-// when every lattice allows them) and, for pair strips, the one-column
-// strips of the iterations the pair form leaves out.
 void worker_main(swb_server *sv) {
     cudaSetDevice(sv->device);
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, sv->device);
-    const int occ = swb::batch_blocks_per_sm(sv->precision, swb::kBatchNT);
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;  // device time of a tick
+    cudaEventCreate(&ev0);
+    cudaEventCreate(&ev1);
+    const int occ1 = swb::batch_blocks_per_sm(sv->precision, swb::kBatchNT);
     std::vector<Req *> joining;  // initialised on the copy stream; join at the next tick
     std::vector<Req *> leaving;  // finished at the last tick; results still to download
     bool changed = false;
@@ -277,20 +343,36 @@ void worker_main(swb_server *sv) {
         const double tb = sv->now();
         cudaError_t e = cudaSuccess;
         if (tick > 0) {
-            const int ntiles = count_tiles(sv);
-            const int grid = std::min(ntiles, sms * occ);
-            bool gen = false, tau1 = true, rare = false;  // the general kernel if any resident request needs it
+            // the general kernel if any resident request needs it
+            bool gen = false, tau1 = true, rare = false, wave = false;
             for (Req *r : sv->active) {
                 gen = gen || swb::step_general(r->a);
                 rare = rare || swb::step_rare(r->a);
                 tau1 = tau1 && r->a.tau_is_one;
+                wave = wave || r->a.theta_mode == swb::THETA_WAVE;
             }
-            for (int64_t k = 0; k < tick && e == cudaSuccess; ++k)
-                e = swb::launch_batch_step(sv->precision, swb::kBatchNT, gen,
-                                           tau1 && !(sv->fresh_pending && k == 0), sv->d_args,
-                                           sv->d_tiles, ntiles, grid, (int)k, sv->stream, rare);
+            // pair strips: one CTA per table entry (the hardware balances the
+            // uneven strips; on GB300 faster than persistent CTAs walking the
+            // table); one-column strips: persistent CTAs
+            const int grid = sv->nt < 0 ? sv->ntiles : std::min(sv->ntiles, sms * occ1);
+            const int grid_fb = std::min(sv->ntiles_fb, sms * occ1);
+            cudaEventRecord(ev0, sv->stream);
+            for (int64_t k = 0; k < tick && e == cudaSuccess; ++k) {
+                const bool steady = tau1 && !(sv->fresh_pending && k == 0);
+                if (sv->nt < 0 && !steady)  // an iteration the pair form leaves out
+                    e = swb::launch_batch_step(sv->precision, swb::kBatchNT, gen, steady, sv->d_args_fb,
+                                               sv->d_tiles_fb, sv->ntiles_fb, grid_fb, (int)k,
+                                               sv->stream, rare);
+                else if (sv->nt < 0)
+                    e = swb::launch_batch_step(sv->precision, sv->nt, wave, steady, sv->d_args,
+                                               sv->d_tiles, sv->ntiles, grid, (int)k, sv->stream);
+                else
+                    e = swb::launch_batch_step(sv->precision, sv->nt, gen, steady, sv->d_args,
+                                               sv->d_tiles, sv->ntiles, grid, (int)k, sv->stream, rare);
+            }
             if (e == cudaSuccess)
                 e = swb::launch_batch_advance(sv->d_args, (int)sv->active.size(), (int)tick, sv->stream);
+            cudaEventRecord(ev1, sv->stream);
             sv->fresh_pending = false;
         }
         // 2. while it runs, on the copy stream: the results of the requests
@@ -352,12 +434,17 @@ void worker_main(swb_server *sv) {
             if (tick > 0) {
                 sv->st.busy_seconds += sv->now() - tb;
                 sv->st.ticks++;
+                float ms = 0.f;
+                if (e == cudaSuccess && cudaEventElapsedTime(&ms, ev0, ev1) == cudaSuccess)
+                    sv->st.device_seconds += ms * 1e-3;
             }
             if (e != cudaSuccess) sv->err = std::string("tick: ") + cudaGetErrorString(e);
         }
     }
     cudaStreamSynchronize(sv->stream);
     cudaStreamSynchronize(sv->copy);
+    cudaEventDestroy(ev0);
+    cudaEventDestroy(ev1);
 }
 
 }  // namespace
@@ -411,6 +498,8 @@ int swb_server_destroy(swb_server *sv) {
     cudaStreamSynchronize(sv->stream);
     cudaFree(sv->d_args);
     cudaFree(sv->d_tiles);
+    cudaFree(sv->d_args_fb);
+    cudaFree(sv->d_tiles_fb);
     cudaFree(sv->staging);
     if (sv->pool) cudaMemPoolDestroy(sv->pool);
     cudaStreamDestroy(sv->stream);

@@ -174,15 +174,22 @@ int pair_blocks_per_sm(int precision, int nt) {
 // Resident CTAs per SM of the batch kernel most launches use (the steady
 // form at the default width: fewer registers, so more CTAs).  The table walk
 // needs no co-residency, so a grid sized for it is valid for every form.
-int batch_blocks_per_sm_f32(int precision, int nt) {
+int batch_blocks_per_sm_f32(int precision, int nt, bool wave) {
     int n = 0;
-    if (nt < 0) {
-        if (nt == -32)
-            DISPATCH_STORE(precision, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_pair_kernel<S, 32, false>, 32, 0));
-        else if (nt == -128)
-            DISPATCH_STORE(precision, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_pair_kernel<S, 128, false>, 128, 0));
+    if (nt < 0) {  // the pair kernel of the θ-wave form, or the plain one
+        auto occ = [&](auto w) {
+            constexpr bool W = decltype(w)::value;
+            if (nt == -32)
+                DISPATCH_STORE(precision, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_pair_kernel<S, 32, W>, 32, 0));
+            else if (nt == -128)
+                DISPATCH_STORE(precision, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_pair_kernel<S, 128, W>, 128, 0));
+            else
+                DISPATCH_STORE(precision, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_pair_kernel<S, 64, W>, 64, 0));
+        };
+        if (wave)
+            occ(std::true_type{});
         else
-            DISPATCH_STORE(precision, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_pair_kernel<S, 64, false>, 64, 0));
+            occ(std::false_type{});
         return n < 1 ? 1 : n;
     }
     if (nt == kBatchNT)

@@ -2025,8 +2025,17 @@ __global__ void __launch_bounds__(NT) batch_step_kernel(const StepArgs *__restri
 // Batch on pair strips: the table's strips are pair strips of NT threads;
 // every lattice is at a steady τ = 1 iteration without rare forces or θ
 // field (WAVE: some lattice has the θ wave) and has even Lx (the host knows).
+// Register budget: left alone the compiler gives the WAVE form 148 registers
+// (6 CTAs of 64 threads per SM) and the plain form 128; capped at 128 and 96
+// (8 and 10 CTAs) they spill nothing and 24 bytes.  Measured on GB300: the
+// θ-wave serving mix 53 -> 74 GLUPS at 128, the plain ensemble 70 -> 74
+// GLUPS at 96 (the WAVE form at 96 spills 80 bytes and is slower).
+template <int NT, bool WAVE>
+constexpr int batch_pair_min_blocks() {
+    return 65536 / ((WAVE || NT < 64 ? 128 : 96) * NT);
+}
 template <class S, int NT, bool WAVE>
-__global__ void __launch_bounds__(NT) batch_pair_kernel(const StepArgs *__restrict__ args,
+__global__ void __launch_bounds__(NT, (batch_pair_min_blocks<NT, WAVE>())) batch_pair_kernel(const StepArgs *__restrict__ args,
                                                                  const TileRef *__restrict__ tiles,
                                                                  int ntiles, int k) {
     __shared__ __align__(16) PairSmem<NT> sm;

@@ -59,7 +59,8 @@ class ServerStats(C.Structure):
     _fields_ = [("submitted", C.c_int64), ("admitted", C.c_int64), ("completed", C.c_int64),
                 ("rejected", C.c_int64), ("queued", C.c_int64), ("running", C.c_int64),
                 ("lattice_updates", C.c_double), ("busy_seconds", C.c_double),
-                ("hbm_in_use", C.c_size_t), ("hbm_budget", C.c_size_t), ("ticks", C.c_int64)]
+                ("hbm_in_use", C.c_size_t), ("hbm_budget", C.c_size_t), ("ticks", C.c_int64),
+                ("device_seconds", C.c_double)]
 
 
 class SwbError(RuntimeError):

@@ -430,6 +430,32 @@ def test_server_alone_equals_mixed():
     sv.close()
 
 
+@pytest.mark.parametrize("T", [np.float32, np.float16])
+def test_server_pair_and_one_column_sets(T):
+    """The resident set runs as pair strips while every lattice has an even
+    width, as one-column strips once an odd-width lattice joins; a lattice's
+    result is the single state's either way, in FP32 and FP16 storage."""
+    sv = sw.Server(1 << 30, T=T, steps_per_tick=40)
+    cases = [((64, 100), 150, 3), ((128, 64), 90, 4), ((62, 130), 170, 5)]
+    rids = [sv.submit(sysc(lx, ly, theta=1 / 7), rough(lx, ly, k), n, dtheta=1 / 36, v=1 / 98)
+            for (lx, ly), n, k in cases]
+    outs = [_wait(sv, r, shape) for r, (shape, _, _) in zip(rids, cases)]
+    odd = ((63, 40), 120, 6)
+    rid_odd = sv.submit(sysc(63, 40), rough(63, 40, 6), 120)
+    rid_even = sv.submit(sysc(64, 100, theta=1 / 7), rough(64, 100, 3), 150, dtheta=1 / 36, v=1 / 98)
+    out_odd = _wait(sv, rid_odd, (63, 40))
+    out_even = _wait(sv, rid_even, (64, 100))
+    sv.close()
+    assert np.array_equal(out_even, outs[0])
+    for ((lx, ly), n, k), out in zip(cases + [odd], outs + [out_odd]):
+        st = sw.Sys(sysc(lx, ly, theta=1 / 7) if (lx, ly) != (63, 40) else sysc(63, 40), "GB300", T=T)
+        st.height = rough(lx, ly, k)
+        if (lx, ly) != (63, 40):
+            st.set_theta_wave(1 / 7, 1 / 36, 1 / 98)
+        st.step(n)
+        assert np.array_equal(out, st.height), (lx, ly)
+
+
 def _wait(sv, rid, shape, timeout=60):
     import time
     t0 = time.time()
