@@ -747,6 +747,9 @@ def profile_case(args):
         # the first 64 members of the coalescence ensemble, batched (~0.7 GB)
         members, _ = configs.ensemble(64)
         b = sw.Batch([m.sysc for m in members], T=T)
+        if args.geometry:  # e.g. -64,32: the pair strips the autotuner picks for the ensemble
+            nt, hh = (int(v) for v in args.geometry.split(","))
+            b.set_geometry(nt, hh)
         for i, m in enumerate(members):
             b.set_height(i, m.h0)
         b.step(args.case_steps)
@@ -754,7 +757,7 @@ def profile_case(args):
         tx, ty, spg = b.tile()
         print(json.dumps({"case": args.profile_case, "precision": args.precision,
                           "lattices": len(members), "cells": sum(m.sysc.Lx * m.sysc.Ly for m in members),
-                          "strip": [tx, ty], "steps": args.case_steps}))
+                          "strip": [tx, ty], "geometry": list(b.geometry()), "steps": args.case_steps}))
         b.close()
         return
     if args.profile_case == "rt512":
