@@ -428,10 +428,16 @@ def lattice_2048_run(sw, np, torch, hbm, precs=("f32", "f16", "f64"), geometry="
     n = 2048
     h0 = np.asfortranarray(1.0 + rng.uniform(-0.1, 0.1, (n, n)))
     s2 = sw.SysConst(n, n, sw.Taumucs())
-    for prec, T, steps in (("f32", np.float32, 300), ("f16", np.float16, 300), ("f64", np.float64, 30)):
-        if prec not in precs:
+    # f16_no_controller: FP16 storage with its mass controller off (on by
+    # default: FP16 cannot hold the rounding residue, and the controller's
+    # exact per-step mass sum costs ~7 % of the step)
+    for prec, T, steps in (("f32", np.float32, 300), ("f16", np.float16, 300),
+                           ("f16_no_controller", np.float16, 300), ("f64", np.float64, 30)):
+        if prec.split("_")[0] not in precs:
             continue
         st = sw.Sys(s2, "GB300", T=T)
+        if prec == "f16_no_controller":
+            st.set_mass_correction(False)
         if geometry:
             st.set_geometry(*(int(v) for v in geometry.split(",")))
         stream = torch.cuda.Stream()
@@ -444,7 +450,7 @@ def lattice_2048_run(sw, np, torch, hbm, precs=("f32", "f16", "f64"), geometry="
         e1.record(stream)
         e1.synchronize()
         t = e0.elapsed_time(e1) / 1e3 / steps
-        ach = B_ALG[prec] * n * n / t / 1e9
+        ach = B_ALG[prec.split("_")[0]] * n * n / t / 1e9
         out.setdefault("lattice_2048", {})[prec] = {
             "MLUPS": n * n / t / 1e6, "launch_us": t * 1e6, "achieved_GBs": ach, "frac": ach / hbm,
             "geometry": list(st.geometry())}
