@@ -58,6 +58,8 @@ def parse():
     ap.add_argument("--step-mode", default="per_iteration", choices=["per_iteration", "multi"],
                     help="launch form for --profile-case")
     ap.add_argument("--case-steps", type=int, default=12)
+    ap.add_argument("--mass-correction", default="default", choices=["default", "on", "off"],
+                    help="mass controller of --profile-case (default: on for FP16 only)")
     ap.add_argument("--size", type=int, default=0, help="lattice side of --workload dewetting")
     ap.add_argument("--dry-run", action="store_true",
                     help="rank set-up and ensemble sharding only, no GPU work")
@@ -422,12 +424,17 @@ def run_ours(args):
 
 def lattice_2048_run(sw, np, torch, hbm, precs=("f32", "f16", "f64"), geometry=""):
     """HBM-bound 2048² runs (the state is larger than L2), event-timed on the
-    state's stream; `geometry` "NT,H" overrides the size rule's strips."""
+    state's stream; `geometry` "NT,H" overrides the size rule's strips.
+    FP32 also end to end (time_loop with pinned Float64 host buffers: h, ux,
+    uy up and h down every call) and against Float64 after the same
+    iterations (relative L2 of h)."""
     out = {}
     rng = np.random.default_rng(3)
     n = 2048
     h0 = np.asfortranarray(1.0 + rng.uniform(-0.1, 0.1, (n, n)))
     s2 = sw.SysConst(n, n, sw.Taumucs())
+    h_f32 = None
+    total_f32 = 0
     # f16_no_controller: FP16 storage with its mass controller off (on by
     # default: FP16 cannot hold the rounding residue, and the controller's
     # exact per-step mass sum costs ~7 % of the step)
@@ -451,11 +458,50 @@ def lattice_2048_run(sw, np, torch, hbm, precs=("f32", "f16", "f64"), geometry="
         e1.synchronize()
         t = e0.elapsed_time(e1) / 1e3 / steps
         ach = B_ALG[prec.split("_")[0]] * n * n / t / 1e9
-        out.setdefault("lattice_2048", {})[prec] = {
-            "MLUPS": n * n / t / 1e6, "launch_us": t * 1e6, "achieved_GBs": ach, "frac": ach / hbm,
-            "geometry": list(st.geometry())}
+        line = {"MLUPS": n * n / t / 1e6, "launch_us": t * 1e6, "achieved_GBs": ach,
+                "frac": ach / hbm, "geometry": list(st.geometry())}
+        if prec == "f32":
+            h_f32, total_f32 = st.height, 64 + steps
+            line["e2e"] = lattice_2048_e2e(sw, np, torch, st, s2, h0)
+        if prec == "f64" and h_f32 is not None:
+            st.step(total_f32 - 64 - steps)
+            h64 = st.height
+            line_f32 = out["lattice_2048"]["f32"]
+            line_f32["check"] = {
+                "vs": "GPU Float64 path (bit-identical to the oracle)",
+                "after_time_steps": total_f32,
+                "rel_l2_h": float(np.linalg.norm(h_f32 - h64) / np.linalg.norm(h64)),
+                "rel_l2_h_minus_1": float(np.linalg.norm(h_f32 - h64) / np.linalg.norm(h64 - 1.0))}
+        out.setdefault("lattice_2048", {})[prec] = line
         del st
     return out
+
+
+def lattice_2048_e2e(sw, np, torch, st, sysc, h0, calls=5, tmax=300):
+    """MLUPS through time_loop with pinned Float64 host buffers (h, ux, uy
+    uploaded and h downloaded every call, inside the timed region)."""
+    def pinned():
+        return torch.empty((sysc.Ly, sysc.Lx), dtype=torch.float64, pin_memory=True).numpy().T
+
+    h_in, zeros, h_out = pinned(), pinned(), pinned()
+    h_in[...] = h0
+    zeros[...] = 0.0
+    e2e_sys = sw.SysConst(sysc.Lx, sysc.Ly, sysc.param.replace(Tmax=tmax, tdump=tmax))
+    st.set_stream(None)
+    times = []
+    for k in range(calls + 1):
+        t0 = time.perf_counter()
+        st.height = h_in
+        st.velx = zeros
+        st.vely = zeros
+        sw.time_loop(e2e_sys, st)
+        st.get("height", out=h_out)
+        if k > 0:  # the first call warms up
+            times.append(time.perf_counter() - t0)
+    nb = sysc.Lx * sysc.Ly * 8
+    return {"MLUPS": sysc.Lx * sysc.Ly * tmax * len(times) / sum(times) / 1e6,
+            "time_steps_per_call": tmax, "h2d_bytes_per_call": 3 * nb, "d2h_bytes_per_call": nb,
+            "host_buffers": "pinned"}
 
 
 def side_runs(sw, L, np, torch, hbm):
@@ -783,12 +829,14 @@ def profile_case(args):
     else:
         st.set_geometry(0, 0)
     st.set_step_mode(args.step_mode)
+    if args.mass_correction != "default":
+        st.set_mass_correction(args.mass_correction == "on")
     st.height = h0
     st.step(args.case_steps)
     st.sync()
     print(json.dumps({"case": args.profile_case, "precision": args.precision,
                       "geometry": st.geometry(), "form": st.step_mode(),
-                      "steps": args.case_steps}))
+                      "mass_correction": args.mass_correction, "steps": args.case_steps}))
 
 
 def launch_ranks(args) -> int:
