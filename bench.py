@@ -600,7 +600,7 @@ def ensemble_run(sw, np, count=512, steps=200, plain_sample=8, geometry="", rank
 
 
 def serving_run(sw, np, duration=12.0, rate=200.0, budget=24 << 30, steps_per_tick=100,
-                queue_limit=256, policy="sjf", max_cells=16 << 20):
+                queue_limit=256, policy="sjf", max_cells=16 << 20, geometry=None):
     """Poisson arrivals (200/s) of thin-film solves (sides 64..2048, 1k-100k
     steps, moving wettability, g in [-1e-3, 0]) into the server for
     `duration` seconds.  The offered load is ~300x what one GPU serves, so
@@ -612,6 +612,8 @@ def serving_run(sw, np, duration=12.0, rate=200.0, budget=24 << 30, steps_per_ti
     sv = sw.Server(budget, T=np.float32, steps_per_tick=steps_per_tick)
     sv.set_queue_limit(queue_limit)
     sv.set_policy(policy, max_cells)
+    if geometry:  # (nt, rows): fixed strips instead of the server's choice
+        sv.set_geometry(*geometry)
     t0 = time.perf_counter()
     pending, done, rejected, i = {}, [], 0, 0
     sizes, failed = [], {}

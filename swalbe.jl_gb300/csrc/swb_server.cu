@@ -85,6 +85,8 @@ struct swb_server {
     cudaStream_t copy = nullptr;    // admissions and results, beside the ticks
     cudaMemPool_t pool = nullptr;
     int nt = swb::kBatchNT;         // strip geometry of the resident set (< 0: pair strips)
+    int want_nt = 0, want_rows = 0; // swb_server_set_geometry (0: chosen per set)
+    bool geometry_dirty = false;
     bool fresh_pending = false;     // lattices that joined are at their first iteration
     StepArgs *d_args = nullptr;
     TileRef *d_tiles = nullptr;
@@ -193,9 +195,12 @@ void choose_geometry(swb_server *sv) {
     bool pair = sv->precision == SWB_F32 || sv->precision == SWB_F16;
     for (Req *r : sv->active) pair = pair && r->p.Lx % 2 == 0 && swb::pair_form_ok(r->a);
     sv->nt = swb::kBatchNT;
-    if (pair) sv->nt = padded_cells(sv->active, -32) < padded_cells(sv->active, -64) ? -32 : -64;
+    const int cap = sv->want_nt != 0 ? sv->want_rows : kServePairRows;
+    if (pair)
+        sv->nt = sv->want_nt != 0 ? sv->want_nt
+                                  : (padded_cells(sv->active, -32) < padded_cells(sv->active, -64) ? -32 : -64);
     for (Req *r : sv->active) {
-        const int h = pair ? balanced_rows(r->p.Ly, kServePairRows) : std::min(swb::kBatchRows, r->p.Ly);
+        const int h = pair ? balanced_rows(r->p.Ly, cap) : std::min(swb::kBatchRows, r->p.Ly);
         swb::set_geometry(r->a, sv->nt, std::max(h, swb::kMinRows));
     }
 }
@@ -331,6 +336,11 @@ void worker_main(swb_server *sv) {
         // 1. the tick: every resident request advances together (a request
         // whose steps run out stops inside the tick; the tick is as long as
         // the longest remaining request allows, at most steps_per_tick)
+        {
+            std::lock_guard<std::mutex> g(sv->mu);
+            if (sv->geometry_dirty) changed = true;
+            sv->geometry_dirty = false;
+        }
         if (changed && !sv->active.empty() && !upload_table(sv)) {
             set_error(sv, "tile table upload failed");
             std::this_thread::sleep_for(std::chrono::milliseconds(10));
@@ -571,6 +581,19 @@ int swb_server_set_queue_limit(swb_server *sv, int64_t max_queued) {
     if (!sv || max_queued < 1) return sfail(SWB_ERR_ARG, "bad arguments");
     std::lock_guard<std::mutex> g(sv->mu);
     sv->max_queued = max_queued;
+    return SWB_OK;
+}
+
+int swb_server_set_geometry(swb_server *sv, int nt, int rows) {
+    if (!sv || (nt != 0 && nt != -32 && nt != -64) || (nt != 0 && rows < swb::kMinRows))
+        return sfail(SWB_ERR_ARG, "bad arguments");
+    {
+        std::lock_guard<std::mutex> g(sv->mu);
+        sv->want_nt = nt;
+        sv->want_rows = nt != 0 ? rows : 0;
+        sv->geometry_dirty = true;
+    }
+    sv->cv.notify_all();
     return SWB_OK;
 }
 

@@ -135,6 +135,7 @@ def lib() -> C.CDLL:
             "swb_server_submit": (i, [p, PP, p, d, d, d, i64, C.POINTER(i64)]),
             "swb_server_set_queue_limit": (i, [p, i64]),
             "swb_server_set_policy": (i, [p, i, i64]),
+            "swb_server_set_geometry": (i, [p, i, i]),
             "swb_count_droplets": (i, [p, i, i, d, C.POINTER(i64)]),
             "swb_set_thermal_seed": (i, [p, C.c_uint64]),
             "swb_thermal_field": (i, [p, i64, p, p]),

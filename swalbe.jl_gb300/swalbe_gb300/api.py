@@ -846,6 +846,12 @@ class Server:
     def set_queue_limit(self, n: int) -> None:
         check(lib().swb_server_set_queue_limit(self._h, int(n)))
 
+    def set_geometry(self, nt: int = 0, rows: int = 0) -> None:
+        """Strips of the resident set: nt = 0 chosen per set (default), or
+        pair strips of nt = -32 / -64 threads with rows balanced up to
+        `rows` whenever every lattice allows them."""
+        check(lib().swb_server_set_geometry(self._h, int(nt), int(rows)))
+
     def set_policy(self, policy: str = "fifo", max_resident_cells: int = 0) -> None:
         """"fifo" or "sjf" (shortest job first by Lx*Ly*nsteps, shedding the
         largest queued job when the queue is full), and an optional bound
