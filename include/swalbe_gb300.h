@@ -373,10 +373,11 @@ int swb_server_set_queue_limit(swb_server *sv, int64_t max_queued);
 int swb_server_set_policy(swb_server *sv, int policy, int64_t max_resident_cells);
 /* Strip geometry of the resident set.  nt = 0 (default): chosen whenever the
  * set changes (pair strips of 60 or 124 columns, whichever processes fewer
- * cells, rows balanced up to 64, when every lattice allows pair strips;
- * one-column strips of 64 threads otherwise).  nt = -32 or -64: those pair
- * strips whenever every lattice allows them, with each lattice's rows
- * balanced up to `rows` (>= 2).  Results do not depend on the geometry. */
+ * cells, when every lattice allows pair strips; one-column strips of 64
+ * threads otherwise), each lattice's rows balanced up to `rows` (0: 64).
+ * nt = -32 or -64: those pair strips whenever every lattice allows them,
+ * rows balanced up to `rows` (>= 2).  Results do not depend on the
+ * geometry. */
 int swb_server_set_geometry(swb_server *sv, int nt, int rows);
 /* Queues a solve: params (Lx, Ly, γ, θ, g, ...), initial height (copied),
  * moving wettability (dtheta = 0 for none) and the step count. */

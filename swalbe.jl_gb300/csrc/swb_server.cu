@@ -195,7 +195,7 @@ void choose_geometry(swb_server *sv) {
     bool pair = sv->precision == SWB_F32 || sv->precision == SWB_F16;
     for (Req *r : sv->active) pair = pair && r->p.Lx % 2 == 0 && swb::pair_form_ok(r->a);
     sv->nt = swb::kBatchNT;
-    const int cap = sv->want_nt != 0 ? sv->want_rows : kServePairRows;
+    const int cap = sv->want_rows > 0 ? sv->want_rows : kServePairRows;
     if (pair)
         sv->nt = sv->want_nt != 0 ? sv->want_nt
                                   : (padded_cells(sv->active, -32) < padded_cells(sv->active, -64) ? -32 : -64);
@@ -585,12 +585,13 @@ int swb_server_set_queue_limit(swb_server *sv, int64_t max_queued) {
 }
 
 int swb_server_set_geometry(swb_server *sv, int nt, int rows) {
-    if (!sv || (nt != 0 && nt != -32 && nt != -64) || (nt != 0 && rows < swb::kMinRows))
+    if (!sv || (nt != 0 && nt != -32 && nt != -64) || (rows != 0 && rows < swb::kMinRows) ||
+        (nt != 0 && rows == 0))
         return sfail(SWB_ERR_ARG, "bad arguments");
     {
         std::lock_guard<std::mutex> g(sv->mu);
         sv->want_nt = nt;
-        sv->want_rows = nt != 0 ? rows : 0;
+        sv->want_rows = rows;
         sv->geometry_dirty = true;
     }
     sv->cv.notify_all();

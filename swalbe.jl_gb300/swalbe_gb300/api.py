@@ -848,8 +848,8 @@ class Server:
 
     def set_geometry(self, nt: int = 0, rows: int = 0) -> None:
         """Strips of the resident set: nt = 0 chosen per set (default), or
-        pair strips of nt = -32 / -64 threads with rows balanced up to
-        `rows` whenever every lattice allows them."""
+        pair strips of nt = -32 / -64 threads whenever every lattice allows
+        them; each lattice's rows balanced up to `rows` (0 with nt = 0: 64)."""
         check(lib().swb_server_set_geometry(self._h, int(nt), int(rows)))
 
     def set_policy(self, policy: str = "fifo", max_resident_cells: int = 0) -> None:
