@@ -456,6 +456,32 @@ def test_server_pair_and_one_column_sets(T):
         assert np.array_equal(out, st.height), (lx, ly)
 
 
+@pytest.mark.parametrize("geo", [(-64, 32), (-32, 16), (0, 48)])
+def test_server_fixed_geometry_equals_single(geo):
+    """swb_server_set_geometry changes the strips, not the results."""
+    sv = sw.Server(1 << 30, T=np.float32, steps_per_tick=30)
+    sv.set_geometry(*geo)
+    cases = [((128, 100), 95, 7), ((64, 64), 70, 8)]
+    rids = [sv.submit(sysc(lx, ly, theta=1 / 6), rough(lx, ly, k), n, dtheta=1 / 36, v=1 / 98)
+            for (lx, ly), n, k in cases]
+    outs = [_wait(sv, r, shape) for r, (shape, _, _) in zip(rids, cases)]
+    sv.close()
+    for ((lx, ly), n, k), out in zip(cases, outs):
+        st = sw.Sys(sysc(lx, ly, theta=1 / 6), "GB300", T=np.float32)
+        st.height = rough(lx, ly, k)
+        st.set_theta_wave(1 / 6, 1 / 36, 1 / 98)
+        st.step(n)
+        assert np.array_equal(out, st.height), (geo, lx, ly)
+
+
+def test_server_geometry_rejects_bad_arguments():
+    sv = sw.Server(1 << 28, T=np.float32)
+    for nt, rows in ((-128, 32), (64, 32), (-64, 0), (0, 1)):
+        with pytest.raises(sw.SwbError):
+            sv.set_geometry(nt, rows)
+    sv.close()
+
+
 def _wait(sv, rid, shape, timeout=60):
     import time
     t0 = time.time()
