@@ -11,7 +11,10 @@
 // of the requests that finished at the previous tick (and frees their pool
 // memory) and initialises the newly admitted ones, which join at the next
 // tick.  Each lattice's arithmetic is independent of which others share the
-// launch, so a result is bit-identical alone and in the mix.
+// launch, so a result is bit-identical alone and in the mix.  The strip
+// geometry is chosen for the resident set whenever it changes
+// (choose_geometry): pair strips when every lattice allows them, 60 or 124
+// columns wide by the cells either would process.
 //
 // Resident requests advance in lock step, so a request's latency is its
 // step count times the time of one step of the whole resident set.  The
