@@ -88,8 +88,9 @@ struct swb_server {
     cudaStream_t copy = nullptr;    // admissions and results, beside the ticks
     cudaMemPool_t pool = nullptr;
     int nt = swb::kBatchNT;         // strip geometry of the resident set (< 0: pair strips)
-    int want_nt = 0, want_rows = 0; // swb_server_set_geometry (0: chosen per set)
-    bool geometry_dirty = false;
+    int want_nt = 0, want_rows = 0; // swb_server_set_geometry (0: chosen per set), under mu
+    bool geometry_dirty = false;    // under mu
+    int geo_nt = 0, geo_rows = 0;   // the worker's copy of want_nt / want_rows
     bool fresh_pending = false;     // lattices that joined are at their first iteration
     StepArgs *d_args = nullptr;
     TileRef *d_tiles = nullptr;
@@ -198,10 +199,10 @@ void choose_geometry(swb_server *sv) {
     bool pair = sv->precision == SWB_F32 || sv->precision == SWB_F16;
     for (Req *r : sv->active) pair = pair && r->p.Lx % 2 == 0 && swb::pair_form_ok(r->a);
     sv->nt = swb::kBatchNT;
-    const int cap = sv->want_rows > 0 ? sv->want_rows : kServePairRows;
+    const int cap = sv->geo_rows > 0 ? sv->geo_rows : kServePairRows;
     if (pair)
-        sv->nt = sv->want_nt != 0 ? sv->want_nt
-                                  : (padded_cells(sv->active, -32) < padded_cells(sv->active, -64) ? -32 : -64);
+        sv->nt = sv->geo_nt != 0 ? sv->geo_nt
+                                 : (padded_cells(sv->active, -32) < padded_cells(sv->active, -64) ? -32 : -64);
     for (Req *r : sv->active) {
         const int h = pair ? balanced_rows(r->p.Ly, cap) : std::min(swb::kBatchRows, r->p.Ly);
         swb::set_geometry(r->a, sv->nt, std::max(h, swb::kMinRows));
@@ -343,6 +344,8 @@ void worker_main(swb_server *sv) {
             std::lock_guard<std::mutex> g(sv->mu);
             if (sv->geometry_dirty) changed = true;
             sv->geometry_dirty = false;
+            sv->geo_nt = sv->want_nt;
+            sv->geo_rows = sv->want_rows;
         }
         if (changed && !sv->active.empty() && !upload_table(sv)) {
             set_error(sv, "tile table upload failed");

@@ -920,7 +920,12 @@ __device__ __forceinline__ float2 force_fast(const CellConst<float> &cc, float h
 // only); *hlo_p: the rounding residue of the pulled height (not read for a
 // fresh step).  Shared by every FP32-arithmetic kernel, so that they all
 // round identically.
-template <class S, bool FRESH, bool TAU1>
+// HB_ONLY (FP16 storage): the caller stores planes 1..8 from hb and reads
+// only fo[0], so fo[1..8] may hold the stored values x kScale, and at τ = 1
+// the populations are computed x kScale from the start (the weights and
+// sources scaled by the power of two kScale: the same bits, fewer
+// multiplications).
+template <class S, bool FRESH, bool TAU1, bool HB_ONLY = false>
 __device__ __forceinline__ void collide_fast(const CellConst<float> &cc, float h, float ux,
                                              float uy, float Fx, float Fy, float hft,
                                              const float *fq, int cell, long long tt,
@@ -947,16 +952,19 @@ __device__ __forceinline__ void collide_fast(const CellConst<float> &cc, float h
     // Opposite populations (q+, q-) share their equilibrium's even part
     // A and odd part B (feq = A ± B, src/equilibrium.jl:67-114) and their
     // force source ±S (src/collide.jl:80-89).
+    // populations computed x ks (FP16 planes stored from them directly)
+    constexpr bool kScaled = S::kHalf && TAU1 && HB_ONLY;
+    constexpr float ks = kScaled ? StoreF16::kScale : 1.0f;
     const R vsq = __fmaf_rn(ux, ux, uy * uy);
     const R base = __fmaf_rn(R(1.5) * cc.g, h, R(-1.5) * vsq);
-    const R w1h = h * R(1.0 / 9.0), w5h = h * R(1.0 / 36.0);
+    const R w1h = h * (R(1.0 / 9.0) * ks), w5h = h * (R(1.0 / 36.0) * ks);
     // the k = (1, 2) and (5, 6) directions as packed pairs: velocities
     // cu = (ux, uy) and (ux + uy, uy - ux), weights w1 h and w5 h, sources
     // (Fx, Fy) / 3 and (Fx + Fy, Fy - Fx) / 24
     const float2 U = f2(ux, uy), F2 = f2(Fx, Fy);
     const float2 CU[2] = {U, add2(U, f2(uy, -ux))};
-    const float2 SQ[2] = {mul2(f2(1.0f / 3.0f, 1.0f / 3.0f), F2),
-                          mul2(f2(1.0f / 24.0f, 1.0f / 24.0f), add2(F2, f2(Fy, -Fx)))};
+    const float2 SQ[2] = {mul2(f2(1.0f / 3.0f * ks, 1.0f / 3.0f * ks), F2),
+                          mul2(f2(1.0f / 24.0f * ks, 1.0f / 24.0f * ks), add2(F2, f2(Fy, -Fx)))};
     const R wq[2] = {w1h, w5h};
     const float2 BASE = f2(base, base);
     constexpr int qp[2] = {1, 5}, qm[2] = {3, 7};  // and qp + 1, qm + 1
@@ -979,10 +987,19 @@ __device__ __forceinline__ void collide_fast(const CellConst<float> &cc, float h
         }
         if constexpr (S::kHalf) {
             const float2 sc = f2(S::kScale, S::kScale), inv = f2(S::kInv, S::kInv);
-            hb[2 * j] = __float22half2_rn(mul2(P, sc));
-            hb[2 * j + 1] = __float22half2_rn(mul2(M, sc));
-            const float2 rp = mul2(__half22float2(hb[2 * j]), inv);
-            const float2 rm = mul2(__half22float2(hb[2 * j + 1]), inv);
+            if constexpr (kScaled) {
+                hb[2 * j] = __float22half2_rn(P);
+                hb[2 * j + 1] = __float22half2_rn(M);
+            } else {
+                hb[2 * j] = __float22half2_rn(mul2(P, sc));
+                hb[2 * j + 1] = __float22half2_rn(mul2(M, sc));
+            }
+            // the values the planes hold (x kScale with HB_ONLY)
+            float2 rp = __half22float2(hb[2 * j]), rm = __half22float2(hb[2 * j + 1]);
+            if constexpr (!HB_ONLY) {
+                rp = mul2(rp, inv);
+                rm = mul2(rm, inv);
+            }
             fo[qp[j]] = rp.x;
             fo[qp[j] + 1] = rp.y;
             fo[qm[j]] = rm.x;
@@ -998,7 +1015,9 @@ __device__ __forceinline__ void collide_fast(const CellConst<float> &cc, float h
     if constexpr (!FRESH) hlo = *hlo_p;
     // Σ_q fpost_q = (1-1/τ) Σ ft + Σ feq/τ = h once h is the pulled mass
     const R mc = (TAU1 || !FRESH) ? h : cc.omeg * hft + cc.invtau * h;
-    const R ssum = small8(fo);
+    // Σ_{q>0} f_q as stored (with HB_ONLY, FP16 values x kScale: the sum of
+    // the scaled values times 1/kScale is the same bits)
+    const R ssum = (S::kHalf && HB_ONLY) ? small8(fo) * R(StoreF16::kInv) : small8(fo);
     const R f0 = mc - ssum;
     const R e = (mc - f0) - ssum;
     const R c = e + hlo + cc.corr;
@@ -1093,7 +1112,7 @@ __device__ __forceinline__ void collide_cell(const StepArgs &a,
     } else {
         float fo[9];
         [[maybe_unused]] __half2 hb[4];
-        collide_fast<S, FRESH, TAU1>(cc, h, ux, uy, Fx, Fy, hft, fq, cell, tt, hlo_p, fo, hb);
+        collide_fast<S, FRESH, TAU1, true>(cc, h, ux, uy, Fx, Fy, hft, fq, cell, tt, hlo_p, fo, hb);
         if constexpr (S::kHalf) {
             reinterpret_cast<float *>(dst)[cell] = fo[0];
             __half *hpl = const_cast<__half *>(S::hp(dst, pitch)) + cell;
@@ -1560,7 +1579,7 @@ __device__ __forceinline__ void march2_run(const StepArgs &a, int bx, int by, lo
             velocity<false>(h2.x, jx2.x, jy2.x, ux, uy);
             grad9<R>(c1[tl], m.x, c.y, pl.x, m1[tl], m.y, pl.y, p1[tl], gpx, gpy);  // h∇p!
             const float2 F = force_fast(cc, h2.x, ux, uy, gpx, gpy);
-            collide_fast<S, false, true>(cc, h2.x, ux, uy, F.x, F.y, h2.x, nullptr, cellA, tt,
+            collide_fast<S, false, true, true>(cc, h2.x, ux, uy, F.x, F.y, h2.x, nullptr, cellA, tt,
                                          &lo2.x, foA, hbA);
         }
         {
@@ -1568,7 +1587,7 @@ __device__ __forceinline__ void march2_run(const StepArgs &a, int bx, int by, lo
             velocity<false>(h2.y, jx2.y, jy2.y, ux, uy);
             grad9<R>(c.x, m.y, c1[tr], pl.y, m.x, m1[tr], p1[tr], pl.x, gpx, gpy);
             const float2 F = force_fast(cc, h2.y, ux, uy, gpx, gpy);
-            collide_fast<S, false, true>(cc, h2.y, ux, uy, F.x, F.y, h2.y, nullptr, cellA + 1, tt,
+            collide_fast<S, false, true, true>(cc, h2.y, ux, uy, F.x, F.y, h2.y, nullptr, cellA + 1, tt,
                                          &lo2.y, foB, hbB);
         }
         reinterpret_cast<float2 *>(reinterpret_cast<float *>(dst) + cellA)[0] = f2(foA[0], foB[0]);
@@ -1812,7 +1831,7 @@ __device__ __forceinline__ void march2_alt_run(const StepArgs &a, int bx, int by
             velocity<false>(h2.x, jx2.x, jy2.x, ux, uy);
             grad9<R>(c1[tl], m.x, c.y, pl.x, m1[tl], m.y, pl.y, p1[tl], gpx, gpy);  // h∇p!
             const float2 F = force_fast(cc, h2.x, ux, uy, gpx, gpy);
-            collide_fast<S, false, true>(cc, h2.x, ux, uy, F.x, F.y, h2.x, nullptr, cellA, tt,
+            collide_fast<S, false, true, true>(cc, h2.x, ux, uy, F.x, F.y, h2.x, nullptr, cellA, tt,
                                          &lo2.x, foA, hbA);
         }
         {
@@ -1820,7 +1839,7 @@ __device__ __forceinline__ void march2_alt_run(const StepArgs &a, int bx, int by
             velocity<false>(h2.y, jx2.y, jy2.y, ux, uy);
             grad9<R>(c.x, m.y, c1[tr], pl.y, m.x, m1[tr], p1[tr], pl.x, gpx, gpy);
             const float2 F = force_fast(cc, h2.y, ux, uy, gpx, gpy);
-            collide_fast<S, false, true>(cc, h2.y, ux, uy, F.x, F.y, h2.y, nullptr, cellA + 1, tt,
+            collide_fast<S, false, true, true>(cc, h2.y, ux, uy, F.x, F.y, h2.y, nullptr, cellA + 1, tt,
                                          &lo2.y, foB, hbB);
         }
         reinterpret_cast<float2 *>(reinterpret_cast<float *>(dst) + cellA)[0] = f2(foA[0], foB[0]);
