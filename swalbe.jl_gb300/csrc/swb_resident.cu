@@ -50,14 +50,6 @@ __host__ __device__ constexpr size_t res_floats(int h) {
 // CTA raises *err and all CTAs stop at their next wait; the host re-arms the
 // words.  The counter is the multi-step barrier's top counter, which that
 // barrier also leaves at 0.
-__device__ __forceinline__ void res_arrive(unsigned int *ctr) {
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        atomicAdd(ctr, 1u);
-    }
-}
-
 __device__ __forceinline__ bool res_wait(unsigned int *ctr, int *err, unsigned int target) {
     int ok = 1;
     if (threadIdx.x == 0) {
@@ -253,10 +245,33 @@ __global__ void __launch_bounds__(NT, kResThreads / NT) resident_run_kernel(cons
                 }
             }
         }
+        // The CTA's measures and its arrival with one CTA barrier: each warp
+        // reduces its partials into red[warp]; the barrier (which also ORs
+        // the NaN flags) orders every thread's stores of this iteration
+        // before thread 0's fence; warp 0 reduces red, thread 0 adds the
+        // result to the accumulators, fences and arrives.  red is written
+        // again only after the next iteration's phase barriers.
+        if (measure) {
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) part_merge(part, part_shfl(part, off));
+            if ((t & 31) == 0) red[t >> 5] = part;
+        }
         any_nan = __syncthreads_or(any_nan);
-        if (any_nan && t == 0) a.ctl->nan_flag = 1;
-        if (measure) write_partials<NT>(a, part, tt, b, red);
-        res_arrive(a.bar);
+        if (t < 32) {
+            if (measure) {
+                PartQ q;
+                part_init(q);
+                if (t < NT / 32) q = red[t];
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) part_merge(q, part_shfl(q, off));
+                if (t == 0) add_partials(a, q, tt, b);
+            }
+            if (t == 0) {
+                if (any_nan) a.ctl->nan_flag = 1;
+                __threadfence();
+                atomicAdd(a.bar, 1u);
+            }
+        }
         // after the last iteration only the last CTA waits (to reduce it)
         if ((k + 1 < n || b == G - 1) &&
             !res_wait(a.bar, &a.ctl->bar_err, (unsigned int)(k + 1) * (unsigned int)G))

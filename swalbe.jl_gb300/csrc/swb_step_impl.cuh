@@ -685,22 +685,24 @@ __device__ __forceinline__ void write_partials(const StepArgs &a, const PartT<R>
 // FP32-arithmetic states: added by integer atomics into lane blin % 32 of the
 // iteration's accumulators (exact and order-free; fire-and-forget reductions
 // in L2, so no CTA waits).
+__device__ __forceinline__ void add_partials(const StepArgs &a, const PartQ &tot, long long t,
+                                             int blin) {  // one thread
+    unsigned long long(*acc)[kAccLanes] = a.ctl->acc[t & 1];
+    const int l = blin & (kAccLanes - 1);
+    atomicAdd(&acc[kAccMass][l], (unsigned long long)tot.mq);
+    atomicAdd(&acc[kAccWet][l], (unsigned long long)tot.wet);
+    atomicMax(&acc[kAccHmax][l], key_max(tot.hmax));
+    atomicMax(&acc[kAccHmin][l], key_min(tot.hmin));
+    if (a.meas_mask & SWB_MEAS_AREA) {
+        atomicAdd(&acc[kAccArea][l], (unsigned long long)tot.area);
+        atomicAdd(&acc[kAccCos][l], (unsigned long long)tot.cossum);
+    }
+}
 template <int NT>
 __device__ __forceinline__ void write_partials(const StepArgs &a, const PartQ &part, long long t,
                                                int blin, PartQ *red) {
     const PartQ tot = block_reduce<NT>(part, red);
-    if (threadIdx.x == 0) {
-        unsigned long long(*acc)[kAccLanes] = a.ctl->acc[t & 1];
-        const int l = blin & (kAccLanes - 1);
-        atomicAdd(&acc[kAccMass][l], (unsigned long long)tot.mq);
-        atomicAdd(&acc[kAccWet][l], (unsigned long long)tot.wet);
-        atomicMax(&acc[kAccHmax][l], key_max(tot.hmax));
-        atomicMax(&acc[kAccHmin][l], key_min(tot.hmin));
-        if (a.meas_mask & SWB_MEAS_AREA) {
-            atomicAdd(&acc[kAccArea][l], (unsigned long long)tot.area);
-            atomicAdd(&acc[kAccCos][l], (unsigned long long)tot.cossum);
-        }
-    }
+    if (threadIdx.x == 0) add_partials(a, tot, t, blin);
 }
 
 // The record of iteration s and, with the mass correction on, the
