@@ -19,7 +19,10 @@ const libswb = get(ENV, "SWALBE_GB300_LIB",
 
 # status codes and modes (include/swalbe_gb300.h)
 const SWB_OK = Cint(0)
+const SWB_ERR_ARG = Cint(-1)
 const SWB_ERR_NAN = Cint(-4)
+const SWB_ERR_NOT_FOUND = Cint(-7)
+const SWB_ERR_BUSY = Cint(-8)
 const PRECISION = Dict(Float64 => Cint(0), Float32 => Cint(1), Float16 => Cint(2))
 const SWB_PLAIN64 = Cint(3)
 const FIELD_HEIGHT, FIELD_VELX, FIELD_VELY, FIELD_PRESSURE = Cint(0), Cint(1), Cint(2), Cint(3)
@@ -315,5 +318,143 @@ Swalbe.inclination!(α::Vector, s::GB300State; t = 1000, tstart = 0, tsmooth = 1
     check(ccall((:swb_op_inclination, libswb), Cint,
                 (Ptr{Cvoid}, Cdouble, Cdouble, Int64, Int64, Int64), s.handle, α[1], α[2], t,
                 tstart, tsmooth), s.handle)
+
+# ------------------------------------------------------------------ ensembles
+"""
+    GB300Batch(systems; T = Float32)
+
+Many lattices of uneven size and parameters, advanced together by one launch
+per time step over all of them (swb_batch_*): the GPU form of a loop of
+independent simulations.  Lattice `i` (1-based) starts from height 1 until
+`set_height!` gives it a film.
+"""
+mutable struct GB300Batch
+    handle::Ptr{Cvoid}
+    systems::Vector{Swalbe.SysConst}
+end
+
+function GB300Batch(systems::AbstractVector{<:Swalbe.SysConst}; T = Float32)
+    params = [SwbParams(s) for s in systems]
+    ref = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:swb_batch_create, libswb), Cint, (Ptr{SwbParams}, Cint, Cint, Ref{Ptr{Cvoid}}),
+                params, length(params), PRECISION[T], ref), C_NULL)
+    b = GB300Batch(ref[], collect(systems))
+    finalizer(b) do x
+        x.handle == C_NULL || ccall((:swb_batch_destroy, libswb), Cint, (Ptr{Cvoid},), x.handle)
+        x.handle = C_NULL
+    end
+    return b
+end
+
+set_height!(b::GB300Batch, i::Integer, h::AbstractMatrix) =
+    check(ccall((:swb_batch_set_height, libswb), Cint, (Ptr{Cvoid}, Cint, Ptr{Float64}),
+                b.handle, i - 1, Matrix{Float64}(h)), C_NULL)
+
+function height(b::GB300Batch, i::Integer)
+    sys = b.systems[i]
+    h = zeros(sys.Lx, sys.Ly)
+    check(ccall((:swb_batch_get_height, libswb), Cint, (Ptr{Cvoid}, Cint, Ptr{Float64}),
+                b.handle, i - 1, h), C_NULL)
+    return h
+end
+
+# θ(x, t) = θ0 + Δθ sin(2π(x - v t)/Lx) for lattice i (moving wettability)
+set_theta_wave!(b::GB300Batch, i::Integer, θ0, Δθ, v) =
+    check(ccall((:swb_batch_set_theta_wave, libswb), Cint,
+                (Ptr{Cvoid}, Cint, Cdouble, Cdouble, Cdouble), b.handle, i - 1, θ0, Δθ, v), C_NULL)
+
+# strips of every lattice (default: chosen by timing real steps)
+set_geometry!(b::GB300Batch, nt::Integer, rows::Integer) =
+    check(ccall((:swb_batch_set_geometry, libswb), Cint, (Ptr{Cvoid}, Cint, Cint), b.handle, nt,
+                rows), C_NULL)
+
+function step!(b::GB300Batch, n::Integer)
+    check(ccall((:swb_batch_step, libswb), Cint, (Ptr{Cvoid}, Int64), b.handle, n), C_NULL)
+    check(ccall((:swb_batch_sync, libswb), Cint, (Ptr{Cvoid},), b.handle), C_NULL)
+end
+
+# ------------------------------------------------------------------ serving
+# swb_request_info: the same field order and C types (Int32 then padding)
+struct SwbRequestInfo
+    id::Int64
+    status::Int32
+    steps_done::Int64
+    t_submit::Float64
+    t_admit::Float64
+    t_done::Float64
+end
+
+"""
+    GB300Server(hbm_budget; T = Float32, steps_per_tick = 100)
+
+A request loop (swb_server_*): solves are admitted while their device memory
+fits `hbm_budget` bytes and advanced together, `steps_per_tick` time steps
+per scheduling tick; `submit` queues one, `poll` returns its height when it
+is done.
+"""
+mutable struct GB300Server
+    handle::Ptr{Cvoid}
+end
+
+function GB300Server(hbm_budget::Integer; T = Float32, steps_per_tick::Integer = 100)
+    ref = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:swb_server_create, libswb), Cint, (Csize_t, Cint, Cint, Ref{Ptr{Cvoid}}),
+                hbm_budget, PRECISION[T], steps_per_tick, ref), C_NULL)
+    sv = GB300Server(ref[])
+    finalizer(sv) do x
+        x.handle == C_NULL || ccall((:swb_server_destroy, libswb), Cint, (Ptr{Cvoid},), x.handle)
+        x.handle = C_NULL
+    end
+    return sv
+end
+
+# :fifo or :sjf (shortest job first), and an optional bound on resident cells
+set_policy!(sv::GB300Server, policy::Symbol; max_resident_cells::Integer = 0) =
+    check(ccall((:swb_server_set_policy, libswb), Cint, (Ptr{Cvoid}, Cint, Int64), sv.handle,
+                policy === :sjf ? 1 : 0, max_resident_cells), C_NULL)
+
+set_queue_limit!(sv::GB300Server, n::Integer) =
+    check(ccall((:swb_server_set_queue_limit, libswb), Cint, (Ptr{Cvoid}, Int64), sv.handle, n),
+          C_NULL)
+
+# strips of the resident set (nt = 0: chosen per set)
+set_geometry!(sv::GB300Server, nt::Integer = 0, rows::Integer = 0) =
+    check(ccall((:swb_server_set_geometry, libswb), Cint, (Ptr{Cvoid}, Cint, Cint), sv.handle, nt,
+                rows), C_NULL)
+
+"""
+    submit(sv, sys, h0, nsteps; θ0 = sys.param.θ, Δθ = 0, v = 0)
+
+Queues a solve of `nsteps` time steps from the film `h0` (moving wettability
+when Δθ or v is not 0).  Returns its id, or `nothing` when the queue is full.
+"""
+function submit(sv::GB300Server, sys::Swalbe.SysConst, h0::AbstractMatrix, nsteps::Integer;
+                θ0 = sys.param.θ, Δθ = 0.0, v = 0.0)
+    id = Ref{Int64}(0)
+    st = ccall((:swb_server_submit, libswb), Cint,
+               (Ptr{Cvoid}, Ref{SwbParams}, Ptr{Float64}, Cdouble, Cdouble, Cdouble, Int64,
+                Ref{Int64}), sv.handle, Ref(SwbParams(sys)), Matrix{Float64}(h0), θ0, Δθ, v,
+               nsteps, id)
+    st == SWB_ERR_BUSY && return nothing
+    check(st, C_NULL)
+    return id[]
+end
+
+"""
+    poll(sv, id, sys) -> (done, height or nothing, info)
+
+A failed or cancelled request is reported through `info.status < 0`.
+"""
+function poll(sv::GB300Server, id::Integer, sys::Swalbe.SysConst)
+    h = zeros(sys.Lx, sys.Ly)
+    info = Ref{SwbRequestInfo}()
+    st = ccall((:swb_server_poll, libswb), Cint,
+               (Ptr{Cvoid}, Int64, Ptr{Float64}, Ref{SwbRequestInfo}), sv.handle, id, h, info)
+    (st == SWB_ERR_ARG || st == SWB_ERR_NOT_FOUND) && check(st, C_NULL)
+    return st == 1, (st == 1 ? h : nothing), info[]
+end
+
+cancel!(sv::GB300Server, id::Integer) =
+    check(ccall((:swb_server_cancel, libswb), Cint, (Ptr{Cvoid}, Int64), sv.handle, id), C_NULL)
 
 end  # module

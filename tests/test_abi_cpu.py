@@ -23,6 +23,19 @@ def test_exports_every_declared_symbol(lib):
     assert missing == []
 
 
+def test_julia_binding_calls_declared_entry_points():
+    """Every entry point the Julia binding ccalls is one the header declares
+    (Julia is not installed here, so the binding itself cannot run)."""
+    import os
+    import re
+    src = open(os.path.join(os.path.dirname(L.LIB_PATH), "..", "julia", "SwalbeGB300.jl")).read()
+    called = set(re.findall(r"ccall\(\(:(\w+), libswb\)", src))
+    called |= set(re.findall(r"\(:(swb_\w+)\s*,", src))  # the per-op table
+    assert len(called) >= 30
+    declared = set(L.header_functions())
+    assert sorted(called - declared) == []
+
+
 def test_abi_version(lib):
     assert lib.swb_abi_version() == 1
 
