@@ -186,11 +186,11 @@ int balanced_rows(int Ly, int cap) {
     const int strips = (Ly + cap - 1) / cap;
     return (Ly + strips - 1) / strips;
 }
-double padded_cells(const std::vector<Req *> &set, int nt) {
+double padded_cells(const std::vector<Req *> &set, int nt, int cap) {
     const int w = -2 * nt - 4;
     double n = 0.0;
     for (const Req *r : set) {
-        const int h = balanced_rows(r->p.Ly, kServePairRows);
+        const int h = balanced_rows(r->p.Ly, cap);
         n += (double)((r->p.Lx + w - 1) / w) * (w + 4) * (double)((r->p.Ly + h - 1) / h) * (h + 4);
     }
     return n;
@@ -202,7 +202,9 @@ void choose_geometry(swb_server *sv) {
     const int cap = sv->geo_rows > 0 ? sv->geo_rows : kServePairRows;
     if (pair)
         sv->nt = sv->geo_nt != 0 ? sv->geo_nt
-                                 : (padded_cells(sv->active, -32) < padded_cells(sv->active, -64) ? -32 : -64);
+                                 : (padded_cells(sv->active, -32, cap) < padded_cells(sv->active, -64, cap)
+                                        ? -32
+                                        : -64);
     for (Req *r : sv->active) {
         const int h = pair ? balanced_rows(r->p.Ly, cap) : std::min(swb::kBatchRows, r->p.Ly);
         swb::set_geometry(r->a, sv->nt, std::max(h, swb::kMinRows));
