@@ -1420,239 +1420,16 @@ __device__ __forceinline__ __half shfl_lo_down(__half2 w) {
     return __low2half(__shfl_down_sync(0xffffffffu, w, 1));
 }
 
+// One iteration on pair strip (bx, by): thread t owns columns c = x0 - 2 + 2t
+// and c + 1 and marches the strip's rows with shared-memory rings of pairs,
+// as march_run does with one column.  Strips of odd index march up, the
+// others down (below).  Measured on GB300 (A/B on one box): the 512-member
+// ensemble 74.8k -> 78.0k MLUPS; a single 2048² lattice (one wave of strips)
+// FP32 53.3 us either way, FP16 storage 55.7 -> 54.7 us.  Results are the
+// same bits (the per-cell arithmetic and each cell's neighbours do not
+// change).
 template <class S, int NT, bool WAVE>
 __device__ __forceinline__ void march2_run(const StepArgs &a, int bx, int by, long long done,
-                                           PairSmem<NT> &sm) {
-    static_assert(!S::kLiteral && NT % 32 == 0, "pair strips: FP32 arithmetic, whole warps");
-    using R = float;
-    using PP = PairPull<S>;
-    constexpr int W = 2 * NT - 4;
-    const int t = threadIdx.x, lane = t & 31;
-    const int Lx = a.Lx, Ly = a.Ly;
-    const int H = a.march_h;
-    const int pitch = (int)a.pitch;  // 9 * pitch < 2^31 (checked at creation)
-    const long long tt = done + 1;
-    const void *src = (done & 1) ? a.fb : a.fa;
-    void *dst = (done & 1) ? a.fa : a.fb;
-    const int x0 = bx * W, y0 = by * H;
-    const int rows = min(H, Ly - y0);
-    const R gamma = R(a.gamma), hmin = R(a.hmin), hcrit = R(a.hcrit);
-    const bool tiny_y = Ly < 3;
-    auto wrow = [&](int yy) {
-        return tiny_y ? wrapc(yy, Ly) : (yy < 0 ? yy + Ly : (yy >= Ly ? yy - Ly : yy));
-    };
-    // this thread's pair (c, c + 1); x0 and Lx are even
-    const int cx = wrapc(x0 - 2 + 2 * t, Lx);
-    // κ and cospi(θ) of the two columns: the scalar θ, or θ(x, t) of the
-    // moving-wettability wave (depends on x only), as march_run computes them
-    constexpr bool wave = WAVE;
-    R kapA = R(a.kap), kapB = R(a.kap), cosA = R(a.cos_theta), cosB = R(a.cos_theta);
-    if constexpr (WAVE) {
-        const KapCos<R> wA = wave_at<R>(a, cx, tt), wB = wave_at<R>(a, cx + 1, tt);
-        kapA = wA.kap;
-        kapB = wB.kap;
-        cosA = wA.cs;
-        cosB = wB.cs;
-    }
-    const bool interior = t >= 1 && t < NT - 1 && x0 - 2 + 2 * t < Lx;
-    // lanes 0 / 31: the column and planes of the values from outside the warp
-    const bool edge = lane == 0 || lane == 31;
-    const int ecol = lane == 0 ? (cx == 0 ? Lx - 1 : cx - 1) : (cx + 2 >= Lx ? cx + 2 - Lx : cx + 2);
-    const int eq0 = lane == 0 ? 1 : 3, eq1 = lane == 0 ? 5 : 6, eq2 = lane == 0 ? 8 : 7;
-    // neighbours of the pair in a ring row of pairs, read as floats (clamped
-    // at the CTA's ends, whose values are not used)
-    const int tl = t > 0 ? 2 * t - 1 : 0, tr = t < NT - 1 ? 2 * t + 2 : 2 * NT - 1;
-
-    PP fa_, fb_;
-    auto issue = [&](PP &P, int yy) {
-        const int gy = wrow(yy);
-        const int gym = gy == 0 ? Ly - 1 : gy - 1, gyp = gy == Ly - 1 ? 0 : gy + 1;
-        const int rc = gy * Lx, rm = gym * Lx, rp = gyp * Lx;
-        P.f0 = pair_f0<S>(src, rc + cx);
-        P.q[0] = pair_ld<S>(src, pitch, 1, rc + cx);  // f1 from x - 1
-        P.q[1] = pair_ld<S>(src, pitch, 2, rm + cx);  // f2 from y - 1
-        P.q[2] = pair_ld<S>(src, pitch, 3, rc + cx);  // f3 from x + 1
-        P.q[3] = pair_ld<S>(src, pitch, 4, rp + cx);  // f4 from y + 1
-        P.q[4] = pair_ld<S>(src, pitch, 5, rm + cx);  // f5 from (x - 1, y - 1)
-        P.q[5] = pair_ld<S>(src, pitch, 6, rm + cx);  // f6 from (x + 1, y - 1)
-        P.q[6] = pair_ld<S>(src, pitch, 7, rp + cx);  // f7 from (x + 1, y + 1)
-        P.q[7] = pair_ld<S>(src, pitch, 8, rp + cx);  // f8 from (x - 1, y + 1)
-        if (edge) {
-            P.e[0] = one_ld<S>(src, pitch, eq0, rc + ecol);
-            P.e[1] = one_ld<S>(src, pitch, eq1, rm + ecol);
-            P.e[2] = one_ld<S>(src, pitch, eq2, rp + ecol);
-        }
-    };
-    auto consume = [&](const PP &P, int yy) {
-        const int r = yy - y0 + 2;  // >= 0
-        // the halves of the x-pulled planes that come from the neighbouring pairs
-        auto l1 = shfl_hi_up(P.q[0]), l5 = shfl_hi_up(P.q[4]), l8 = shfl_hi_up(P.q[7]);
-        auto r3 = shfl_lo_down(P.q[2]), r6 = shfl_lo_down(P.q[5]), r7 = shfl_lo_down(P.q[6]);
-        if (lane == 0) {
-            l1 = P.e[0];
-            l5 = P.e[1];
-            l8 = P.e[2];
-        }
-        if (lane == 31) {
-            r3 = P.e[0];
-            r6 = P.e[1];
-            r7 = P.e[2];
-        }
-        float2 F[9];
-        F[0] = P.f0;
-        F[1] = left_pull(l1, P.q[0]);
-        F[2] = pair_val(P.q[1]);
-        F[3] = right_pull(P.q[2], r3);
-        F[4] = pair_val(P.q[3]);
-        F[5] = left_pull(l5, P.q[4]);
-        F[6] = right_pull(P.q[5], r6);
-        F[7] = right_pull(P.q[6], r7);
-        F[8] = left_pull(l8, P.q[7]);
-        R fA[9], fB[9];
-#pragma unroll
-        for (int q = 0; q < 9; ++q) {
-            fA[q] = F[q].x;
-            fB[q] = F[q].y;
-        }
-        R hA, jxA, jyA, hB, jxB, jyB;
-        moments9<false>(fA, hA, jxA, jyA);
-        moments9<false>(fB, hB, jxB, jyB);
-        sm.h[r & 7][t] = f2(hA, hB);
-        sm.jx[r & 3][t] = f2(jxA, jxB);
-        sm.jy[r & 3][t] = f2(jyA, jyB);
-        sm.lo[r & 3][t] = f2(moments_lo(fA, hA), moments_lo(fB, hB));
-    };
-    auto pressure_row = [&](int yy) {
-        const int r = yy - y0 + 2;  // >= 1
-        const float2 *hm = sm.h[(r + 7) & 7], *hc = sm.h[r & 7], *hp = sm.h[(r + 1) & 7];
-        const float2 m = hm[t], c = hc[t], pl = hp[t];
-        const float *m1 = reinterpret_cast<const float *>(hm), *c1 = reinterpret_cast<const float *>(hc),
-                    *p1 = reinterpret_cast<const float *>(hp);
-        // ip = h[i-1,j], jp = h[i,j-1], im = h[i+1,j], jm = h[i,j+1], ...
-        const R pA = pressure_cell<false, R>(c.x, c1[tl], m.x, c.y, pl.x, m1[tl], m.y, pl.y, p1[tl],
-                                             kapA, gamma, hmin, hcrit, a.n, a.m);
-        const R pB = pressure_cell<false, R>(c.y, c.x, m.y, c1[tr], pl.y, m.x, m1[tr], p1[tr], pl.x,
-                                             kapB, gamma, hmin, hcrit, a.n, a.m);
-        sm.p[r & 3][t] = f2(pA, pB);
-    };
-
-    issue(fa_, y0 - 2);
-    issue(fb_, y0 - 1);
-    consume(fa_, y0 - 2);
-    issue(fa_, y0);
-    consume(fb_, y0 - 1);
-    issue(fb_, y0 + 1);
-    consume(fa_, y0);
-    issue(fa_, y0 + 2);
-    consume(fb_, y0 + 1);
-    __syncthreads();
-    pressure_row(y0 - 1);
-    pressure_row(y0);
-
-    const CellConst<R> cc = cell_consts<R>(a, tt, a.mass_corr ? __ldcg(&a.ctl->corr[tt & 1]) : 0.0);
-    const R thr = R(a.hthresh);
-    const bool measure = a.meas_mask || a.mass_corr;
-    PartQ part;
-    part_init(part);
-    int any_nan = 0;
-
-#pragma unroll 1
-    for (int j = 0; j < rows; ++j) {
-        const int y = y0 + j;
-        consume(fa_, y + 2);
-        if (j + 1 < rows) issue(fa_, y + 3);  // one row ahead
-        __syncthreads();
-        pressure_row(y + 1);
-        __syncthreads();
-        if (!interior) continue;
-        // ---- output row y, columns cx, cx + 1 ----
-        const int r = y - y0 + 2;
-        const int cellA = wrow(y) * Lx + cx;
-        const float2 h2 = sm.h[r & 7][t], jx2 = sm.jx[r & 3][t], jy2 = sm.jy[r & 3][t];
-        const float2 lo2 = sm.lo[r & 3][t];
-        const float2 *pm = sm.p[(r + 3) & 3], *pc = sm.p[r & 3], *pp = sm.p[(r + 1) & 3];
-        const float2 m = pm[t], c = pc[t], pl = pp[t];
-        const float *m1 = reinterpret_cast<const float *>(pm), *c1 = reinterpret_cast<const float *>(pc),
-                    *p1 = reinterpret_cast<const float *>(pp);
-        float foA[9], foB[9];
-        [[maybe_unused]] __half2 hbA[4], hbB[4];
-        {
-            R ux, uy, gpx, gpy;
-            velocity<false>(h2.x, jx2.x, jy2.x, ux, uy);
-            grad9<R>(c1[tl], m.x, c.y, pl.x, m1[tl], m.y, pl.y, p1[tl], gpx, gpy);  // h∇p!
-            const float2 F = force_fast(cc, h2.x, ux, uy, gpx, gpy);
-            collide_fast<S, false, true, true>(cc, h2.x, ux, uy, F.x, F.y, h2.x, nullptr, cellA, tt,
-                                         &lo2.x, foA, hbA);
-        }
-        {
-            R ux, uy, gpx, gpy;
-            velocity<false>(h2.y, jx2.y, jy2.y, ux, uy);
-            grad9<R>(c.x, m.y, c1[tr], pl.y, m.x, m1[tr], p1[tr], pl.x, gpx, gpy);
-            const float2 F = force_fast(cc, h2.y, ux, uy, gpx, gpy);
-            collide_fast<S, false, true, true>(cc, h2.y, ux, uy, F.x, F.y, h2.y, nullptr, cellA + 1, tt,
-                                         &lo2.y, foB, hbB);
-        }
-        reinterpret_cast<float2 *>(reinterpret_cast<float *>(dst) + cellA)[0] = f2(foA[0], foB[0]);
-        if constexpr (S::kHalf) {
-            __half2 *hpl = reinterpret_cast<__half2 *>(const_cast<__half *>(S::hp(dst, pitch)) + cellA);
-            const int pitch2 = pitch >> 1;  // pitch in pairs (pitch is a multiple of 64)
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                hpl[(2 * k) * pitch2] = __lows2half2(hbA[k], hbB[k]);
-                hpl[(2 * k + 1) * pitch2] = __highs2half2(hbA[k], hbB[k]);
-            }
-        } else {
-            float2 *d2 = reinterpret_cast<float2 *>(reinterpret_cast<float *>(dst) + cellA);
-            const int pitch2 = pitch >> 1;
-#pragma unroll
-            for (int q = 1; q < 9; ++q) d2[q * pitch2] = f2(foA[q], foB[q]);
-        }
-        // measures of the heights at the start of this iteration
-        if (!isfinite(h2.x) || !isfinite(h2.y)) any_nan = 1;
-        if (measure) {
-            mass_add(part, h2.x);
-            mass_add(part, h2.y);
-            mass_add_lo(part, lo2.x);
-            mass_add_lo(part, lo2.y);
-            const bool wA = h2.x > thr, wB = h2.y > thr;
-            part.wet += (wA ? 1 : 0) + (wB ? 1 : 0);
-            part.hmax = fmaxf(part.hmax, fmaxf(h2.x, h2.y));
-            part.hmin = fminf(part.hmin, fminf(h2.x, h2.y));
-            if ((a.meas_mask & SWB_MEAS_AREA) && (wA || wB)) {
-                const float2 *hm = sm.h[(r + 7) & 7], *hc = sm.h[r & 7], *hp = sm.h[(r + 1) & 7];
-                const float2 hm2 = hm[t], hp2 = hp[t];
-                const float *hm1 = reinterpret_cast<const float *>(hm),
-                            *hc1 = reinterpret_cast<const float *>(hc),
-                            *hp1 = reinterpret_cast<const float *>(hp);
-                R gx2, gy2;
-                if (wA) {
-                    grad9<R>(hc1[tl], hm2.x, h2.y, hp2.x, hm1[tl], hm2.y, hp2.y, hp1[tl], gx2, gy2);
-                    area_add(part, R(sqrt(gx2 * gx2 + gy2 * gy2 + R(1))));
-                    if constexpr (wave) cos_add(part, cosA);
-                }
-                if (wB) {
-                    grad9<R>(h2.x, hm2.y, hc1[tr], hp2.y, hm2.x, hm1[tr], hp1[tr], hp2.x, gx2, gy2);
-                    area_add(part, R(sqrt(gx2 * gx2 + gy2 * gy2 + R(1))));
-                    if constexpr (wave) cos_add(part, cosB);
-                }
-            }
-        }
-    }
-    grid_dep_launch();
-    any_nan = __syncthreads_or(any_nan);
-    if (any_nan && t == 0) a.ctl->nan_flag = 1;
-    if (measure) write_partials<NT>(a, part, tt, by * a.tiles_x + bx, sm.red);
-}
-
-// march2_run with alternating march directions, for the batch kernel.
-// Measured on GB300 (the same box, A/B): the 512-member ensemble (one CTA
-// per strip, about 17 waves of strips) 74.8k -> 78.0k MLUPS.  It is a
-// separate function because folding the alternation into march2_run, even
-// switched off by a template flag, made the compiled one-lattice pair kernel
-// slower (2048²: 53.3 -> 55.2 us per iteration).  Results are the same bits
-// (the per-cell arithmetic and each cell's neighbours do not change).
-template <class S, int NT, bool WAVE>
-__device__ __forceinline__ void march2_alt_run(const StepArgs &a, int bx, int by, long long done,
                                            PairSmem<NT> &sm) {
     static_assert(!S::kLiteral && NT % 32 == 0, "pair strips: FP32 arithmetic, whole warps");
     using R = float;
@@ -2330,9 +2107,9 @@ __global__ void __launch_bounds__(NT, (batch_pair_min_blocks<NT, WAVE>())) batch
         const long long done = sa.ctl->step_base + k;
         if (tr.tx >= 0) {
             if (WAVE && sa.theta_mode == THETA_WAVE) {
-                march2_alt_run<S, NT, WAVE>(sa, tr.tx, tr.ty, done, sm);
+                march2_run<S, NT, WAVE>(sa, tr.tx, tr.ty, done, sm);
             } else {
-                march2_alt_run<S, NT, false>(sa, tr.tx, tr.ty, done, sm);
+                march2_run<S, NT, false>(sa, tr.tx, tr.ty, done, sm);
             }
         } else if (k > 0 && done <= sa.stop_at) {
             reduce_step<NT>(sa, done, sm.redd);
