@@ -3,8 +3,8 @@ past the device ring's capacity.
 
 * Rayleigh–Taylor film, 512² (g = -0.001, γ = 0.0005, θ = 1/9, h0 = 1 +
   U[-0.01, 0.01], seed 2), 2000 steps with the Δh series: Float64 bit-exact
-  against the oracle; FP32 within 1e-4 relative L2 of h (the north-star
-  tolerance of the FP32 mode).
+  against the oracle; FP32 within 1e-4 relative L2 of h (the tolerance of
+  the FP32 mode).
 * Coalescence ensemble: two members of each lattice size (128², 256², 512²,
   1024x256) from the seeded ensemble, through one Batch: FP32 equal to the
   same members run alone, Float64 bit-exact against the oracle.
